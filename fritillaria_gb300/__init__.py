@@ -1,0 +1,595 @@
+"""GB300-native BGZF -> device columns.
+
+A Python mirror of the reference's surface for this path, over the C ABI in
+``include/frt.h`` (``libfrt_gb300.so``):
+
+  * :class:`CudaCodec` -- ``CudaCodec`` as ``BlockCodec`` / ``DeviceBlockCodec``
+    (crates/fritillaria-cuda/src/lib.rs:152-293);
+  * :func:`select_codec` / :class:`Backend` (crates/fritillaria/src/lib.rs:151-260);
+  * :class:`DeviceBgzfReader` -- ``next_batch`` / ``carry_from``
+    (crates/fritillaria-bgzf/src/device_read.rs:57-280);
+  * :class:`BamDecoder` / :class:`DeviceRecordBatch` -- ``decode`` / ``tail``
+    (crates/fritillaria-cuda/src/bam.rs:113-187, crates/fritillaria-bam/src/columnar/device.rs);
+  * :class:`BatchEngine` -- the batched, device-resident form.
+
+There is no CPU fallback: if the library or a GB300 is missing, constructors
+raise.  Device memory, streams and events belong to the CUDA runtime the
+library links; torch is only used by callers that want tensors.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import re
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libfrt_gb300.so"
+HEADER = _PKG.parent / "include" / "frt.h"
+
+# ---------------------------------------------------------------------------
+# errors (crates/fritillaria-core/src/error.rs:14-67)
+# ---------------------------------------------------------------------------
+
+
+class FrtError(Exception):
+    code = -1
+
+    def __init__(self, err=None, message: str | None = None):
+        if err is not None:
+            self.offset = err.offset
+            self.expected = err.expected
+            self.actual = err.actual
+            self.position = err.position
+            self.format = err.format.decode(errors="replace")
+            self.reason = err.reason.decode(errors="replace")
+        else:
+            self.offset = self.expected = self.actual = self.position = 0
+            self.format = ""
+            self.reason = message or ""
+        super().__init__(self._describe())
+
+    def _describe(self):
+        return self.reason
+
+
+class IoError(FrtError):
+    code = 1
+
+
+class InvalidBlock(FrtError):
+    code = 2
+
+    def _describe(self):
+        return f"invalid BGZF block at offset {self.offset}: {self.reason}"
+
+
+class ChecksumMismatch(FrtError):
+    code = 3
+
+    def _describe(self):
+        return (f"checksum mismatch in block at offset {self.offset}: expected crc32 {self.expected:#010x}, "
+                f"got {self.actual:#010x}")
+
+
+class SizeMismatch(FrtError):
+    code = 4
+
+    def _describe(self):
+        return (f"size mismatch in block at offset {self.offset}: ISIZE says {self.expected} bytes, "
+                f"inflated {self.actual}")
+
+
+class InflateError(FrtError):
+    code = 5
+
+    def _describe(self):
+        return f"inflate failed for block at offset {self.offset}: {self.reason}"
+
+
+class Malformed(FrtError):
+    code = 6
+
+    def _describe(self):
+        return f"malformed {self.format} at position {self.position}: {self.reason}"
+
+
+class InvalidDeviceBatch(FrtError):
+    code = 7
+
+
+class CudaUnavailable(FrtError):
+    code = 8
+
+
+class CudaError(FrtError):
+    code = 9
+
+
+class InvalidArgument(FrtError):
+    code = 10
+
+
+_ERRORS = {c.code: c for c in (IoError, InvalidBlock, ChecksumMismatch, SizeMismatch, InflateError, Malformed,
+                               InvalidDeviceBatch, CudaUnavailable, CudaError, InvalidArgument)}
+
+
+class _Err(C.Structure):
+    _fields_ = [("code", C.c_int32), ("offset", C.c_uint64), ("expected", C.c_uint64), ("actual", C.c_uint64),
+                ("position", C.c_uint64), ("format", C.c_char * 16), ("reason", C.c_char * 200)]
+
+
+class Span(C.Structure):
+    """BlockSpan (crates/fritillaria-core/src/codec.rs:17-41)."""
+    _fields_ = [("compressed_offset", C.c_uint64), ("payload_start", C.c_uint64), ("payload_len", C.c_uint64),
+                ("isize", C.c_uint32), ("crc32", C.c_uint32)]
+
+
+SPAN_DTYPE = np.dtype([("compressed_offset", "<u8"), ("payload_start", "<u8"), ("payload_len", "<u8"),
+                       ("isize", "<u4"), ("crc32", "<u4")])
+
+
+class EngineConfig(C.Structure):
+    _fields_ = [("warps_per_cta", C.c_uint32), ("queue_chunk", C.c_uint32), ("use_graph", C.c_uint32),
+                ("sort_queue", C.c_uint32)]
+
+
+class EngineStats(C.Structure):
+    _fields_ = [("members", C.c_uint64), ("compressed_bytes", C.c_uint64), ("inflated_bytes", C.c_uint64),
+                ("records", C.c_uint64), ("tail", C.c_uint64), ("aux_fields", C.c_uint64),
+                ("fallbacks", C.c_uint64), ("status", C.c_int32), ("error_member", C.c_uint32)]
+
+
+def _raise(rc: int, err: _Err):
+    if rc:
+        raise _ERRORS.get(rc, FrtError)(err)
+
+
+_lib = None
+_P = C.c_void_p
+
+
+def header_functions() -> list[str]:
+    """Every function `include/frt.h` declares."""
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"\b(frt_[a-z0-9_]+)\s*\(", text)
+    seen = []
+    for n in names:
+        if n not in seen and n != "frt_read_fn":
+            seen.append(n)
+    return seen
+
+
+def lib():
+    """The native library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`"
+                           " (there is no CPU fallback)")
+    L = C.CDLL(str(LIB_PATH))
+    sig = {
+        "frt_cuda_is_usable": (C.c_int, []),
+        "frt_select_codec": (C.c_int, [C.c_int, _P, _P, _P]),
+        "frt_codec_create": (C.c_int, [C.c_int, _P, _P, _P]),
+        "frt_codec_destroy": (None, [_P]),
+        "frt_codec_name": (C.c_char_p, [_P]),
+        "frt_codec_device_ordinal": (C.c_int, [_P]),
+        "frt_codec_stream": (_P, [_P]),
+        "frt_codec_inflate_batch_device": (C.c_int, [_P, _P, C.c_size_t, _P, C.c_size_t, _P, _P]),
+        "frt_codec_inflate_batch_host": (C.c_int, [_P, _P, C.c_size_t, _P, C.c_size_t, _P, C.c_size_t, _P, _P]),
+        "frt_codec_crc32_device": (C.c_int, [_P, _P, _P, _P, C.c_size_t, _P, _P]),
+        "frt_inflate_batch_len": (C.c_size_t, [_P]),
+        "frt_inflate_batch_byte_len": (C.c_size_t, [_P]),
+        "frt_inflate_batch_data": (_P, [_P]),
+        "frt_inflate_batch_offsets": (C.POINTER(C.c_uint64), [_P]),
+        "frt_inflate_batch_compressed_offsets": (C.POINTER(C.c_uint64), [_P]),
+        "frt_inflate_batch_device_ordinal": (C.c_int, [_P]),
+        "frt_inflate_batch_ready_event": (_P, [_P]),
+        "frt_inflate_batch_to_host": (C.c_int, [_P, _P, C.c_size_t, _P]),
+        "frt_inflate_batch_free": (None, [_P]),
+        "frt_reader_open_memory": (C.c_int, [_P, C.c_size_t, _P, _P, _P]),
+        "frt_reader_open_path": (C.c_int, [C.c_char_p, _P, _P, _P]),
+        "frt_reader_set_blocks_per_batch": (None, [_P, C.c_size_t]),
+        "frt_reader_next_batch": (C.c_int, [_P, _P, _P, _P, _P]),
+        "frt_reader_carry_from": (C.c_int, [_P, C.c_uint64, _P]),
+        "frt_reader_codec_name": (C.c_char_p, [_P]),
+        "frt_reader_device_ordinal": (C.c_int, [_P]),
+        "frt_reader_close": (None, [_P]),
+        "frt_bgzf_discover": (C.c_int, [_P, C.c_size_t, C.c_uint64, _P, C.c_size_t, _P, _P, _P]),
+        "frt_bam_decoder_create": (C.c_int, [C.c_int, _P, _P, _P]),
+        "frt_bam_decoder_set_reference_count": (None, [_P, C.c_int32]),
+        "frt_bam_decoder_destroy": (None, [_P]),
+        "frt_bam_decode": (C.c_int, [_P, _P, C.c_uint64, _P, _P]),
+        "frt_bam_decoder_last_fallbacks": (C.c_uint64, [_P]),
+        "frt_record_batch_len": (C.c_uint64, [_P]),
+        "frt_record_batch_tail": (C.c_uint64, [_P]),
+        "frt_record_batch_aux_fields": (C.c_uint64, [_P]),
+        "frt_record_batch_device_ordinal": (C.c_int, [_P]),
+        "frt_record_batch_column": (C.c_int, [_P, C.c_int, _P, _P, _P]),
+        "frt_record_batch_column_to_host": (C.c_int, [_P, C.c_int, _P, C.c_size_t, _P]),
+        "frt_record_batch_ready_event": (_P, [_P]),
+        "frt_record_batch_free": (None, [_P]),
+        "frt_engine_create": (C.c_int, [C.c_int, _P, _P, _P, _P]),
+        "frt_engine_destroy": (None, [_P]),
+        "frt_engine_bind_bam": (C.c_int, [_P, _P, C.c_size_t, _P]),
+        "frt_engine_run": (C.c_int, [_P, _P]),
+        "frt_engine_finish": (C.c_int, [_P, _P, _P]),
+        "frt_engine_run_host": (C.c_int, [_P, _P, C.c_size_t, _P, _P]),
+        "frt_engine_column": (C.c_int, [_P, C.c_int, _P, _P, _P]),
+        "frt_engine_inflated": (_P, [_P, _P]),
+    }
+    for name, (res, args) in sig.items():
+        if hasattr(L, name):
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+    _lib = L
+    return L
+
+
+def cuda_is_usable() -> bool:
+    """cuda_is_usable (crates/fritillaria/src/lib.rs:183-186)."""
+    try:
+        return bool(lib().frt_cuda_is_usable())
+    except RuntimeError:
+        return False
+
+
+class Backend(enum.IntEnum):
+    """Backend (crates/fritillaria/src/lib.rs:151-176)."""
+    AUTO = 0
+    CPU = 1
+    CUDA = 2
+    NVCOMP = 3
+
+
+def _u8(data) -> np.ndarray:
+    if isinstance(data, np.ndarray):
+        return np.ascontiguousarray(data).view(np.uint8).reshape(-1)
+    return np.frombuffer(bytes(data), dtype=np.uint8)
+
+
+# ---------------------------------------------------------------------------
+# codec
+# ---------------------------------------------------------------------------
+class CudaCodec:
+    """CudaCodec: inflate BGZF members on the GB300, CRC32 + ISIZE verified."""
+
+    def __init__(self, device: int = 0, stream: int | None = None, _handle=None):
+        L = lib()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            h = _P()
+            err = _Err()
+            _raise(L.frt_codec_create(device, stream, C.byref(h), C.byref(err)), err)
+            self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def name(self) -> str:
+        return lib().frt_codec_name(self._h).decode()
+
+    def device_ordinal(self) -> int:
+        return lib().frt_codec_device_ordinal(self._h)
+
+    @property
+    def stream(self) -> int:
+        return lib().frt_codec_stream(self._h) or 0
+
+    def inflate_batch_device(self, batch, spans) -> "DeviceInflateBatch":
+        """DeviceBlockCodec::inflate_batch_device."""
+        b = _u8(batch)
+        s = np.ascontiguousarray(spans, dtype=SPAN_DTYPE)
+        out = _P()
+        err = _Err()
+        _raise(lib().frt_codec_inflate_batch_device(self._h, b.ctypes.data, b.size, s.ctypes.data, len(s),
+                                                    C.byref(out), C.byref(err)), err)
+        return DeviceInflateBatch(out)
+
+    def inflate_batch(self, batch, spans):
+        """BlockCodec::inflate_batch: (bytes, offsets) on the host."""
+        b = _u8(batch)
+        s = np.ascontiguousarray(spans, dtype=SPAN_DTYPE)
+        total = int(s["isize"].astype(np.uint64).sum())
+        out = np.empty(total + 1, dtype=np.uint8)
+        offs = np.empty(len(s) + 1, dtype=np.uint64)
+        err = _Err()
+        _raise(lib().frt_codec_inflate_batch_host(self._h, b.ctypes.data, b.size, s.ctypes.data, len(s),
+                                                  out.ctypes.data, out.size, offs.ctypes.data, C.byref(err)), err)
+        return out[:total], offs
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.frt_codec_destroy(h)
+            self._h = None
+
+
+def select_codec(backend: Backend = Backend.AUTO):
+    """select_codec: (codec, resolved backend).  No CPU fallback."""
+    h = _P()
+    resolved = C.c_int()
+    err = _Err()
+    _raise(lib().frt_select_codec(int(backend), C.byref(h), C.byref(resolved), C.byref(err)), err)
+    return CudaCodec(_handle=h), Backend(resolved.value)
+
+
+def discover_blocks(data, base_offset: int = 0):
+    """BGZF member spans (host walk, discover.rs:51-109) and bytes consumed."""
+    b = _u8(data)
+    cap = b.size // 28 + 2
+    spans = np.zeros(cap, dtype=SPAN_DTYPE)
+    n = C.c_size_t()
+    used = C.c_size_t()
+    err = _Err()
+    _raise(lib().frt_bgzf_discover(b.ctypes.data, b.size, base_offset, spans.ctypes.data, cap, C.byref(n),
+                                   C.byref(used), C.byref(err)), err)
+    return spans[: n.value].copy(), used.value
+
+
+class DeviceInflateBatch:
+    """DeviceInflateBatch: inflated bytes on the device plus member offsets."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @property
+    def handle(self):
+        return self._h
+
+    def __len__(self):
+        return lib().frt_inflate_batch_len(self._h)
+
+    def byte_len(self) -> int:
+        return lib().frt_inflate_batch_byte_len(self._h)
+
+    def data_ptr(self) -> int:
+        return lib().frt_inflate_batch_data(self._h) or 0
+
+    def offsets(self) -> np.ndarray:
+        n = len(self) + 1
+        p = lib().frt_inflate_batch_offsets(self._h)
+        return np.ctypeslib.as_array(p, shape=(n,)).copy()
+
+    def compressed_offsets(self) -> np.ndarray:
+        n = len(self)
+        if n == 0:
+            return np.zeros(0, dtype=np.uint64)
+        p = lib().frt_inflate_batch_compressed_offsets(self._h)
+        return np.ctypeslib.as_array(p, shape=(n,)).copy()
+
+    def device_ordinal(self) -> int:
+        return lib().frt_inflate_batch_device_ordinal(self._h)
+
+    def ready_event(self) -> int:
+        return lib().frt_inflate_batch_ready_event(self._h) or 0
+
+    def to_host(self) -> np.ndarray:
+        out = np.empty(self.byte_len(), dtype=np.uint8)
+        err = _Err()
+        _raise(lib().frt_inflate_batch_to_host(self._h, out.ctypes.data, out.size, C.byref(err)), err)
+        return out
+
+    def free(self):
+        if self._h and _lib is not None:
+            _lib.frt_inflate_batch_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        self.free()
+
+
+class DeviceBatch:
+    """DeviceBatch {data, start} (device_read.rs:47-56)."""
+
+    def __init__(self, data: DeviceInflateBatch, start: int):
+        self.data = data
+        self.start = start
+
+
+class DeviceBgzfReader:
+    """DeviceBgzfReader over a file path, bytes or a numpy buffer."""
+
+    def __init__(self, source, codec: CudaCodec, blocks_per_batch: int | None = None):
+        self._codec = codec  # must outlive the reader
+        h = _P()
+        err = _Err()
+        if isinstance(source, (str, Path)):
+            rc = lib().frt_reader_open_path(str(source).encode(), codec.handle, C.byref(h), C.byref(err))
+            self._src = None
+        else:
+            self._src = _u8(source)
+            rc = lib().frt_reader_open_memory(self._src.ctypes.data, self._src.size, codec.handle, C.byref(h),
+                                              C.byref(err))
+        _raise(rc, err)
+        self._h = h
+        if blocks_per_batch is not None:
+            self.with_blocks_per_batch(blocks_per_batch)
+
+    def with_blocks_per_batch(self, blocks: int) -> "DeviceBgzfReader":
+        lib().frt_reader_set_blocks_per_batch(self._h, max(0, int(blocks)))
+        return self
+
+    def codec_name(self) -> str:
+        return lib().frt_reader_codec_name(self._h).decode()
+
+    def device_ordinal(self) -> int:
+        return lib().frt_reader_device_ordinal(self._h)
+
+    def next_batch(self) -> DeviceBatch | None:
+        out = _P()
+        start = C.c_uint64()
+        has = C.c_int()
+        err = _Err()
+        _raise(lib().frt_reader_next_batch(self._h, C.byref(out), C.byref(start), C.byref(has), C.byref(err)), err)
+        if not has.value:
+            return None
+        return DeviceBatch(DeviceInflateBatch(out), start.value)
+
+    def carry_from(self, tail: int) -> None:
+        err = _Err()
+        _raise(lib().frt_reader_carry_from(self._h, int(tail), C.byref(err)), err)
+
+    def __iter__(self):
+        while True:
+            b = self.next_batch()
+            if b is None:
+                return
+            yield b
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.frt_reader_close(h)
+            self._h = None
+
+
+# Column ids (frt_bam_column) and dtypes.
+BAM_COLUMNS = {
+    "ref_id": (0, np.int32), "pos": (1, np.int32), "flags": (2, np.uint16), "mapq": (3, np.uint8),
+    "seq_len": (4, np.uint32), "mate_ref_id": (5, np.int32), "mate_pos": (6, np.int32), "tlen": (7, np.int32),
+    "record_offsets": (8, np.uint64), "cigar_start": (9, np.uint32), "sequence_start": (10, np.uint32),
+    "quality_start": (11, np.uint32), "aux_start": (12, np.uint32), "record_end": (13, np.uint32),
+    "bin": (14, np.uint16), "n_cigar": (15, np.uint16), "name_len": (16, np.uint8),
+    "virtual_offset": (17, np.uint64), "aux_count": (18, np.uint32), "aux_status": (19, np.uint8),
+    "aux_first": (20, np.uint32),
+}
+AUX_DTYPE = np.dtype([("tag", "u1", (2,)), ("type", "u1"), ("subtype", "u1"), ("value_offset", "<u4"),
+                      ("count", "<u4")])
+
+
+class BamDecoder:
+    """BamDecoder: record boundaries and columns on device."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        h = _P()
+        err = _Err()
+        _raise(lib().frt_bam_decoder_create(device, stream, C.byref(h), C.byref(err)), err)
+        self._h = h
+
+    def set_reference_count(self, n_ref: int) -> "BamDecoder":
+        lib().frt_bam_decoder_set_reference_count(self._h, int(n_ref))
+        return self
+
+    def decode(self, batch: DeviceInflateBatch | None, start: int) -> "DeviceRecordBatch":
+        out = _P()
+        err = _Err()
+        _raise(lib().frt_bam_decode(self._h, batch.handle if batch is not None else None, int(start), C.byref(out),
+                                    C.byref(err)), err)
+        return DeviceRecordBatch(out)
+
+    def last_fallbacks(self) -> int:
+        return lib().frt_bam_decoder_last_fallbacks(self._h)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.frt_bam_decoder_destroy(h)
+            self._h = None
+
+
+class DeviceRecordBatch:
+    """DeviceRecordBatch: device columns; keeps its inflate batch alive."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    def __len__(self):
+        return lib().frt_record_batch_len(self._h)
+
+    def tail(self) -> int:
+        return lib().frt_record_batch_tail(self._h)
+
+    def aux_fields(self) -> int:
+        return lib().frt_record_batch_aux_fields(self._h)
+
+    def device_ordinal(self) -> int:
+        return lib().frt_record_batch_device_ordinal(self._h)
+
+    def column_ptr(self, name: str):
+        cid = BAM_COLUMNS[name][0] if name != "aux_entries" else 21
+        p = _P()
+        nb = C.c_size_t()
+        w = C.c_size_t()
+        lib().frt_record_batch_column(self._h, cid, C.byref(p), C.byref(nb), C.byref(w))
+        return p.value or 0, nb.value, w.value
+
+    def column(self, name: str) -> np.ndarray:
+        if name == "aux_entries":
+            cid, dt = 21, AUX_DTYPE
+        else:
+            cid, dt = BAM_COLUMNS[name]
+        _, nb, _ = self.column_ptr(name)
+        out = np.empty(nb // np.dtype(dt).itemsize, dtype=dt)
+        err = _Err()
+        _raise(lib().frt_record_batch_column_to_host(self._h, cid, out.ctypes.data, out.nbytes, C.byref(err)), err)
+        return out
+
+    def to_host(self) -> dict:
+        return {name: self.column(name) for name in BAM_COLUMNS}
+
+    def free(self):
+        if self._h and _lib is not None:
+            _lib.frt_record_batch_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        self.free()
+
+
+class BatchEngine:
+    """The batched form: a whole BGZF BAM resident on the device, inflated,
+    verified, scanned and decoded by persistent kernels fed from a device work
+    queue, the steady state replayed as a CUDA graph."""
+
+    def __init__(self, device: int = 0, stream: int | None = None, warps_per_cta: int = 0, queue_chunk: int = 0,
+                 use_graph: bool = True, sort_queue: bool = True):
+        cfg = EngineConfig(warps_per_cta, queue_chunk, int(use_graph), int(sort_queue))
+        h = _P()
+        err = _Err()
+        _raise(lib().frt_engine_create(device, stream, C.byref(cfg), C.byref(h), C.byref(err)), err)
+        self._h = h
+
+    def bind_bam(self, dev_ptr: int, length: int) -> None:
+        err = _Err()
+        _raise(lib().frt_engine_bind_bam(self._h, dev_ptr, length, C.byref(err)), err)
+
+    def run(self) -> None:
+        err = _Err()
+        _raise(lib().frt_engine_run(self._h, C.byref(err)), err)
+
+    def finish(self) -> EngineStats:
+        st = EngineStats()
+        err = _Err()
+        _raise(lib().frt_engine_finish(self._h, C.byref(st), C.byref(err)), err)
+        return st
+
+    def run_host(self, data) -> EngineStats:
+        b = _u8(data)
+        st = EngineStats()
+        err = _Err()
+        _raise(lib().frt_engine_run_host(self._h, b.ctypes.data, b.size, C.byref(st), C.byref(err)), err)
+        return st
+
+    def column_ptr(self, name: str):
+        cid = BAM_COLUMNS[name][0] if name != "aux_entries" else 21
+        p = _P()
+        nb = C.c_size_t()
+        w = C.c_size_t()
+        lib().frt_engine_column(self._h, cid, C.byref(p), C.byref(nb), C.byref(w))
+        return p.value or 0, nb.value, w.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.frt_engine_destroy(h)
+            self._h = None

@@ -1,0 +1,47 @@
+// BAM record scan / decode kernels: constants and the column pointer block.
+#pragma once
+
+#include "common.cuh"
+
+// Record offsets stored per member during the scan.  A record occupies at
+// least 36 bytes, so a member of at most 65,536 inflated bytes holds at most
+// 1,821 record starts.
+#define FRT_SCAN_CAP 1824
+
+struct FrtBamColumnsDev {
+    int *ref_id;
+    int *pos;
+    u16 *flags;
+    u8 *mapq;
+    u32 *seq_len;
+    int *mate_ref_id;
+    int *mate_pos;
+    int *tlen;
+    u64 *record_offsets;
+    u32 *cigar_start;
+    u32 *sequence_start;
+    u32 *quality_start;
+    u32 *aux_start;
+    u32 *record_end;
+    u16 *bin;
+    u16 *n_cigar;
+    u8 *name_len;
+    u64 *virtual_offset;
+    u32 *aux_count;
+    u8 *aux_status;
+};
+
+
+cudaError_t frt_launch_bam_spec(const u8 *buf, u64 len, const u64 *starts, u32 n, u64 start, int n_ref, u64 *entry,
+                                u32 *count, u64 *land, u8 *flags, u16 *scratch, cudaStream_t s);
+cudaError_t frt_launch_bam_reconcile(const u8 *buf, u64 len, const u64 *starts, u32 n, u64 start, u64 *entry,
+                                     u32 *count, u64 *land, u8 *flags, u16 *scratch, u32 *first_index, u64 *totals,
+                                     cudaStream_t s);
+cudaError_t frt_launch_bam_decode(const u8 *buf, const u64 *starts, const u64 *coff, u32 n, const u32 *count,
+                                  const u32 *first_index, const u16 *scratch, const FrtBamColumnsDev &c,
+                                  cudaStream_t s);
+size_t frt_scan_partials_len(u64 n);
+cudaError_t frt_launch_scan_u32(const u32 *in, u64 n, u32 *partials, u32 *out, u32 *total, cudaStream_t s);
+cudaError_t frt_launch_bam_aux_dir(const u8 *buf, const u64 *record_offsets, const u32 *aux_start,
+                                   const u32 *record_end, const u32 *aux_count, const u32 *aux_first, u32 *entries,
+                                   u64 n, cudaStream_t s);

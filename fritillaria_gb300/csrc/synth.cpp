@@ -1,0 +1,550 @@
+// Seeded synthetic BAM generators and a BGZF writer.
+//
+// Produces the workloads the benchmark and the tests run on:
+//   * short paired-end reads (100k records on one 50 Mb contig, or 20M records
+//     over 24 contigs proportional to the human chromosomes), CIGAR 150M for
+//     90% of reads else one insertion, one deletion or a leading soft clip,
+//     uniform ACGT with 0.1% N, Phred ~ N(35, 5) clipped to 2..41, NM/MD/RG;
+//   * ultra-long unaligned reads (flag 4, refID -1) with log-normal lengths and
+//     MM:Z / ML:B:C / qs:f / ch:i tags.
+// The BAM byte layout follows the SAM specification as read by the reference
+// (crates/fritillaria-bam/src/columnar/record.rs:1-22, header.rs:1-12).
+//
+// BGZF packing follows one of two writers:
+//   * "full" packs a 65,495-byte staging buffer and flushes only when it is
+//     full, so records straddle members (the noodles writer's
+//     MAX_BUF_SIZE = 65536 - 18 - 8 - 15, crates/fritillaria-bgzf/src/io/writer.rs:24);
+//   * "record" starts a new member before a record that would not fit in
+//     65,280 bytes (htslib's bgzf_flush_try), so members start on records
+//     unless a record is larger than a member.
+// Compression is zlib raw deflate at a per-member level (even/odd members may
+// alternate levels).  Everything is deterministic in the seed and independent
+// of the thread count.
+
+#include <zlib.h>
+
+#include <algorithm>
+#include <functional>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// xoshiro256** seeded through splitmix64 (Blackman & Vigna, public domain
+// algorithms restated here).
+struct Rng {
+    uint64_t s[4];
+    static uint64_t splitmix(uint64_t &x)
+    {
+        uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    explicit Rng(uint64_t seed, uint64_t stream = 0)
+    {
+        uint64_t x = seed ^ (stream * 0xD1B54A32D192ED03ull);
+        for (auto &v : s) v = splitmix(x);
+    }
+    static uint64_t rotl(uint64_t v, int k) { return (v << k) | (v >> (64 - k)); }
+    uint64_t next()
+    {
+        uint64_t r = rotl(s[1] * 5, 7) * 9;
+        uint64_t t = s[1] << 17;
+        s[2] ^= s[0];
+        s[3] ^= s[1];
+        s[1] ^= s[2];
+        s[0] ^= s[3];
+        s[2] ^= t;
+        s[3] = rotl(s[3], 45);
+        return r;
+    }
+    double uniform() { return (next() >> 11) * (1.0 / 9007199254740992.0); }
+    uint32_t below(uint32_t n) { return (uint32_t)(((next() >> 32) * (uint64_t)n) >> 32); }
+    double normal()
+    {
+        double u1 = uniform(), u2 = uniform();
+        if (u1 < 1e-300) u1 = 1e-300;
+        return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+    }
+};
+
+void put32(std::vector<uint8_t> &b, uint32_t v)
+{
+    uint8_t x[4] = {(uint8_t)v, (uint8_t)(v >> 8), (uint8_t)(v >> 16), (uint8_t)(v >> 24)};
+    b.insert(b.end(), x, x + 4);
+}
+void put16(std::vector<uint8_t> &b, uint16_t v)
+{
+    b.push_back((uint8_t)v);
+    b.push_back((uint8_t)(v >> 8));
+}
+void patch32(std::vector<uint8_t> &b, size_t at, uint32_t v)
+{
+    b[at] = (uint8_t)v;
+    b[at + 1] = (uint8_t)(v >> 8);
+    b[at + 2] = (uint8_t)(v >> 16);
+    b[at + 3] = (uint8_t)(v >> 24);
+}
+
+// SAM specification, section 5.3: the smallest bin containing [beg, end).
+int reg2bin(int64_t beg, int64_t end)
+{
+    --end;
+    if (beg >> 14 == end >> 14) return (int)(((1 << 15) - 1) / 7 + (beg >> 14));
+    if (beg >> 17 == end >> 17) return (int)(((1 << 12) - 1) / 7 + (beg >> 17));
+    if (beg >> 20 == end >> 20) return (int)(((1 << 9) - 1) / 7 + (beg >> 20));
+    if (beg >> 23 == end >> 23) return (int)(((1 << 6) - 1) / 7 + (beg >> 23));
+    if (beg >> 26 == end >> 26) return (int)(((1 << 3) - 1) / 7 + (beg >> 26));
+    return 0;
+}
+
+// Human chromosome lengths (GRCh38, chr1..22, X, Y), used as relative weights.
+const double kHumanLengths[24] = {
+    248956422, 242193529, 198295559, 190214555, 181538259, 170805979, 159345973, 145138636,
+    138394717, 133797422, 135086622, 133275309, 114364328, 107043718, 101991189, 90338345,
+    83257441,  80373285,  58617616,  64444167,  46709983,  50818468,  156040895, 57227415};
+
+struct Contig {
+    std::string name;
+    uint32_t length;
+};
+
+std::vector<Contig> make_contigs(int n_contigs, uint64_t genome_len)
+{
+    std::vector<Contig> c;
+    if (n_contigs <= 1) {
+        c.push_back({"chr1", (uint32_t)genome_len});
+        return c;
+    }
+    double sum = 0;
+    for (int i = 0; i < 24; ++i) sum += kHumanLengths[i];
+    for (int i = 0; i < n_contigs && i < 24; ++i) {
+        std::string nm = i < 22 ? "chr" + std::to_string(i + 1) : (i == 22 ? "chrX" : "chrY");
+        c.push_back({nm, (uint32_t)(genome_len * (kHumanLengths[i] / sum))});
+    }
+    return c;
+}
+
+std::vector<uint8_t> bam_header(const std::vector<Contig> &contigs, bool sorted)
+{
+    std::string text = sorted ? "@HD\tVN:1.6\tSO:coordinate\n" : "@HD\tVN:1.6\tSO:unsorted\n";
+    for (auto &c : contigs) text += "@SQ\tSN:" + c.name + "\tLN:" + std::to_string(c.length) + "\n";
+    text += "@RG\tID:rg1\tSM:sample1\n";
+    std::vector<uint8_t> b = {'B', 'A', 'M', 1};
+    put32(b, (uint32_t)text.size());
+    b.insert(b.end(), text.begin(), text.end());
+    put32(b, (uint32_t)contigs.size());
+    for (auto &c : contigs) {
+        put32(b, (uint32_t)c.name.size() + 1);
+        b.insert(b.end(), c.name.begin(), c.name.end());
+        b.push_back(0);
+        put32(b, c.length);
+    }
+    return b;
+}
+
+const uint8_t kNibble[4] = {1, 2, 4, 8}; // A C G T in =ACMGRSVTWYHKDBN
+const char kBase[4] = {'A', 'C', 'G', 'T'};
+
+// One short paired-end record (150 bp) at global index `i`.
+void short_record(std::vector<uint8_t> &out, uint64_t i, uint64_t n_records,
+                  const std::vector<Contig> &contigs, const std::vector<uint64_t> &cum, uint64_t seed)
+{
+    Rng r(seed, i + 1);
+    const int L = 150;
+    // Stratified uniform positions: sorted by construction.
+    uint64_t genome = cum.back();
+    uint64_t g = (uint64_t)(((double)i + r.uniform()) * (double)genome / (double)n_records);
+    if (g >= genome) g = genome - 1;
+    size_t ci = std::upper_bound(cum.begin(), cum.end(), g) - cum.begin() - 1;
+    int64_t pos = (int64_t)(g - cum[ci]);
+    int64_t clen = contigs[ci].length;
+    if (pos > clen - L) pos = std::max<int64_t>(0, clen - L);
+
+    static const uint16_t kFlags[4] = {99, 147, 83, 163};
+    uint16_t flag = kFlags[r.below(4)];
+    uint8_t mapq = (uint8_t)r.below(61);
+
+    // CIGAR
+    uint32_t cig[3];
+    int ncig = 0;
+    int kind = 0, k = 0, a = 0;
+    int64_t ref_len = L;
+    if (r.uniform() >= 0.9) {
+        kind = 1 + (int)r.below(3);
+        if (kind == 1) { // aM kI bM
+            k = 1 + (int)r.below(5);
+            a = 10 + (int)r.below(L - 20 - k);
+            cig[ncig++] = ((uint32_t)a << 4) | 0;
+            cig[ncig++] = ((uint32_t)k << 4) | 1;
+            cig[ncig++] = ((uint32_t)(L - a - k) << 4) | 0;
+            ref_len = L - k;
+        } else if (kind == 2) { // aM kD bM
+            k = 1 + (int)r.below(5);
+            a = 10 + (int)r.below(L - 20);
+            cig[ncig++] = ((uint32_t)a << 4) | 0;
+            cig[ncig++] = ((uint32_t)k << 4) | 2;
+            cig[ncig++] = ((uint32_t)(L - a) << 4) | 0;
+            ref_len = L + k;
+        } else { // sS bM
+            k = 1 + (int)r.below(30);
+            cig[ncig++] = ((uint32_t)k << 4) | 4;
+            cig[ncig++] = ((uint32_t)(L - k) << 4) | 0;
+            ref_len = L - k;
+        }
+    } else {
+        cig[ncig++] = ((uint32_t)L << 4) | 0;
+    }
+    int bin = reg2bin(pos, pos + ref_len);
+    int insert = (int)std::lround(300 + 50 * r.normal());
+    if (insert < L) insert = L;
+    bool reverse = (flag & 16) != 0;
+    int64_t mpos = reverse ? std::max<int64_t>(0, pos - insert + L) : pos + insert - L;
+    int32_t tlen = reverse ? -insert : insert;
+
+    char name[16];
+    snprintf(name, sizeof name, "r%09llu", (unsigned long long)(i / 2));
+    size_t name_len = strlen(name) + 1;
+
+    // MD/NM over the aligned reference bases
+    int aligned = (int)(ref_len - (kind == 2 ? k : 0)); // M bases
+    int mism = 0;
+    double u = r.uniform();
+    mism = u < 0.6 ? 0 : (u < 0.85 ? 1 : (u < 0.95 ? 2 : 3));
+    std::vector<int> mpos_list;
+    for (int m = 0; m < mism; ++m) mpos_list.push_back((int)r.below((uint32_t)aligned));
+    std::sort(mpos_list.begin(), mpos_list.end());
+    mpos_list.erase(std::unique(mpos_list.begin(), mpos_list.end()), mpos_list.end());
+    std::string md;
+    {
+        int run = 0, m_idx = 0;
+        int del_at = (kind == 2) ? a : -1;
+        for (int p = 0; p < aligned; ++p) {
+            if (p == del_at) {
+                md += std::to_string(run);
+                md += '^';
+                for (int d = 0; d < k; ++d) md += kBase[r.below(4)];
+                run = 0;
+            }
+            if (m_idx < (int)mpos_list.size() && mpos_list[m_idx] == p) {
+                md += std::to_string(run);
+                md += kBase[r.below(4)];
+                run = 0;
+                ++m_idx;
+            } else {
+                ++run;
+            }
+        }
+        md += std::to_string(run);
+    }
+    int nm = (int)mpos_list.size() + ((kind == 1 || kind == 2) ? k : 0);
+
+    size_t start = out.size();
+    put32(out, 0); // block_size placeholder
+    put32(out, (uint32_t)ci);
+    put32(out, (uint32_t)pos);
+    out.push_back((uint8_t)name_len);
+    out.push_back(mapq);
+    put16(out, (uint16_t)bin);
+    put16(out, (uint16_t)ncig);
+    put16(out, flag);
+    put32(out, (uint32_t)L);
+    put32(out, (uint32_t)ci);
+    put32(out, (uint32_t)mpos);
+    put32(out, (uint32_t)tlen);
+    out.insert(out.end(), name, name + name_len - 1);
+    out.push_back(0);
+    for (int c = 0; c < ncig; ++c) put32(out, cig[c]);
+    uint8_t packed[75];
+    for (int b = 0; b < L; b += 2) {
+        uint8_t hi = r.uniform() < 0.001 ? 15 : kNibble[r.below(4)];
+        uint8_t lo = r.uniform() < 0.001 ? 15 : kNibble[r.below(4)];
+        packed[b / 2] = (uint8_t)((hi << 4) | lo);
+    }
+    out.insert(out.end(), packed, packed + 75);
+    for (int b = 0; b < L; ++b) {
+        long q = std::lround(35.0 + 5.0 * r.normal());
+        q = std::min(41L, std::max(2L, q));
+        out.push_back((uint8_t)q);
+    }
+    // NM:C (htslib writes the narrowest integer type), MD:Z, RG:Z
+    out.push_back('N'); out.push_back('M'); out.push_back('C'); out.push_back((uint8_t)nm);
+    out.push_back('M'); out.push_back('D'); out.push_back('Z');
+    out.insert(out.end(), md.begin(), md.end());
+    out.push_back(0);
+    const char rg[] = "RGZrg1";
+    out.insert(out.end(), rg, rg + 6);
+    out.push_back(0);
+    patch32(out, start, (uint32_t)(out.size() - start - 4));
+}
+
+// One ultra-long unaligned read with base-modification tags.
+void long_record(std::vector<uint8_t> &out, uint64_t i, uint32_t l_seq, uint64_t seed)
+{
+    Rng r(seed ^ 0x5555, i + 1);
+    char name[40];
+    snprintf(name, sizeof name, "%08x-%04x-%04x-%04x-%012llx", (unsigned)r.next(), (unsigned)(r.next() & 0xffff),
+             (unsigned)(r.next() & 0xffff), (unsigned)(r.next() & 0xffff), (unsigned long long)(r.next() & 0xffffffffffffull));
+    size_t name_len = strlen(name) + 1;
+    size_t start = out.size();
+    put32(out, 0);
+    put32(out, 0xffffffffu); // refID -1
+    put32(out, 0xffffffffu); // pos -1
+    out.push_back((uint8_t)name_len);
+    out.push_back(0);        // mapq
+    put16(out, 4680);        // bin of an unplaced read
+    put16(out, 0);           // n_cigar
+    put16(out, 4);           // flag: unmapped
+    put32(out, l_seq);
+    put32(out, 0xffffffffu);
+    put32(out, 0xffffffffu);
+    put32(out, 0);
+    out.insert(out.end(), name, name + name_len - 1);
+    out.push_back(0);
+    // sequence
+    std::vector<uint8_t> bases(l_seq);
+    for (uint32_t b = 0; b < l_seq; ++b) bases[b] = (uint8_t)r.below(4);
+    size_t p0 = out.size();
+    out.resize(p0 + (l_seq + 1) / 2);
+    for (uint32_t b = 0; b < l_seq; b += 2) {
+        uint8_t hi = kNibble[bases[b]];
+        uint8_t lo = (b + 1 < l_seq) ? kNibble[bases[b + 1]] : 0;
+        out[p0 + b / 2] = (uint8_t)((hi << 4) | lo);
+    }
+    // qualities: 5 + geometric(mean ~10), clipped to 5..40
+    double qsum = 0;
+    size_t q0 = out.size();
+    out.resize(q0 + l_seq);
+    const double lg = std::log(1.0 - 1.0 / 11.0);
+    for (uint32_t b = 0; b < l_seq; ++b) {
+        double u = r.uniform();
+        if (u < 1e-300) u = 1e-300;
+        int q = 5 + (int)std::floor(std::log(u) / lg);
+        q = std::min(40, std::max(5, q));
+        out[q0 + b] = (uint8_t)q;
+        qsum += q;
+    }
+    // MM:Z C+m? with skip counts over C sites, ML:B:C one byte per listed site
+    std::string mm = "C+m?";
+    std::vector<uint8_t> ml;
+    uint32_t skip = 0;
+    for (uint32_t b = 0; b < l_seq; ++b) {
+        if (bases[b] != 1) continue;
+        if (r.uniform() < 0.2) {
+            mm += ',';
+            mm += std::to_string(skip);
+            ml.push_back((uint8_t)r.below(256));
+            skip = 0;
+        } else {
+            ++skip;
+        }
+    }
+    mm += ';';
+    out.push_back('M'); out.push_back('M'); out.push_back('Z');
+    out.insert(out.end(), mm.begin(), mm.end());
+    out.push_back(0);
+    out.push_back('M'); out.push_back('L'); out.push_back('B'); out.push_back('C');
+    put32(out, (uint32_t)ml.size());
+    out.insert(out.end(), ml.begin(), ml.end());
+    float qs = l_seq ? (float)(qsum / l_seq) : 0.0f;
+    uint32_t qbits;
+    memcpy(&qbits, &qs, 4);
+    out.push_back('q'); out.push_back('s'); out.push_back('f');
+    put32(out, qbits);
+    uint32_t ch = 1 + r.below(512);
+    out.push_back('c'); out.push_back('h');
+    if (ch <= 255) { out.push_back('C'); out.push_back((uint8_t)ch); }
+    else { out.push_back('S'); put16(out, (uint16_t)ch); }
+    patch32(out, start, (uint32_t)(out.size() - start - 4));
+}
+
+void run_parallel(int threads, size_t n, const std::function<void(size_t)> &fn)
+{
+    if (threads < 1) threads = 1;
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&] {
+            for (;;) {
+                size_t i = next.fetch_add(1);
+                if (i >= n) break;
+                fn(i);
+            }
+        });
+    for (auto &th : pool) th.join();
+}
+} // namespace
+
+extern "C" {
+
+typedef struct {
+    int32_t kind;           // 0 short paired reads, 1 ultra-long unaligned
+    int32_t n_contigs;      // short reads: 1 or 24
+    uint64_t n_records;
+    uint64_t genome_len;
+    uint64_t seed;
+    int32_t threads;
+    int32_t n_long_extra;   // ultra-long: extra reads of 250-800 kb
+} frt_synth_bam_params;
+
+// Generates an uncompressed BAM stream (header + records).  `record_ends`
+// receives, when non-null, a malloc'd array of the end offset of the header
+// and of every record (n_records + 1 entries) for record-aligned packing.
+int frt_synth_bam(const frt_synth_bam_params *p, uint8_t **raw, size_t *raw_len, uint64_t **record_ends,
+                  size_t *n_ends)
+{
+    std::vector<Contig> contigs;
+    if (p->kind == 0) contigs = make_contigs(p->n_contigs, p->genome_len);
+    else contigs = make_contigs(1, 248956422);
+    std::vector<uint8_t> hdr = bam_header(contigs, p->kind == 0);
+    std::vector<uint64_t> cum(1, 0);
+    for (auto &c : contigs) cum.push_back(cum.back() + c.length);
+
+    // ultra-long lengths are drawn up front so chunks are independent
+    std::vector<uint32_t> lens;
+    uint64_t n = p->n_records;
+    if (p->kind == 1) {
+        Rng r(p->seed, 0x10000);
+        uint64_t total = n + (uint64_t)std::max(0, p->n_long_extra);
+        lens.resize(total);
+        for (uint64_t i = 0; i < n; ++i) {
+            double l = std::exp(std::log(15000.0) + 1.0 * r.normal());
+            lens[i] = (uint32_t)std::min(1000000.0, std::max(1.0, std::floor(l)));
+        }
+        for (uint64_t i = n; i < total; ++i) lens[i] = 250000 + r.below(550001);
+        // scatter the extra long reads
+        for (uint64_t i = total - 1; i > 0; --i) std::swap(lens[i], lens[r.below((uint32_t)std::min<uint64_t>(i + 1, 0xffffffffull))]);
+        n = total;
+    }
+    const uint64_t chunk = p->kind == 0 ? 65536 : 256;
+    size_t n_chunks = (size_t)((n + chunk - 1) / chunk);
+    std::vector<std::vector<uint8_t>> parts(n_chunks);
+    std::vector<std::vector<uint64_t>> ends(n_chunks);
+    run_parallel(p->threads, n_chunks, [&](size_t c) {
+        uint64_t b = c * chunk, e = std::min(n, b + chunk);
+        auto &out = parts[c];
+        for (uint64_t i = b; i < e; ++i) {
+            if (p->kind == 0) short_record(out, i, n, contigs, cum, p->seed);
+            else long_record(out, i, lens[i], p->seed);
+            if (record_ends) ends[c].push_back(out.size());
+        }
+    });
+    std::vector<size_t> base(n_chunks + 1, hdr.size());
+    for (size_t c = 0; c < n_chunks; ++c) base[c + 1] = base[c] + parts[c].size();
+    size_t total = base[n_chunks];
+    uint8_t *buf = (uint8_t *)malloc(total ? total : 1);
+    if (!buf) return -1;
+    memcpy(buf, hdr.data(), hdr.size());
+    run_parallel(p->threads, n_chunks, [&](size_t c) {
+        memcpy(buf + base[c], parts[c].data(), parts[c].size());
+        std::vector<uint8_t>().swap(parts[c]);
+    });
+    if (record_ends) {
+        uint64_t *re = (uint64_t *)malloc(sizeof(uint64_t) * (n + 1));
+        re[0] = hdr.size();
+        size_t k = 1;
+        for (size_t c = 0; c < n_chunks; ++c)
+            for (uint64_t v : ends[c]) re[k++] = base[c] + v;
+        *record_ends = re;
+        *n_ends = k;
+    }
+    *raw = buf;
+    *raw_len = total;
+    return 0;
+}
+
+// Splits `raw` into BGZF members.  mode 0: fixed payloads of `member_payload`
+// bytes (records straddle members).  mode 1: record-aligned, using
+// `record_ends` (ascending end offsets; the first is the header's end).
+// Members at even index are compressed at level_even, odd at level_odd.
+int frt_synth_bgzf(const uint8_t *raw, size_t raw_len, int mode, uint32_t member_payload,
+                   const uint64_t *record_ends, size_t n_ends, int level_even, int level_odd,
+                   int threads, uint8_t **out, size_t *out_len, uint64_t *n_members_out)
+{
+    std::vector<uint64_t> cuts; // member start offsets into raw, plus raw_len
+    cuts.push_back(0);
+    if (member_payload == 0 || member_payload > 65280) member_payload = 65280;
+    if (mode == 0) {
+        for (uint64_t o = member_payload; o < raw_len; o += member_payload) cuts.push_back(o);
+    } else {
+        // htslib: flush before a record that does not fit; split larger ones
+        uint64_t block_start = 0;
+        for (size_t k = 0; k < n_ends; ++k) {
+            uint64_t rec_beg = k == 0 ? 0 : record_ends[k - 1];
+            uint64_t rec_end = record_ends[k];
+            if (k == 0) { // header: its own member(s)
+                for (uint64_t o = member_payload; o < rec_end; o += member_payload) cuts.push_back(o);
+                if (rec_end < raw_len) cuts.push_back(rec_end);
+                block_start = rec_end;
+                continue;
+            }
+            if (rec_end - block_start > member_payload && rec_beg > block_start) {
+                cuts.push_back(rec_beg);
+                block_start = rec_beg;
+            }
+            while (rec_end - block_start > member_payload) {
+                block_start += member_payload;
+                cuts.push_back(block_start);
+            }
+        }
+    }
+    if (cuts.back() != raw_len || raw_len == 0) cuts.push_back(raw_len);
+    if (raw_len == 0) cuts.assign({0, 0});
+    size_t nm = cuts.size() - 1;
+    std::vector<std::vector<uint8_t>> mem(nm);
+    run_parallel(threads, nm, [&](size_t m) {
+        const uint8_t *src = raw + cuts[m];
+        uInt len = (uInt)(cuts[m + 1] - cuts[m]);
+        int level = (m % 2 == 0) ? level_even : level_odd;
+        std::vector<uint8_t> buf(65536 + 64);
+        uint32_t clen = 0;
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            z_stream zs;
+            memset(&zs, 0, sizeof zs);
+            deflateInit2(&zs, attempt == 0 ? level : 0, Z_DEFLATED, -15, 8, Z_DEFAULT_STRATEGY);
+            zs.next_in = (Bytef *)src;
+            zs.avail_in = len;
+            zs.next_out = buf.data() + 18;
+            zs.avail_out = 65536 - 26;
+            int rc = deflate(&zs, Z_FINISH);
+            clen = (uint32_t)(65536 - 26 - zs.avail_out);
+            deflateEnd(&zs);
+            if (rc == Z_STREAM_END) break;
+        }
+        uint32_t bsize = 18 + clen + 8;
+        const uint8_t h[18] = {0x1f, 0x8b, 8, 4, 0, 0, 0, 0, 0, 0xff, 6, 0, 'B', 'C', 2, 0,
+                               (uint8_t)((bsize - 1) & 0xff), (uint8_t)((bsize - 1) >> 8)};
+        memcpy(buf.data(), h, 18);
+        uint32_t crc = (uint32_t)crc32(0, src, len);
+        uint8_t *t = buf.data() + 18 + clen;
+        for (int b = 0; b < 4; ++b) t[b] = (uint8_t)(crc >> (8 * b));
+        for (int b = 0; b < 4; ++b) t[4 + b] = (uint8_t)(len >> (8 * b));
+        buf.resize(bsize);
+        mem[m] = std::move(buf);
+    });
+    static const uint8_t eof[28] = {0x1f, 0x8b, 0x08, 0x04, 0x00, 0x00, 0x00, 0x00, 0x00, 0xff, 0x06, 0x00, 0x42, 0x43,
+                                    0x02, 0x00, 0x1b, 0x00, 0x03, 0x00, 0x00, 0x00, 0x00, 0x00, 0x00, 0x00, 0x00, 0x00};
+    std::vector<size_t> base(nm + 1, 0);
+    for (size_t m = 0; m < nm; ++m) base[m + 1] = base[m] + mem[m].size();
+    size_t total = base[nm] + 28;
+    uint8_t *o = (uint8_t *)malloc(total);
+    if (!o) return -1;
+    run_parallel(threads, nm, [&](size_t m) { memcpy(o + base[m], mem[m].data(), mem[m].size()); });
+    memcpy(o + base[nm], eof, 28);
+    *out = o;
+    *out_len = total;
+    if (n_members_out) *n_members_out = nm + 1;
+    return 0;
+}
+
+void frt_synth_free(void *p) { free(p); }
+
+} // extern "C"

@@ -1,0 +1,113 @@
+"""Seeded synthetic inputs (native generator in ``csrc/synth.cpp``).
+
+Workloads:
+  * ``short_reads``: paired-end 2x150 bp, coordinate-sorted, NM/MD/RG tags --
+    100k records on one 50 Mb contig, or 20M records over 24 contigs
+    proportional to the human chromosomes (3.1 Gb);
+  * ``ultra_long``: unaligned reads with log-normal lengths (median 15 kb,
+    sigma 1.0, capped at 1 Mb) plus extra 250-800 kb reads, MM/ML/qs/ch tags.
+Members are packed "full" (records straddle members, as the noodles writer
+does) or "record" aligned (as htslib does), at one or two alternating levels.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+
+
+class _Params(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("n_contigs", C.c_int32), ("n_records", C.c_uint64),
+                ("genome_len", C.c_uint64), ("seed", C.c_uint64), ("threads", C.c_int32),
+                ("n_long_extra", C.c_int32)]
+
+
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        path = _PKG / "libfrt_synth.so"
+        if not path.exists():
+            from fritillaria_gb300.build import build_synth
+            build_synth()
+        _lib = C.CDLL(str(path))
+        _lib.frt_synth_bam.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.frt_synth_bgzf.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_uint32, C.c_void_p, C.c_size_t,
+                                        C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.frt_synth_free.argtypes = [C.c_void_p]
+    return _lib
+
+
+def _take(ptr: C.c_void_p, n: int) -> np.ndarray:
+    arr = np.empty(n, dtype=np.uint8)
+    if n:
+        C.memmove(arr.ctypes.data, ptr, n)
+    _load().frt_synth_free(ptr)
+    return arr
+
+
+def raw_bam(kind: str = "short_reads", n_records: int = 1000, n_contigs: int = 1, genome_len: int = 50_000_000,
+            seed: int = 1, n_long_extra: int = 0, threads: int | None = None):
+    """Uncompressed BAM bytes and the end offset of the header and of each
+    record."""
+    lib = _load()
+    p = _Params(0 if kind == "short_reads" else 1, n_contigs, n_records, genome_len, seed,
+                threads or os.cpu_count() or 1, n_long_extra)
+    raw = C.c_void_p()
+    raw_len = C.c_size_t()
+    ends = C.c_void_p()
+    n_ends = C.c_size_t()
+    if lib.frt_synth_bam(C.byref(p), C.byref(raw), C.byref(raw_len), C.byref(ends), C.byref(n_ends)) != 0:
+        raise MemoryError("synthetic BAM generation failed")
+    data = _take(raw, raw_len.value)
+    e = np.empty(n_ends.value, dtype=np.uint64)
+    C.memmove(e.ctypes.data, ends, 8 * n_ends.value)
+    lib.frt_synth_free(ends)
+    return data, e
+
+
+def bgzf(raw: np.ndarray, packing: str = "full", levels=(6, 6), record_ends=None, member_payload: int = 65495,
+         threads: int | None = None) -> np.ndarray:
+    """BGZF-compress `raw` into members (plus the EOF member)."""
+    lib = _load()
+    raw = np.ascontiguousarray(raw, dtype=np.uint8)
+    mode = 0 if packing == "full" else 1
+    if mode == 1 and record_ends is None:
+        raise ValueError("record packing needs record_ends")
+    ends = np.ascontiguousarray(record_ends if record_ends is not None else np.zeros(1), dtype=np.uint64)
+    out = C.c_void_p()
+    out_len = C.c_size_t()
+    nm = C.c_uint64()
+    payload = member_payload if mode == 0 else 65280
+    rc = lib.frt_synth_bgzf(raw.ctypes.data, raw.size, mode, payload, ends.ctypes.data,
+                            len(ends) if record_ends is not None else 0, levels[0], levels[1],
+                            threads or os.cpu_count() or 1, C.byref(out), C.byref(out_len), C.byref(nm))
+    if rc != 0:
+        raise MemoryError("BGZF compression failed")
+    return _take(out, out_len.value)
+
+
+def short_read_bam(n_records: int, n_contigs: int = 1, genome_len: int = 50_000_000, seed: int = 1,
+                   levels=(6, 6), packing: str = "full", member_payload: int = 65495):
+    raw, ends = raw_bam("short_reads", n_records, n_contigs, genome_len, seed)
+    return raw, bgzf(raw, packing, levels, ends, member_payload)
+
+
+def ultra_long_bam(n_records: int, n_long_extra: int = 0, seed: int = 3, levels=(6, 6), packing: str = "full",
+                   member_payload: int = 65495):
+    raw, ends = raw_bam("ultra_long", n_records, 1, 0, seed, n_long_extra)
+    return raw, bgzf(raw, packing, levels, ends, member_payload)
+
+
+# The benchmark configurations.
+CONFIGS = {
+    "short_reads_100k": dict(n_records=100_000, n_contigs=1, genome_len=50_000_000, levels=(6, 6)),
+    "short_reads_20m": dict(n_records=20_000_000, n_contigs=24, genome_len=3_100_000_000, levels=(1, 6)),
+}

@@ -1,0 +1,258 @@
+/*
+ * frt.h -- C ABI of the GB300 BGZF -> device-columns library.
+ *
+ * The entry points mirror the reference's Rust surface for this path so that a
+ * Rust host (through build.rs + an `extern "C"` block) or any other FFI caller
+ * can use it as a drop-in.  Each declaration names the reference item it
+ * replaces (paths relative to the fritillaria workspace).
+ *
+ * Conventions
+ *   - Every fallible call returns an frt_status and, when `err` is non-null,
+ *     fills it; FRT_OK is 0.  Error codes mirror the variants of
+ *     crates/fritillaria-core/src/error.rs:14-67; `offset` is the member's
+ *     absolute compressed offset, as there.
+ *   - Handles are opaque and caller-freed.  A record batch holds a reference
+ *     to the inflate batch its columns point into, so freeing the inflate batch
+ *     first cannot free the bytes under the columns
+ *     (crates/fritillaria-bam/src/columnar/device.rs:39-42).
+ *   - Device pointers are plain `void *`/`uint8_t *` in the current CUDA
+ *     context; streams and events are passed as `void *` (cudaStream_t /
+ *     cudaEvent_t).
+ *   - There is no CPU fallback: without a usable GB300 every codec constructor
+ *     returns FRT_ERR_CUDA_UNAVAILABLE.
+ */
+#ifndef FRT_H
+#define FRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    FRT_OK = 0,
+    FRT_ERR_IO = 1,                   /* Error::Io */
+    FRT_ERR_INVALID_BLOCK = 2,        /* Error::InvalidBlock{offset, reason} */
+    FRT_ERR_CHECKSUM = 3,             /* Error::ChecksumMismatch{offset, expected, actual} */
+    FRT_ERR_SIZE = 4,                 /* Error::SizeMismatch{offset, expected, actual} */
+    FRT_ERR_INFLATE = 5,              /* Error::Inflate{offset, reason} */
+    FRT_ERR_MALFORMED = 6,            /* Error::Malformed{format, position, reason} */
+    FRT_ERR_INVALID_DEVICE_BATCH = 7, /* Error::InvalidDeviceBatch{reason} */
+    FRT_ERR_CUDA_UNAVAILABLE = 8,     /* Error::CudaUnavailable */
+    FRT_ERR_CUDA = 9,                 /* Error::Cuda */
+    FRT_ERR_INVALID_ARGUMENT = 10
+} frt_status;
+
+typedef struct {
+    int32_t code;      /* frt_status */
+    uint64_t offset;   /* member compressed offset (block errors) */
+    uint64_t expected; /* CRC32 or ISIZE */
+    uint64_t actual;
+    uint64_t position; /* Malformed: byte position in the inflated batch */
+    char format[16];   /* Malformed: "bam", "bgzf", "bcf", "fastq" ... */
+    char reason[200];
+} frt_error;
+
+/* BlockSpan, crates/fritillaria-core/src/codec.rs:17-41. */
+typedef struct {
+    uint64_t compressed_offset;
+    uint64_t payload_start;
+    uint64_t payload_len;
+    uint32_t isize;
+    uint32_t crc32;
+} frt_span;
+
+typedef struct frt_codec frt_codec;
+typedef struct frt_inflate_batch frt_inflate_batch;
+typedef struct frt_reader frt_reader;
+typedef struct frt_bam_decoder frt_bam_decoder;
+typedef struct frt_record_batch frt_record_batch;
+
+/* Backend, crates/fritillaria/src/lib.rs:151-176. */
+typedef enum { FRT_BACKEND_AUTO = 0, FRT_BACKEND_CPU = 1, FRT_BACKEND_CUDA = 2, FRT_BACKEND_NVCOMP = 3 } frt_backend;
+
+/* ---- device and selection ---------------------------------------------- */
+
+/* cuda_is_usable, crates/fritillaria/src/lib.rs:183-186. */
+int frt_cuda_is_usable(void);
+
+/* select_codec, crates/fritillaria/src/lib.rs:242-260.  Auto and Cuda resolve
+ * to this library's GB300 codec or fail with FRT_ERR_CUDA_UNAVAILABLE; Nvcomp
+ * fails with FRT_ERR_CUDA_UNAVAILABLE (no nvCOMP path); Cpu fails with
+ * FRT_ERR_INVALID_ARGUMENT (the CPU codec is not part of this library). */
+int frt_select_codec(int backend, frt_codec **out, int *resolved, frt_error *err);
+
+/* ---- codec: CudaCodec as BlockCodec / DeviceBlockCodec ------------------ */
+
+/* CudaCodec::new / with_context(ctx, stream), crates/fritillaria-cuda/src/lib.rs:170-213.
+ * `stream` may be NULL (the codec creates its own) or a cudaStream_t on
+ * `device` owned by the caller. */
+int frt_codec_create(int device, void *stream, frt_codec **out, frt_error *err);
+void frt_codec_destroy(frt_codec *codec);
+/* DeviceBlockCodec::name / device_ordinal, crates/fritillaria-core/src/device.rs:306-324. */
+const char *frt_codec_name(const frt_codec *codec);
+int frt_codec_device_ordinal(const frt_codec *codec);
+void *frt_codec_stream(const frt_codec *codec);
+
+/* DeviceBlockCodec::inflate_batch_device, crates/fritillaria-core/src/device.rs:316-324,
+ * implemented by CudaCodec (crates/fritillaria-cuda/src/lib.rs:276-293).
+ * `batch` is host memory holding the compressed window; spans index it.
+ * CRC32 and ISIZE are verified; on failure *out is left untouched. */
+int frt_codec_inflate_batch_device(frt_codec *codec, const uint8_t *batch, size_t batch_len,
+                                   const frt_span *spans, size_t n_spans, frt_inflate_batch **out,
+                                   frt_error *err);
+
+/* BlockCodec::inflate_batch, crates/fritillaria-core/src/codec.rs:159-173: the
+ * same inflate with the bytes copied back.  `out` receives sum(ISIZE) bytes,
+ * `out_offsets` n_spans + 1 entries. */
+int frt_codec_inflate_batch_host(frt_codec *codec, const uint8_t *batch, size_t batch_len,
+                                 const frt_span *spans, size_t n_spans, uint8_t *out, size_t out_cap,
+                                 uint64_t *out_offsets, frt_error *err);
+
+/* crc32_blocks, crates/fritillaria-cuda/kernels/crc32.cu:13-38: CRC32 of
+ * device-resident members (`data` device pointer). */
+int frt_codec_crc32_device(frt_codec *codec, const uint8_t *data, const uint64_t *offsets,
+                           const uint32_t *lengths, size_t n, uint32_t *crcs_host, frt_error *err);
+
+/* ---- DeviceInflateBatch, crates/fritillaria-core/src/device.rs:145-287 --- */
+
+size_t frt_inflate_batch_len(const frt_inflate_batch *b);          /* members */
+size_t frt_inflate_batch_byte_len(const frt_inflate_batch *b);     /* inflated bytes */
+const uint8_t *frt_inflate_batch_data(const frt_inflate_batch *b); /* device pointer */
+const uint64_t *frt_inflate_batch_offsets(const frt_inflate_batch *b); /* host, len + 1 */
+const uint64_t *frt_inflate_batch_compressed_offsets(const frt_inflate_batch *b); /* host, len */
+int frt_inflate_batch_device_ordinal(const frt_inflate_batch *b);
+/* CudaCodec::ready_event, crates/fritillaria-cuda/src/lib.rs:215-225. */
+void *frt_inflate_batch_ready_event(const frt_inflate_batch *b);
+/* DeviceInflateBatch::to_host, device.rs:276-287. */
+int frt_inflate_batch_to_host(const frt_inflate_batch *b, uint8_t *dst, size_t cap, frt_error *err);
+void frt_inflate_batch_free(frt_inflate_batch *b);
+
+/* ---- DeviceBgzfReader, crates/fritillaria-bgzf/src/device_read.rs:57-280 -- */
+
+/* A byte source: returns bytes read (0 at end of stream) or -1 on error. */
+typedef int64_t (*frt_read_fn)(void *ctx, uint8_t *buf, size_t cap);
+
+/* DeviceBgzfReader::new(inner, codec).  The codec must outlive the reader. */
+int frt_reader_open(frt_read_fn read, void *ctx, frt_codec *codec, frt_reader **out, frt_error *err);
+/* Convenience sources: a caller-owned memory range, or a file path. */
+int frt_reader_open_memory(const uint8_t *data, size_t len, frt_codec *codec, frt_reader **out, frt_error *err);
+int frt_reader_open_path(const char *path, frt_codec *codec, frt_reader **out, frt_error *err);
+/* with_blocks_per_batch (device_read.rs:113-116): a floor on the compressed
+ * budget, blocks x 64 KiB; values below 1 become 1. */
+void frt_reader_set_blocks_per_batch(frt_reader *r, size_t blocks);
+/* next_batch (device_read.rs:188-280).  *has_batch = 0 at end of stream.
+ * *start is DeviceBatch::start. */
+int frt_reader_next_batch(frt_reader *r, frt_inflate_batch **out, uint64_t *start, int *has_batch,
+                          frt_error *err);
+/* carry_from (device_read.rs:155-182). */
+int frt_reader_carry_from(frt_reader *r, uint64_t tail, frt_error *err);
+const char *frt_reader_codec_name(const frt_reader *r);
+int frt_reader_device_ordinal(const frt_reader *r);
+void frt_reader_close(frt_reader *r);
+
+/* ---- host BGZF framing, crates/fritillaria-bgzf/src/discover.rs:51-109 ---- */
+int frt_bgzf_discover(const uint8_t *buf, size_t len, uint64_t base_offset, frt_span *spans, size_t cap,
+                      size_t *n_spans, size_t *consumed, frt_error *err);
+
+/* ---- BamDecoder, crates/fritillaria-cuda/src/bam.rs:113-187 --------------- */
+
+int frt_bam_decoder_create(int device, void *stream, frt_bam_decoder **out, frt_error *err);
+/* Bounds refID/next_refID in the boundary validator; -1 (default) means
+ * unknown.  Only a hint: results never depend on it. */
+void frt_bam_decoder_set_reference_count(frt_bam_decoder *d, int32_t n_ref);
+void frt_bam_decoder_destroy(frt_bam_decoder *d);
+/* BamDecoder::decode(batch, start) -> DeviceRecordBatch. */
+int frt_bam_decode(frt_bam_decoder *d, const frt_inflate_batch *batch, uint64_t start, frt_record_batch **out,
+                   frt_error *err);
+/* Speculation fallbacks of the last decode (BlockedScan::fallbacks, blocked.rs:80-88). */
+uint64_t frt_bam_decoder_last_fallbacks(const frt_bam_decoder *d);
+
+/* ---- DeviceRecordBatch, crates/fritillaria-bam/src/columnar/device.rs:135-297 */
+
+/* Columns.  0-13 are the reference's DeviceColumns (device.rs:63-110) in its
+ * order; 14+ are the additions of this library. */
+typedef enum {
+    FRT_COL_REF_ID = 0,          /* i32 */
+    FRT_COL_POS = 1,             /* i32 */
+    FRT_COL_FLAGS = 2,           /* u16 */
+    FRT_COL_MAPQ = 3,            /* u8 */
+    FRT_COL_SEQ_LEN = 4,         /* u32 */
+    FRT_COL_MATE_REF_ID = 5,     /* i32 */
+    FRT_COL_MATE_POS = 6,        /* i32 */
+    FRT_COL_TLEN = 7,            /* i32 */
+    FRT_COL_RECORD_OFFSETS = 8,  /* u64, into the inflate batch */
+    FRT_COL_CIGAR_START = 9,     /* u32, record-relative */
+    FRT_COL_SEQUENCE_START = 10, /* u32 */
+    FRT_COL_QUALITY_START = 11,  /* u32 */
+    FRT_COL_AUX_START = 12,      /* u32 */
+    FRT_COL_RECORD_END = 13,     /* u32 */
+    FRT_COL_BIN = 14,            /* u16 */
+    FRT_COL_N_CIGAR = 15,        /* u16 */
+    FRT_COL_NAME_LEN = 16,       /* u8, l_read_name including the NUL */
+    FRT_COL_VIRTUAL_OFFSET = 17, /* u64: member compressed offset << 16 | in-member offset */
+    FRT_COL_AUX_COUNT = 18,      /* u32: aux fields parsed */
+    FRT_COL_AUX_STATUS = 19,     /* u8: 0 aux block parses to its end, 1 malformed field */
+    FRT_COL_AUX_FIRST = 20,      /* u32, n + 1 entries: exclusive prefix of AUX_COUNT */
+    FRT_COL_AUX_ENTRIES = 21,    /* 12 bytes per field: tag[2], type, subtype, u32 value offset, u32 count */
+    FRT_COL_COUNT = 22
+} frt_bam_column;
+
+uint64_t frt_record_batch_len(const frt_record_batch *rb);
+/* DeviceRecordBatch::tail (device.rs:211-215). */
+uint64_t frt_record_batch_tail(const frt_record_batch *rb);
+uint64_t frt_record_batch_aux_fields(const frt_record_batch *rb);
+int frt_record_batch_device_ordinal(const frt_record_batch *rb);
+/* Device pointer, byte length and element width of a column. */
+int frt_record_batch_column(const frt_record_batch *rb, int column, void **ptr, size_t *bytes, size_t *width);
+/* Copies a column to host memory (to_host / field_bounds_to_host, device.rs:223-282). */
+int frt_record_batch_column_to_host(const frt_record_batch *rb, int column, void *dst, size_t cap, frt_error *err);
+void *frt_record_batch_ready_event(const frt_record_batch *rb);
+void frt_record_batch_free(frt_record_batch *rb);
+
+/* ---- batched, device-resident form ---------------------------------------
+ * No reference counterpart: the batched launch model.  Members of a whole
+ * BGZF file resident in device memory are discovered, inflated, verified,
+ * scanned and decoded by one persistent kernel per stage, fed by a device work
+ * queue sorted by compressed size; the steady state replays as a CUDA graph. */
+typedef struct frt_engine frt_engine;
+
+typedef struct {
+    uint32_t warps_per_cta;   /* 0: autotuned */
+    uint32_t queue_chunk;     /* members taken per queue pop; 0: autotuned */
+    uint32_t use_graph;       /* replay the steady state as a CUDA graph */
+    uint32_t sort_queue;      /* longest member first */
+} frt_engine_config;
+
+typedef struct {
+    uint64_t members;
+    uint64_t compressed_bytes;
+    uint64_t inflated_bytes;
+    uint64_t records;
+    uint64_t tail;
+    uint64_t aux_fields;
+    uint64_t fallbacks;
+    int32_t status;        /* frt_status of the last run */
+    uint32_t error_member; /* first failing member, when status is a block error */
+} frt_engine_stats;
+
+int frt_engine_create(int device, void *stream, const frt_engine_config *cfg, frt_engine **out, frt_error *err);
+void frt_engine_destroy(frt_engine *e);
+/* Binds a device-resident BGZF file (a BAM) and sizes every buffer for it. */
+int frt_engine_bind_bam(frt_engine *e, const uint8_t *dev_bgzf, size_t len, frt_error *err);
+/* Runs the bound file to columns on the engine's stream (asynchronous);
+ * frt_engine_finish waits and reports. */
+int frt_engine_run(frt_engine *e, frt_error *err);
+int frt_engine_finish(frt_engine *e, frt_engine_stats *stats, frt_error *err);
+/* Host-buffer convenience: H2D copy, run, and read the stats back. */
+int frt_engine_run_host(frt_engine *e, const uint8_t *host_bgzf, size_t len, frt_engine_stats *stats,
+                        frt_error *err);
+int frt_engine_column(const frt_engine *e, int column, void **ptr, size_t *bytes, size_t *width);
+const uint8_t *frt_engine_inflated(const frt_engine *e, size_t *len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
