@@ -1,0 +1,373 @@
+#!/usr/bin/env python3
+"""BAM -> device columns, decompressed GB/s on GB300.
+
+One step = one pass of the path over the whole synthetic file: BGZF member
+discovery, inflate, CRC32/ISIZE verification, BAM record scan and every
+column, ending with the device error word read back and checked.
+
+  value   batched form, compressed bytes already resident in HBM
+  e2e     the same through the C ABI from pinned host memory (H2D of the
+          compressed file and D2H of the run's stats inside the timed region)
+  plain   the reference-shaped per-batch form (DeviceBgzfReader +
+          BamDecoder, 256 members per batch, host syncs per batch) on the
+          same GPU and the same host bytes
+  cpu_baseline  the oracle's multithreaded restatement of the noodles CPU
+          path (zlib inflate + CRC on all host cores, serial record scan,
+          columns and aux walk)
+
+Inputs are seeded synthetic data (no dataset is available offline); the
+workload is larger than L2, so no flush is needed between steps.
+Multi-GPU: the path shards by file, so N GPUs run N replicas of the workload
+(weak scaling); value = all ranks' bytes / the slowest rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "short_reads_20m": dict(kind="short", n_records=20_000_000, n_contigs=24, genome_len=3_100_000_000,
+                            levels=(1, 6), seed=20,
+                            desc="20M paired-end 2x150 bp records over 24 contigs (3.1 Gb), BGZF members "
+                                 "alternating zlib level 1/6, packed full (records straddle members)"),
+    "short_reads_100k": dict(kind="short", n_records=100_000, n_contigs=1, genome_len=50_000_000, levels=(6, 6),
+                             seed=1, desc="100k 2x150 bp records on one 50 Mb contig, BGZF level 6, packed full"),
+    "ultra_long_50k": dict(kind="long", n_records=50_000, n_long_extra=20, levels=(6, 6), seed=3,
+                           desc="50k unaligned ultra-long reads (log-normal, median 15 kb) + 20 of 250-800 kb, "
+                                "MM/ML/qs/ch tags, BGZF level 6 packed full"),
+}
+
+METRIC = "BAM->device-column decompressed GB/s, batched vs plain, 1 GB300, bit-exact"
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", choices=sorted(WORKLOADS), default="short_reads_20m")
+    p.add_argument("--no-plain", action="store_true", help="skip the per-batch comparison")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    return p.parse_args()
+
+
+def generate(name: str):
+    from fritillaria_gb300 import synth
+
+    w = WORKLOADS[name]
+    if w["kind"] == "short":
+        _, bgzf = synth.short_read_bam(w["n_records"], n_contigs=w["n_contigs"], genome_len=w["genome_len"],
+                                       seed=w["seed"], levels=w["levels"])
+    else:
+        _, bgzf = synth.ultra_long_bam(w["n_records"], n_long_extra=w["n_long_extra"], seed=w["seed"],
+                                       levels=w["levels"])
+    return bgzf
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.out.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = list(csv.reader(io.StringIO(open(self.path).read())))
+        os.unlink(self.path)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if r[5 + k].strip().lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_setup(n_gpus: int):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_baseline(bgzf, inflated_bytes: int):
+    """The oracle's CPU restatement, all host threads, whole file (a bounded
+    sample: seconds of work on 16 cores)."""
+    from oracle import oracle
+
+    threads = os.cpu_count() or 1
+    res = oracle.baseline_bam(bgzf, threads)
+    gbs = res.inflated_bytes / res.seconds / 1e9 if res.seconds > 0 else 0.0
+    return {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"whole file: {res.members} members, {res.inflated_bytes} inflated bytes, {res.records} "
+                      f"records, {res.seconds:.2f} s; C restatement of the noodles multithreaded BGZF reader "
+                      f"(zlib 1.3 inflate + CRC32) and the serial record scan/columns/aux walk",
+            "records": res.records, "status": res.status}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    bgzf = generate(args.workload)
+    from oracle import oracle
+
+    threads = os.cpu_count() or 1
+    times = []
+    res = None
+    for i in range(args.warmup + args.steps):
+        res = oracle.baseline_bam(bgzf, threads)
+        if i >= args.warmup:
+            times.append(res.seconds)
+    total = sum(times)
+    gbs = res.inflated_bytes * len(times) / total / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * total / len(times), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"],
+                   "records": res.records, "inflated_bytes": res.inflated_bytes, "members": res.members},
+        "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": "whole file per step; C restatement of the noodles CPU path (the reference's "
+                                   "Rust CPU path cannot be built here: no Rust toolchain)"},
+        "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_plain(frt, host_bytes, blocks_per_batch=256):
+    """The drop-in per-batch loop (crates/fritillaria-cuda/tests/bam_reader.rs:76-115)."""
+    codec = frt.CudaCodec(0)
+    decoder = frt.BamDecoder(0)
+    t0 = time.perf_counter()
+    reader = frt.DeviceBgzfReader(host_bytes, codec, blocks_per_batch=blocks_per_batch)
+    header = None
+    records = 0
+    inflated = 0
+    batches = 0
+    while True:
+        batch = reader.next_batch()
+        if batch is None:
+            break
+        batches += 1
+        inflated += batch.data.byte_len()
+        if header is None:
+            # the header is parsed on the host from the first batch, as the
+            # reference's consumer loop does
+            try:
+                header = frt.parse_header(batch.data.to_host())
+            except frt.Malformed:
+                reader.carry_from(0)
+                continue
+            decoder.set_reference_count(header[1])
+            begin = header[0]
+        else:
+            begin = batch.start
+        rb = decoder.decode(batch.data, begin)
+        records += len(rb)
+        tail = rb.tail()
+        rb.free()
+        reader.carry_from(tail)
+    dt = time.perf_counter() - t0
+    return records, inflated, dt, batches
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    import fritillaria_gb300 as frt
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    bgzf = generate(args.workload)
+    host = torch.from_numpy(bgzf).pin_memory()
+    dev = host.to("cuda")
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    eng = frt.BatchEngine(0, stream=stream.cuda_stream)
+    eng.bind_bam(dev.data_ptr(), dev.numel())
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            eng.run()
+            st = eng.finish()
+        assert st.status == 0
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        with Clocks(local) as clocks:
+            t0 = time.perf_counter()
+            ev0.record(stream)
+            for _ in range(args.steps):
+                eng.run()
+                st = eng.finish()  # reads and checks the device error word
+                if st.status != 0:
+                    raise RuntimeError(f"engine status {st.status}")
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    ms_step = ms / args.steps
+    inflated = st.inflated_bytes
+    value = world * inflated * args.steps / (ms / 1e3) / 1e9
+
+    # stage breakdown and the roofline of the dominant kernel (inflate)
+    front_ms, inflate_ms, records_ms = eng.time_stages(3)
+    spans = frt.discover_blocks(bgzf)[0]
+    payload = int(spans["payload_len"].astype(np.uint64).sum())
+    col_bytes = 0
+    for name in frt.BAM_COLUMNS:
+        col_bytes += eng.column_ptr(name)[1]
+    col_bytes += eng.column_ptr("aux_entries")[1]
+    peak, peak_kind = peaks()
+    inflate_bytes = payload + inflated
+    achieved = inflate_bytes / (inflate_ms / 1e3) / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "inflate_traffic.json"
+    if tp.exists():
+        d = json.loads(tp.read_text())
+        if d.get("workload") == args.workload:
+            traffic = d.get("traffic_bytes_per_launch")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 5), "traffic": traffic,
+                "kernel": "k_inflate_persistent (persistent warp-per-member inflate + CRC32/ISIZE verify)",
+                "algorithmic_bytes_per_launch": inflate_bytes, "kernel_ms": round(inflate_ms, 3),
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "pipeline": {"bytes": len(bgzf) + inflated + col_bytes, "ms": round(ms_step, 3),
+                             "frac": round((len(bgzf) + inflated + col_bytes) / (ms_step / 1e3) / 1e9 / peak, 5)},
+                "stages_ms": {"discover_plan_queue": round(front_ms, 3), "inflate_verify": round(inflate_ms, 3),
+                              "records_columns": round(records_ms, 3)}}
+
+    # e2e through the C ABI from pinned host memory
+    e2e_steps = max(3, min(args.steps, 5))
+    hbuf = host.numpy()
+    for _ in range(1):
+        eng.run_host(hbuf)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        st2 = eng.run_host(hbuf)
+        assert st2.status == 0
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": round(world * inflated / e2e_s / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": len(bgzf),
+           "d2h_bytes_per_step": 128, "ms_per_step": round(1e3 * e2e_s, 3)}
+
+    plain = None
+    if not args.no_plain:
+        run_plain(frt, hbuf)  # warm
+        recs, infl, dt, batches = run_plain(frt, hbuf)
+        plain = {"value": round(infl / dt / 1e9, 3), "unit": "GB/s", "records": recs, "batches": batches,
+                 "members_per_batch": 256, "note": "per-batch reader+decoder from pinned host memory; "
+                                                  "compare with e2e",
+                 "batched_e2e_over_plain": round((inflated / e2e_s) / (infl / dt), 2)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(bgzf, inflated)
+
+    if rank == 0:
+        w = WORKLOADS[args.workload]
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": args.workload, "description": w["desc"], "records": st.records,
+                       "members": st.members, "compressed_bytes": len(bgzf), "inflated_bytes": inflated,
+                       "aux_fields": st.aux_fields, "column_bytes": col_bytes, "speculation_fallbacks": st.fallbacks,
+                       "l2": "inputs larger than L2 (no flush)", "queue": "sorted by compressed size",
+                       "graph": True, "parallelism": f"replicas x{world}",
+                       "records_per_s": round(world * st.records * args.steps / (ms / 1e3), 1)},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "plain": plain,
+            "gpu_launches": eng.launches_per_run() * args.steps,
+            "clocks": clocks.summary(),
+            "wall_s": round(wall, 3),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

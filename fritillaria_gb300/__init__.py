@@ -202,6 +202,7 @@ def lib():
         "frt_reader_device_ordinal": (C.c_int, [_P]),
         "frt_reader_close": (None, [_P]),
         "frt_bgzf_discover": (C.c_int, [_P, C.c_size_t, C.c_uint64, _P, C.c_size_t, _P, _P, _P]),
+        "frt_bam_parse_header": (C.c_int, [_P, C.c_size_t, _P, _P, _P]),
         "frt_bam_decoder_create": (C.c_int, [C.c_int, _P, _P, _P]),
         "frt_bam_decoder_set_reference_count": (None, [_P, C.c_int32]),
         "frt_bam_decoder_destroy": (None, [_P]),
@@ -223,6 +224,10 @@ def lib():
         "frt_engine_run_host": (C.c_int, [_P, _P, C.c_size_t, _P, _P]),
         "frt_engine_column": (C.c_int, [_P, C.c_int, _P, _P, _P]),
         "frt_engine_inflated": (_P, [_P, _P]),
+        "frt_engine_column_to_host": (C.c_int, [_P, C.c_int, _P, C.c_size_t, _P]),
+        "frt_engine_stream": (_P, [_P]),
+        "frt_engine_time_stages": (C.c_int, [_P, _P, C.c_int, _P]),
+        "frt_engine_launches": (C.c_uint64, [_P]),
     }
     for name, (res, args) in sig.items():
         if hasattr(L, name):
@@ -334,6 +339,18 @@ def discover_blocks(data, base_offset: int = 0):
     _raise(lib().frt_bgzf_discover(b.ctypes.data, b.size, base_offset, spans.ctypes.data, cap, C.byref(n),
                                    C.byref(used), C.byref(err)), err)
     return spans[: n.value].copy(), used.value
+
+
+def parse_header(data):
+    """parse_header (crates/fritillaria-bam/src/columnar/header.rs:43-101):
+    (records_start, n_ref).  Raises Malformed when the bytes do not hold a
+    whole header yet."""
+    b = _u8(data)
+    rs = C.c_uint64()
+    nr = C.c_int32()
+    err = _Err()
+    _raise(lib().frt_bam_parse_header(b.ctypes.data, b.size, C.byref(rs), C.byref(nr), C.byref(err)), err)
+    return rs.value, nr.value
 
 
 class DeviceInflateBatch:
@@ -587,6 +604,37 @@ class BatchEngine:
         w = C.c_size_t()
         lib().frt_engine_column(self._h, cid, C.byref(p), C.byref(nb), C.byref(w))
         return p.value or 0, nb.value, w.value
+
+    def column(self, name: str) -> np.ndarray:
+        if name == "aux_entries":
+            cid, dt = 21, AUX_DTYPE
+        else:
+            cid, dt = BAM_COLUMNS[name]
+        _, nb, _ = self.column_ptr(name)
+        out = np.empty(nb // np.dtype(dt).itemsize, dtype=dt)
+        err = _Err()
+        _raise(lib().frt_engine_column_to_host(self._h, cid, out.ctypes.data, out.nbytes, C.byref(err)), err)
+        return out
+
+    def inflated_ptr(self):
+        n = C.c_size_t()
+        p = lib().frt_engine_inflated(self._h, C.byref(n))
+        return p or 0, n.value
+
+    @property
+    def stream(self) -> int:
+        return lib().frt_engine_stream(self._h) or 0
+
+    def time_stages(self, repeats: int = 3):
+        """Milliseconds per stage (front, inflate, records), each the mean of
+        `repeats` eager runs timed with CUDA events on the engine stream."""
+        ms = (C.c_float * 3)()
+        err = _Err()
+        _raise(lib().frt_engine_time_stages(self._h, ms, repeats, C.byref(err)), err)
+        return list(ms)
+
+    def launches_per_run(self) -> int:
+        return int(lib().frt_engine_launches(self._h))
 
     def __del__(self):
         h = getattr(self, "_h", None)

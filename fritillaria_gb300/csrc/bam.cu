@@ -64,6 +64,12 @@ __device__ __forceinline__ bool plausible(const u8 *buf, u64 len, u64 p, int n_r
     if (!fields_fit(buf, p, p + 4ull + bs)) return false;
     u64 nul = p + 36 + name_len - 1;
     if (nul < len && buf[nul] != 0) return false;
+    // QNAME is printable ([!-~]); the first 16 characters are checked
+    u32 nchk = min(name_len - 1, 16u);
+    for (u32 k = 0; k < nchk && p + 36 + k < len; ++k) {
+        u32 c = buf[p + 36 + k];
+        if (c < 0x21u || c > 0x7eu) return false;
+    }
     return true;
 }
 
@@ -117,10 +123,13 @@ __device__ Seg walk_record(const u8 *buf, u64 len, u64 from, u64 until, u64 msta
 
 // Phase 1.  One warp per member.
 __global__ void k_bam_spec(const u8 *buf, u64 len, const u64 *starts, u32 n_members, u64 start,
-                                        int n_ref, u64 *entry, u32 *count, u64 *land, u8 *flags, u16 *scratch)
+                                        int n_ref, u64 *entry, u32 *count, u64 *land, u8 *flags, u16 *scratch,
+                                        const u64 *start_dev, const int *nref_dev)
 {
     u32 m = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     if (m >= n_members) return;
+    if (start_dev) start = *start_dev;
+    if (nref_dev) n_ref = *nref_dev < 0 ? (1 << 24) : *nref_dev;
     const u32 lane = lane_id();
     u64 ms = starts[m], me = starts[m + 1];
     u64 e = INF64;
@@ -133,11 +142,12 @@ __global__ void k_bam_spec(const u8 *buf, u64 len, const u64 *starts, u32 n_memb
             u64 p = base + lane;
             bool ok = p < me && plausible(buf, len, p, n_ref);
             if (ok) {
+                // the next two records must validate as well, wherever they
+                // fall in the batch (a decoy's length usually lands far away)
                 u64 q = p + 4ull + ld_u32le(buf + p);
-                if (q < me && q + 4 <= len) {
-                    // the next record must validate as well
-                    if (q + 36 <= len) ok = plausible(buf, len, q, n_ref);
-                    else ok = true;
+                for (int k = 0; k < 2 && ok && q + 36 <= len; ++k) {
+                    ok = plausible(buf, len, q, n_ref);
+                    q += 4ull + ld_u32le(buf + q);
                 }
             }
             u32 hit = __ballot_sync(FRT_FULL_MASK, ok);
@@ -161,8 +171,9 @@ __global__ void k_bam_spec(const u8 *buf, u64 len, const u64 *starts, u32 n_memb
 // fallbacks}.
 __global__ void __launch_bounds__(1024)
 k_bam_reconcile(const u8 *buf, u64 len, const u64 *starts, u32 n_members, u64 start, u64 *entry, u32 *count,
-                  u64 *land, u8 *flags, u16 *scratch, u32 *first_index, u64 *totals)
+                  u64 *land, u8 *flags, u16 *scratch, u32 *first_index, u64 *totals, const u64 *start_dev)
 {
+    if (start_dev) start = *start_dev;
     __shared__ u64 s_warp[32];
     __shared__ u64 s_carry;
     __shared__ u32 s_bad;
@@ -389,7 +400,7 @@ __device__ __forceinline__ u32 aux_field(const u8 *rec, u32 pos, u32 end, u32 *w
 // Phase 3: columns.  One warp per member, lanes over its records.
 __global__ void k_bam_decode(const u8 *buf, const u64 *starts, const u64 *member_coffset, u32 n_members,
                                           const u32 *count, const u32 *first_index, const u16 *scratch,
-                                          FrtBamColumnsDev c)
+                                          FrtBamColumnsDev c, u64 rec_cap)
 {
     u32 m = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     if (m >= n_members) return;
@@ -404,6 +415,7 @@ __global__ void k_bam_decode(const u8 *buf, const u64 *starts, const u64 *member
         u64 r = ms + rel;
         const u8 *p = buf + r;
         u64 i = (u64)first + k;
+        if (i >= rec_cap) break;
         u32 bs = ld_u32le(p);
         u32 name_len = p[12];
         u32 n_cigar = ld_u16le(p + 16);
@@ -450,10 +462,12 @@ __global__ void k_bam_decode(const u8 *buf, const u64 *starts, const u64 *member
 // Phase 4: aux-tag directory, one thread per record, entries at aux_first[i].
 __global__ void k_bam_aux_dir(const u8 *buf, const u64 *record_offsets, const u32 *aux_start,
                                            const u32 *record_end, const u32 *aux_count, const u32 *aux_first,
-                                           u32 *entries, u64 n)
+                                           u32 *entries, u64 n, const u64 *n_dev, u64 aux_cap)
 {
     u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n_dev && *n_dev < n) n = *n_dev;
     if (i >= n) return;
+    if ((u64)aux_first[i] + aux_count[i] > aux_cap) return;
     const u8 *p = buf + record_offsets[i];
     u32 pos = aux_start[i], re = record_end[i], nt = aux_count[i];
     u32 *out = entries + 3ull * aux_first[i];
@@ -546,19 +560,21 @@ __global__ void __launch_bounds__(1024) k_scan_apply(const u32 *in, u64 n, const
 
 // ---- host launchers --------------------------------------------------------
 cudaError_t frt_launch_bam_spec(const u8 *buf, u64 len, const u64 *starts, u32 n, u64 start, int n_ref, u64 *entry,
-                                u32 *count, u64 *land, u8 *flags, u16 *scratch, cudaStream_t s)
+                                u32 *count, u64 *land, u8 *flags, u16 *scratch, cudaStream_t s, const u64 *start_dev,
+                                const int *nref_dev)
 {
     if (n == 0) return cudaSuccess;
-    k_bam_spec<<<(n + 7) / 8, 256, 0, s>>>(buf, len, starts, n, start, n_ref, entry, count, land, flags, scratch);
+    k_bam_spec<<<(n + 7) / 8, 256, 0, s>>>(buf, len, starts, n, start, n_ref, entry, count, land, flags, scratch,
+                                           start_dev, nref_dev);
     return cudaGetLastError();
 }
 
 cudaError_t frt_launch_bam_reconcile(const u8 *buf, u64 len, const u64 *starts, u32 n, u64 start, u64 *entry,
                                      u32 *count, u64 *land, u8 *flags, u16 *scratch, u32 *first_index, u64 *totals,
-                                     cudaStream_t s)
+                                     cudaStream_t s, const u64 *start_dev)
 {
     k_bam_reconcile<<<1, 1024, 0, s>>>(buf, len, starts, n, start, entry, count, land, flags, scratch, first_index,
-                                         totals);
+                                         totals, start_dev);
     return cudaGetLastError();
 }
 
@@ -567,7 +583,7 @@ cudaError_t frt_launch_bam_decode(const u8 *buf, const u64 *starts, const u64 *c
                                   cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
-    k_bam_decode<<<(n + 7) / 8, 256, 0, s>>>(buf, starts, coff, n, count, first_index, scratch, c);
+    k_bam_decode<<<(n + 7) / 8, 256, 0, s>>>(buf, starts, coff, n, count, first_index, scratch, c, ~0ull);
     return cudaGetLastError();
 }
 
@@ -589,6 +605,26 @@ cudaError_t frt_launch_bam_aux_dir(const u8 *buf, const u64 *record_offsets, con
 {
     if (n == 0) return cudaSuccess;
     k_bam_aux_dir<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(buf, record_offsets, aux_start, record_end, aux_count,
-                                                                aux_first, entries, n);
+                                                                aux_first, entries, n, nullptr, ~0ull);
+    return cudaGetLastError();
+}
+
+cudaError_t frt_launch_bam_decode_capped(const u8 *buf, const u64 *starts, const u64 *coff, u32 n, const u32 *count,
+                                         const u32 *first_index, const u16 *scratch, const FrtBamColumnsDev &c,
+                                         u64 rec_cap, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_bam_decode<<<(n + 7) / 8, 256, 0, s>>>(buf, starts, coff, n, count, first_index, scratch, c, rec_cap);
+    return cudaGetLastError();
+}
+
+cudaError_t frt_launch_bam_aux_dir_capped(const u8 *buf, const u64 *record_offsets, const u32 *aux_start,
+                                          const u32 *record_end, const u32 *aux_count, const u32 *aux_first,
+                                          u32 *entries, const u64 *n_dev, u64 rec_cap, u64 aux_cap, cudaStream_t s)
+{
+    if (rec_cap == 0) return cudaSuccess;
+    k_bam_aux_dir<<<(unsigned)((rec_cap + 255) / 256), 256, 0, s>>>(buf, record_offsets, aux_start, record_end,
+                                                                    aux_count, aux_first, entries, rec_cap, n_dev,
+                                                                    aux_cap);
     return cudaGetLastError();
 }

@@ -33,10 +33,11 @@ struct FrtBamColumnsDev {
 
 
 cudaError_t frt_launch_bam_spec(const u8 *buf, u64 len, const u64 *starts, u32 n, u64 start, int n_ref, u64 *entry,
-                                u32 *count, u64 *land, u8 *flags, u16 *scratch, cudaStream_t s);
+                                u32 *count, u64 *land, u8 *flags, u16 *scratch, cudaStream_t s,
+                                const u64 *start_dev = nullptr, const int *nref_dev = nullptr);
 cudaError_t frt_launch_bam_reconcile(const u8 *buf, u64 len, const u64 *starts, u32 n, u64 start, u64 *entry,
                                      u32 *count, u64 *land, u8 *flags, u16 *scratch, u32 *first_index, u64 *totals,
-                                     cudaStream_t s);
+                                     cudaStream_t s, const u64 *start_dev = nullptr);
 cudaError_t frt_launch_bam_decode(const u8 *buf, const u64 *starts, const u64 *coff, u32 n, const u32 *count,
                                   const u32 *first_index, const u16 *scratch, const FrtBamColumnsDev &c,
                                   cudaStream_t s);
@@ -45,3 +46,9 @@ cudaError_t frt_launch_scan_u32(const u32 *in, u64 n, u32 *partials, u32 *out, u
 cudaError_t frt_launch_bam_aux_dir(const u8 *buf, const u64 *record_offsets, const u32 *aux_start,
                                    const u32 *record_end, const u32 *aux_count, const u32 *aux_first, u32 *entries,
                                    u64 n, cudaStream_t s);
+cudaError_t frt_launch_bam_decode_capped(const u8 *buf, const u64 *starts, const u64 *coff, u32 n, const u32 *count,
+                                         const u32 *first_index, const u16 *scratch, const FrtBamColumnsDev &c,
+                                         u64 rec_cap, cudaStream_t s);
+cudaError_t frt_launch_bam_aux_dir_capped(const u8 *buf, const u64 *record_offsets, const u32 *aux_start,
+                                          const u32 *record_end, const u32 *aux_count, const u32 *aux_first,
+                                          u32 *entries, const u64 *n_dev, u64 rec_cap, u64 aux_cap, cudaStream_t s);

@@ -1,0 +1,873 @@
+// The batched, device-resident form.
+//
+// Instead of one launch sequence per batch of 256 members with a host sync
+// for the statuses and another for the record totals (the reference's launch
+// model, crates/fritillaria-cuda/src/backend.rs:547-720 and src/bam.rs:324-573),
+// a whole BGZF file resident in HBM goes through one pass of device-only
+// stages, with no host round trip until the final stats read:
+//
+//   discovery   16-byte-vector sieve for gzip/BGZF headers, ordered
+//               compaction (count, scan, emit), then a tiling proof that
+//               the candidates chain from offset 0 to the end; a serial walk
+//               only if the proof fails;
+//   plan        member spans from the headers/trailers, exclusive scan of
+//               ISIZE into output offsets;
+//   queue       counting sort of members by compressed size, longest first;
+//   inflate     the persistent warp-per-member kernel pulls from the queue
+//               and verifies CRC32/ISIZE in-kernel into one error word;
+//   records     BAM header parse, per-member speculative scan, reconcile,
+//               column decode, aux-count scan and aux directory.
+//
+// bind() runs the stages once eagerly to size every buffer, then captures the
+// stage sequence as a CUDA graph; run() replays it.
+
+#include <cstring>
+#include <vector>
+
+#include "bam.cuh"
+#include "engine_kernels.cuh"
+#include "inflate.cuh"
+#include "runtime.h"
+
+using namespace frt;
+
+namespace {
+
+constexpr u64 SIEVE_TILE = 1ull << 16;
+
+// A BGZF member header at p (block.rs:88-165): returns bsize (0 if none) and
+// the header size.  Only complete members inside the buffer count.
+__device__ __forceinline__ u32 member_at(const u8 *buf, u64 len, u64 p, u32 *hsize)
+{
+    if (p + 12 > len) return 0;
+    if (buf[p] != 0x1f || buf[p + 1] != 0x8b || buf[p + 2] != 8 || !(buf[p + 3] & 4)) return 0;
+    u32 xlen = ld_u16le(buf + p + 10);
+    if (p + 12 + xlen > len) return 0;
+    u32 off = 0, bsize = 0;
+    bool found = false;
+    while (off + 4 <= xlen) {
+        const u8 *x = buf + p + 12 + off;
+        u32 slen = ld_u16le(x + 2);
+        if (off + 4 + slen > xlen) break;
+        if (x[0] == 'B' && x[1] == 'C') {
+            if (slen == 2) {
+                bsize = ld_u16le(x + 4) + 1;
+                found = true;
+            }
+            break;
+        }
+        off += 4 + slen;
+    }
+    if (!found) return 0;
+    if (bsize > 65536u || bsize < 12 + xlen + 8) return 0;
+    if (p + bsize > len) return 0;
+    *hsize = 12 + xlen;
+    return bsize;
+}
+
+} // namespace
+
+// One warp per 64 KiB tile, 16 bytes per lane per step.  Count mode
+// (tile_base == nullptr) writes the tile's candidate count; emit mode writes
+// the candidates in order starting at tile_base[tile].
+__global__ void k_bgzf_sieve(const u8 *buf, u64 len, u64 tile, u32 *counts, const u32 *tile_base, u64 *cand,
+                             u64 cand_cap)
+{
+    const u32 lane = lane_id();
+    u64 t = (u64)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    u64 t0 = t * tile;
+    if (t0 >= len) return;
+    u64 t1 = min(len, t0 + tile);
+    u32 found = 0;
+    u64 out = tile_base ? tile_base[t] : 0;
+    for (u64 base = t0; base < t1; base += 512) {
+        u64 p0 = base + 16ull * lane;
+        u32 mine = 0;
+        u64 hits[2];
+        if (p0 < t1) {
+            u32 w[4];
+            if (p0 + 16 <= len && ((u64)(buf + p0) & 15ull) == 0) {
+                uint4 v = *(const uint4 *)(buf + p0);
+                w[0] = v.x;
+                w[1] = v.y;
+                w[2] = v.z;
+                w[3] = v.w;
+            } else {
+                for (int k = 0; k < 4; ++k) {
+                    u32 x = 0;
+                    for (int b = 0; b < 4; ++b) {
+                        u64 q = p0 + 4 * k + b;
+                        x |= (u32)(q < len ? buf[q] : 0) << (8 * b);
+                    }
+                    w[k] = x;
+                }
+            }
+            // bytes equal to 0x1f: the zero-byte test on w ^ 0x1f1f1f1f
+            for (int k = 0; k < 4; ++k) {
+                u32 x = w[k] ^ 0x1f1f1f1fu;
+                u32 z = (x - 0x01010101u) & ~x & 0x80808080u;
+                while (z) {
+                    int b = (__ffs(z) - 1) >> 3;
+                    z &= z - 1;
+                    u64 p = p0 + 4 * k + b;
+                    u32 hs;
+                    if (p < t1 && member_at(buf, len, p, &hs)) {
+                        if (mine < 2) hits[mine] = p;
+                        ++mine;
+                    }
+                }
+            }
+        }
+        // ordered output within the warp: lanes in address order
+        u32 x = mine;
+        for (int d = 1; d < 32; d <<= 1) {
+            u32 y = __shfl_up_sync(FRT_FULL_MASK, x, d);
+            if (lane >= (u32)d) x += y;
+        }
+        u32 excl = x - mine;
+        u32 step_total = __shfl_sync(FRT_FULL_MASK, x, 31);
+        if (tile_base && mine) {
+            // a lane holds at most 16 bytes, so more than two headers in it is
+            // impossible for valid members; extra ones are re-found serially
+            u32 k = 0;
+            for (u32 j = 0; j < mine && j < 2; ++j, ++k)
+                if (out + found + excl + k < cand_cap) cand[out + found + excl + k] = hits[j];
+            if (mine > 2) {
+                u32 seen = 0;
+                for (int b = 0; b < 16; ++b) {
+                    u64 p = p0 + b;
+                    u32 hs;
+                    if (p < t1 && buf[p] == 0x1f && member_at(buf, len, p, &hs)) {
+                        if (seen >= 2 && out + found + excl + seen < cand_cap) cand[out + found + excl + seen] = p;
+                        ++seen;
+                    }
+                }
+            }
+        }
+        found += step_total;
+    }
+    if (!tile_base && lane == 0) counts[t] = found;
+}
+
+// The candidates tile the buffer iff the first is at 0, each one's successor
+// is the next, and the last ends exactly at the buffer end.
+__global__ void k_bgzf_tiling(const u8 *buf, u64 len, const u64 *cand, const u32 *n_cand, u64 n_cap,
+                              EngineDevState *st)
+{
+    u64 n = *n_cand;
+    if (n > n_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            st->capacity_err = 1;
+            st->tiling_failed = 1;
+        }
+        n = n_cap;
+    }
+    u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k == 0) {
+        st->n_members = n;
+        if (n == 0 ? len != 0 : cand[0] != 0) st->tiling_failed = 1;
+    }
+    if (k >= n) return;
+    u32 hs;
+    u32 bs = member_at(buf, len, cand[k], &hs);
+    u64 next = cand[k] + bs;
+    u64 want = k + 1 < n ? cand[k + 1] : len;
+    if (bs == 0 || next != want) st->tiling_failed = 1;
+}
+
+// Fallback when the candidates do not tile: walk the headers from 0 (one
+// thread).  An invalid header stops the walk and is reported.
+__global__ void k_bgzf_walk(const u8 *buf, u64 len, u64 *cand, u64 cap, EngineDevState *st)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0 || !st->tiling_failed) return;
+    u64 p = 0, n = 0;
+    while (p < len) {
+        u32 hs;
+        u32 bs = member_at(buf, len, p, &hs);
+        if (bs == 0) {
+            st->walk_err = p + 1;
+            break;
+        }
+        if (n < cap) cand[n] = p;
+        ++n;
+        p += bs;
+    }
+    st->n_members = n;
+}
+
+// Member spans for the first n members; entries past n (up to n_cap) become
+// empty members so every later stage stays in bounds.
+__global__ void k_bgzf_spans(const u8 *buf, u64 len, const u64 *cand, u64 n_cap, EngineDevState *st, u64 *in_off,
+                             u32 *in_len, u32 *isize, u32 *crc, u64 *coffset)
+{
+    u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_cap) return;
+    u64 n = st->n_members;
+    if (n > n_cap) {
+        if (k == 0) st->capacity_err = 1;
+        n = n_cap;
+    }
+    if (k >= n) {
+        in_off[k] = 0;
+        in_len[k] = 0;
+        isize[k] = 0;
+        crc[k] = 0;
+        coffset[k] = len;
+        return;
+    }
+    u64 p = cand[k];
+    u32 hs = 0;
+    u32 bs = member_at(buf, len, p, &hs);
+    if (bs == 0) { // cannot happen for a proven tiling; keep the member empty
+        in_off[k] = 0;
+        in_len[k] = 0;
+        isize[k] = 0;
+        crc[k] = 0;
+        coffset[k] = p;
+        atomicMin((unsigned long long *)&st->block_err, ((unsigned long long)k << 8) | 2ull);
+        return;
+    }
+    u32 isz = ld_u32le(buf + p + bs - 4);
+    in_off[k] = p + hs;
+    in_len[k] = bs - hs - 8;
+    crc[k] = ld_u32le(buf + p + bs - 8);
+    coffset[k] = p;
+    if (isz > 65536u) { // discover.rs:88-95
+        atomicMin((unsigned long long *)&st->block_err, ((unsigned long long)k << 8) | 2ull);
+        isz = 0;
+    }
+    isize[k] = isz;
+}
+
+// Work queue: members by compressed size, longest first (1024 buckets of 64 B).
+__global__ void k_queue_hist(const u32 *in_len, u64 n, u32 *hist)
+{
+    u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    u32 b = 1023u - min(1023u, in_len[k] >> 6);
+    atomicAdd(&hist[b], 1u);
+}
+
+__global__ void k_queue_scatter(const u32 *in_len, u64 n, u32 *cursor, u32 *order)
+{
+    u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    u32 b = 1023u - min(1023u, in_len[k] >> 6);
+    u32 slot = atomicAdd(&cursor[b], 1u);
+    order[slot] = (u32)k;
+}
+
+// BAM header (crates/fritillaria-bam/src/columnar/header.rs:43-101): one thread.
+__global__ void k_bam_header(const u8 *buf, const u64 *total, EngineDevState *st)
+{
+    if (threadIdx.x || blockIdx.x) return;
+    u64 len = *total;
+    st->header_status = 1;
+    if (len < 12 || buf[0] != 'B' || buf[1] != 'A' || buf[2] != 'M' || buf[3] != 1) return;
+    int l_text = (int)ld_u32le(buf + 4);
+    if (l_text < 0) return;
+    u64 pos = 8ull + (u64)l_text;
+    if (pos + 4 > len) return;
+    int n_ref = (int)ld_u32le(buf + pos);
+    if (n_ref < 0) return;
+    pos += 4;
+    for (int i = 0; i < n_ref; ++i) {
+        if (pos + 4 > len) return;
+        int l_name = (int)ld_u32le(buf + pos);
+        if (l_name < 0) return;
+        pos += 4 + (u64)l_name;
+        if (pos + 4 > len) return;
+        pos += 4;
+    }
+    st->records_start = pos;
+    st->n_ref = n_ref;
+    st->header_status = 0;
+}
+
+namespace {
+
+// exclusive scan of u32 values into u64 offsets (n + 1 entries)
+__global__ void __launch_bounds__(1024) k_scan64_partials(const u32 *in, u64 n, u64 *partials)
+{
+    __shared__ u64 s[32];
+    u64 base = (u64)blockIdx.x * 4096;
+    u64 acc = 0;
+    for (int k = 0; k < 4; ++k) {
+        u64 i = base + (u64)k * 1024 + threadIdx.x;
+        if (i < n) acc += in[i];
+    }
+    for (int d = 16; d; d >>= 1) acc += __shfl_down_sync(FRT_FULL_MASK, acc, d);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        u64 v = s[threadIdx.x];
+        for (int d = 16; d; d >>= 1) v += __shfl_down_sync(FRT_FULL_MASK, v, d);
+        if (threadIdx.x == 0) partials[blockIdx.x] = v;
+    }
+}
+
+__device__ u64 block_scan64(u64 v, u64 *s_warp, u64 *total)
+{
+    const u32 lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    u64 x = v;
+    for (int d = 1; d < 32; d <<= 1) {
+        u64 y = __shfl_up_sync(FRT_FULL_MASK, x, d);
+        if (lane >= (u32)d) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        u64 w = s_warp[lane];
+        for (int d = 1; d < 32; d <<= 1) {
+            u64 y = __shfl_up_sync(FRT_FULL_MASK, w, d);
+            if (lane >= (u32)d) w += y;
+        }
+        s_warp[lane] = w;
+    }
+    __syncthreads();
+    u64 ex = x - v + (wid ? s_warp[wid - 1] : 0ull);
+    *total = s_warp[31];
+    __syncthreads();
+    return ex;
+}
+
+__global__ void __launch_bounds__(1024) k_scan64_partials_scan(u64 *partials, u64 n_parts)
+{
+    __shared__ u64 s_warp[32];
+    u64 carry = 0;
+    for (u64 b = 0; b < n_parts; b += 1024) {
+        u64 i = b + threadIdx.x;
+        u64 v = i < n_parts ? partials[i] : 0ull;
+        u64 tot;
+        u64 ex = block_scan64(v, s_warp, &tot);
+        if (i < n_parts) partials[i] = carry + ex;
+        carry += tot;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_scan64_apply(const u32 *in, u64 n, const u64 *partials, u64 *out,
+                                                       u64 *total_out)
+{
+    __shared__ u64 s_warp[32];
+    u64 base = (u64)blockIdx.x * 4096;
+    u64 carry = partials[blockIdx.x];
+    for (int k = 0; k < 4; ++k) {
+        u64 i = base + (u64)k * 1024 + threadIdx.x;
+        u64 v = i < n ? in[i] : 0ull;
+        u64 tot;
+        u64 ex = block_scan64(v, s_warp, &tot);
+        if (i <= n) out[i] = carry + ex;
+        carry += tot;
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0 && total_out) *total_out = carry;
+}
+
+// Exclusive scan of the 1024 queue buckets into cursors (one CTA).
+__global__ void __launch_bounds__(1024) k_queue_cursor(const u32 *hist, u32 *cursor)
+{
+    __shared__ u64 s_warp[32];
+    u64 tot;
+    u64 ex = block_scan64(hist[threadIdx.x], s_warp, &tot);
+    cursor[threadIdx.x] = (u32)ex;
+}
+
+// Decoded-record and aux-field counts must fit what bind sized.
+__global__ void k_check_counts(EngineDevState *st, u64 rec_cap, u64 aux_cap)
+{
+    if (threadIdx.x || blockIdx.x) return;
+    // the steady state replays what bind measured: any other count means the
+    // bound buffer changed
+    if (st->totals[0] != rec_cap || (u64)st->n_aux != aux_cap) st->capacity_err = 1;
+}
+
+} // namespace
+
+// ===========================================================================
+// host side
+// ===========================================================================
+struct frt_engine {
+    int device = 0;
+    SharedStream *shared = nullptr;
+    cudaStream_t stream = nullptr;
+    frt_engine_config cfg{};
+    int grid = 0;
+    // bound file
+    const uint8_t *in = nullptr;
+    size_t len = 0;
+    u64 n_cap = 0, tiles = 0, out_cap = 0, rec_cap = 0, aux_cap = 0;
+    // buffers
+    EngineDevState *st = nullptr;
+    u32 *tile_counts = nullptr, *tile_base = nullptr;
+    u64 *cand = nullptr, *in_off = nullptr, *coffset = nullptr, *out_off = nullptr, *scan_parts = nullptr;
+    u32 *in_len = nullptr, *isize = nullptr, *crc_expect = nullptr, *order = nullptr, *hist = nullptr,
+        *cursor = nullptr, *status = nullptr, *produced = nullptr, *crc = nullptr;
+    u8 *out = nullptr;
+    // records
+    u64 *entry = nullptr, *land = nullptr;
+    u32 *count = nullptr, *first = nullptr, *aux_parts = nullptr, *aux_entries = nullptr;
+    u8 *flags = nullptr;
+    u16 *scratch = nullptr;
+    u8 *cols = nullptr;
+    size_t col_off[FRT_COL_COUNT] = {};
+    size_t col_bytes[FRT_COL_COUNT] = {};
+    std::vector<void *> allocs;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    EngineDevState host_state{};
+};
+
+namespace {
+
+template <typename T> int ealloc(frt_engine *e, T **p, size_t n, frt_error *err)
+{
+    void *q = nullptr;
+    cudaError_t ce = cudaMallocAsync(&q, n * sizeof(T) + 64, e->stream);
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "allocating engine buffers");
+    e->allocs.push_back(q);
+    *p = (T *)q;
+    return FRT_OK;
+}
+
+void free_all(frt_engine *e)
+{
+    if (e->exec) cudaGraphExecDestroy(e->exec);
+    if (e->graph) cudaGraphDestroy(e->graph);
+    e->exec = nullptr;
+    e->graph = nullptr;
+    for (void *p : e->allocs) cudaFreeAsync(p, e->stream);
+    e->allocs.clear();
+    cudaStreamSynchronize(e->stream);
+}
+
+template <typename T> T *ecol(frt_engine *e, int c) { return (T *)(e->cols + e->col_off[c]); }
+
+// The discovery, plan and queue stages (everything up to the inflate).
+cudaError_t enqueue_front(frt_engine *e)
+{
+    cudaStream_t s = e->stream;
+    cudaMemsetAsync(e->st, 0, sizeof(EngineDevState), s);
+    cudaMemsetAsync(&e->st->block_err, 0xff, 8, s);
+    u64 tiles = e->tiles;
+    unsigned sieve_grid = (unsigned)((tiles + 7) / 8);
+    if (tiles) k_bgzf_sieve<<<sieve_grid, 256, 0, s>>>(e->in, e->len, SIEVE_TILE, e->tile_counts, nullptr, nullptr, 0);
+    frt_launch_scan_u32(e->tile_counts, tiles, (u32 *)e->scan_parts, e->tile_base, e->tile_base + tiles + 1, s);
+    if (tiles)
+        k_bgzf_sieve<<<sieve_grid, 256, 0, s>>>(e->in, e->len, SIEVE_TILE, nullptr, e->tile_base, e->cand, e->n_cap);
+    k_bgzf_tiling<<<(unsigned)((e->n_cap + 255) / 256 + 1), 256, 0, s>>>(e->in, e->len, e->cand, e->tile_base + tiles,
+                                                                         e->n_cap, e->st);
+    k_bgzf_walk<<<1, 32, 0, s>>>(e->in, e->len, e->cand, e->n_cap, e->st);
+    unsigned mgrid = (unsigned)((e->n_cap + 255) / 256);
+    k_bgzf_spans<<<mgrid, 256, 0, s>>>(e->in, e->len, e->cand, e->n_cap, e->st, e->in_off, e->in_len, e->isize,
+                                      e->crc_expect, e->coffset);
+    u64 parts = e->n_cap / 4096 + 1;
+    k_scan64_partials<<<(unsigned)parts, 1024, 0, s>>>(e->isize, e->n_cap, e->scan_parts);
+    k_scan64_partials_scan<<<1, 1024, 0, s>>>(e->scan_parts, parts);
+    k_scan64_apply<<<(unsigned)parts, 1024, 0, s>>>(e->isize, e->n_cap, e->scan_parts, e->out_off,
+                                                    &e->st->inflated_total);
+    cudaMemsetAsync(e->hist, 0, 1024 * 4, s);
+    if (e->cfg.sort_queue) {
+        k_queue_hist<<<mgrid, 256, 0, s>>>(e->in_len, e->n_cap, e->hist);
+        k_queue_cursor<<<1, 1024, 0, s>>>(e->hist, e->cursor);
+        k_queue_scatter<<<mgrid, 256, 0, s>>>(e->in_len, e->n_cap, e->cursor, e->order);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t enqueue_inflate(frt_engine *e)
+{
+    return frt_launch_inflate_persistent(e->in, e->in_off, e->in_len, e->out, e->out_off, e->isize, e->crc_expect,
+                                         e->status, e->produced, e->crc, e->cfg.sort_queue ? e->order : nullptr,
+                                         &e->st->n_members, e->n_cap, e->out_cap, &e->st->queue_head,
+                                         e->cfg.queue_chunk ? e->cfg.queue_chunk : 1, (u32)e->grid,
+                                         (unsigned long long *)&e->st->block_err, e->stream);
+}
+
+void column_ptrs(frt_engine *e, FrtBamColumnsDev &c)
+{
+    c.ref_id = ecol<int>(e, FRT_COL_REF_ID);
+    c.pos = ecol<int>(e, FRT_COL_POS);
+    c.flags = ecol<u16>(e, FRT_COL_FLAGS);
+    c.mapq = ecol<u8>(e, FRT_COL_MAPQ);
+    c.seq_len = ecol<u32>(e, FRT_COL_SEQ_LEN);
+    c.mate_ref_id = ecol<int>(e, FRT_COL_MATE_REF_ID);
+    c.mate_pos = ecol<int>(e, FRT_COL_MATE_POS);
+    c.tlen = ecol<int>(e, FRT_COL_TLEN);
+    c.record_offsets = ecol<u64>(e, FRT_COL_RECORD_OFFSETS);
+    c.cigar_start = ecol<u32>(e, FRT_COL_CIGAR_START);
+    c.sequence_start = ecol<u32>(e, FRT_COL_SEQUENCE_START);
+    c.quality_start = ecol<u32>(e, FRT_COL_QUALITY_START);
+    c.aux_start = ecol<u32>(e, FRT_COL_AUX_START);
+    c.record_end = ecol<u32>(e, FRT_COL_RECORD_END);
+    c.bin = ecol<u16>(e, FRT_COL_BIN);
+    c.n_cigar = ecol<u16>(e, FRT_COL_N_CIGAR);
+    c.name_len = ecol<u8>(e, FRT_COL_NAME_LEN);
+    c.virtual_offset = ecol<u64>(e, FRT_COL_VIRTUAL_OFFSET);
+    c.aux_count = ecol<u32>(e, FRT_COL_AUX_COUNT);
+    c.aux_status = ecol<u8>(e, FRT_COL_AUX_STATUS);
+}
+
+// Record stages: header, speculative scan, reconcile, and (once the record
+// and aux counts are sized) decode and the aux directory.
+cudaError_t enqueue_records(frt_engine *e, bool with_columns)
+{
+    cudaStream_t s = e->stream;
+    k_bam_header<<<1, 32, 0, s>>>(e->out, &e->st->inflated_total, e->st);
+    u32 n = (u32)e->n_cap;
+    u64 len = e->out_cap; // scans stay inside the planned output
+    frt_launch_bam_spec(e->out, len, e->out_off, n, 0, 0, e->entry, e->count, e->land, e->flags, e->scratch, s,
+                        &e->st->records_start, &e->st->n_ref);
+    frt_launch_bam_reconcile(e->out, len, e->out_off, n, 0, e->entry, e->count, e->land, e->flags, e->scratch,
+                             e->first, e->st->totals, s, &e->st->records_start);
+    if (!with_columns) return cudaGetLastError();
+    FrtBamColumnsDev c;
+    column_ptrs(e, c);
+    frt_launch_bam_decode_capped(e->out, e->out_off, e->coffset, n, e->count, e->first, e->scratch, c, e->rec_cap, s);
+    frt_launch_scan_u32(c.aux_count, e->rec_cap, e->aux_parts, ecol<u32>(e, FRT_COL_AUX_FIRST), &e->st->n_aux, s);
+    k_check_counts<<<1, 32, 0, s>>>(e->st, e->rec_cap, e->aux_cap);
+    frt_launch_bam_aux_dir_capped(e->out, c.record_offsets, c.aux_start, c.record_end, c.aux_count,
+                                  ecol<u32>(e, FRT_COL_AUX_FIRST), e->aux_entries, &e->st->totals[0], e->rec_cap,
+                                  e->aux_cap, s);
+    return cudaGetLastError();
+}
+
+int stats_from_state(frt_engine *e, frt_engine_stats *stats, frt_error *err)
+{
+    EngineDevState &h = e->host_state;
+    frt_engine_stats out{};
+    out.members = h.n_members;
+    out.compressed_bytes = e->len;
+    out.inflated_bytes = h.inflated_total;
+    out.records = h.totals[0];
+    out.tail = h.totals[1];
+    out.aux_fields = h.n_aux;
+    out.fallbacks = h.totals[3];
+    out.status = FRT_OK;
+    out.error_member = 0xffffffffu;
+    int rc = FRT_OK;
+    if (h.walk_err) {
+        set_error(err, FRT_ERR_INVALID_BLOCK, h.walk_err - 1, 0, 0, 0, nullptr, "not a BGZF member header");
+        rc = FRT_ERR_INVALID_BLOCK;
+    } else if (h.block_err != ~0ull) {
+        u64 m = h.block_err >> 8;
+        int code = (int)(h.block_err & 0xff);
+        out.error_member = (uint32_t)m;
+        uint32_t vals[3] = {0, 0, 0};
+        uint64_t coff = 0;
+        uint32_t want[2] = {0, 0};
+        cudaMemcpy(&vals[0], e->status + m, 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(&vals[1], e->produced + m, 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(&vals[2], e->crc + m, 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(&coff, e->coffset + m, 8, cudaMemcpyDeviceToHost);
+        cudaMemcpy(&want[0], e->isize + m, 4, cudaMemcpyDeviceToHost);
+        cudaMemcpy(&want[1], e->crc_expect + m, 4, cudaMemcpyDeviceToHost);
+        if (code == FRT_ERR_INFLATE)
+            set_error(err, code, coff, 0, 0, 0, nullptr, "%s", inflate_status_message(vals[0]));
+        else if (code == FRT_ERR_SIZE)
+            set_error(err, code, coff, want[0], vals[1], 0, nullptr, "ISIZE says %u bytes, inflated %u", want[0],
+                      vals[1]);
+        else if (code == FRT_ERR_CHECKSUM)
+            set_error(err, code, coff, want[1], vals[2], 0, nullptr, "expected crc32 %#010x, got %#010x", want[1],
+                      vals[2]);
+        else
+            set_error(err, code, coff, 0, 0, 0, nullptr, "invalid BGZF member");
+        rc = code;
+    } else if (h.tiling_failed && h.n_members == 0 && e->len) {
+        set_error(err, FRT_ERR_INVALID_BLOCK, 0, 0, 0, 0, nullptr, "not a BGZF member header");
+        rc = FRT_ERR_INVALID_BLOCK;
+    } else if (h.capacity_err) {
+        set_error(err, FRT_ERR_INVALID_DEVICE_BATCH, 0, 0, 0, 0, nullptr,
+                  "the bound buffer changed since bind: counts exceed the planned capacity");
+        rc = FRT_ERR_INVALID_DEVICE_BATCH;
+    } else if (h.header_status) {
+        set_error(err, FRT_ERR_MALFORMED, 0, 0, 0, 0, "bam header", "malformed BAM header");
+        rc = FRT_ERR_MALFORMED;
+    } else if (h.totals[2]) {
+        set_error(err, FRT_ERR_MALFORMED, 0, 0, 0, h.totals[1], "bam",
+                  "malformed record reached from a confirmed boundary");
+        rc = FRT_ERR_MALFORMED;
+    }
+    out.status = rc;
+    if (stats) *stats = out;
+    return rc;
+}
+
+void layout(frt_engine *e)
+{
+    size_t off = 0;
+    for (int c = 0; c < FRT_COL_COUNT; ++c) {
+        size_t bytes = c == FRT_COL_AUX_FIRST ? 4 * (e->rec_cap + 1)
+                                              : (c == FRT_COL_AUX_ENTRIES ? 0 : bam_column_width(c) * e->rec_cap);
+        e->col_off[c] = off;
+        e->col_bytes[c] = bytes;
+        off += (bytes + 255) & ~(size_t)255;
+    }
+}
+
+size_t layout_total(frt_engine *e)
+{
+    size_t t = 0;
+    for (int c = 0; c < FRT_COL_COUNT; ++c) t += (e->col_bytes[c] + 255) & ~(size_t)255;
+    return t;
+}
+
+} // namespace
+
+extern "C" int frt_engine_create(int device, void *stream, const frt_engine_config *cfg, frt_engine **out,
+                                 frt_error *err)
+{
+    int rc = check_device(device, err);
+    if (rc) return rc;
+    DeviceGuardLite g(device);
+    configure_pool(device);
+    cudaError_t ce = frt_inflate_prepare();
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "configuring inflate kernels");
+    SharedStream *ss = stream_create(device, stream, err);
+    if (!ss) return FRT_ERR_CUDA;
+    frt_engine *e = new frt_engine;
+    e->device = device;
+    e->shared = ss;
+    e->stream = ss->s;
+    if (cfg) e->cfg = *cfg;
+    else e->cfg = frt_engine_config{0, 0, 1, 1};
+    e->grid = frt_inflate_persistent_grid();
+    *out = e;
+    return FRT_OK;
+}
+
+extern "C" void frt_engine_destroy(frt_engine *e)
+{
+    if (!e) return;
+    DeviceGuardLite g(e->device);
+    free_all(e);
+    stream_release(e->shared);
+    delete e;
+}
+
+extern "C" int frt_engine_bind_bam(frt_engine *e, const uint8_t *dev_bgzf, size_t len, frt_error *err)
+{
+    DeviceGuardLite g(e->device);
+    free_all(e);
+    e->in = dev_bgzf;
+    e->len = len;
+    e->tiles = (len + SIEVE_TILE - 1) / SIEVE_TILE;
+    // Pass 1: discovery alone, to learn the member count.
+    e->n_cap = 0;
+    int rc;
+    u64 tiles = e->tiles;
+    if ((rc = ealloc(e, &e->st, 1, err))) return rc;
+    if ((rc = ealloc(e, &e->tile_counts, tiles + 1, err))) return rc;
+    if ((rc = ealloc(e, &e->tile_base, tiles + 2, err))) return rc;
+    if ((rc = ealloc(e, &e->scan_parts, tiles / 4096 + 2 + 1, err))) return rc;
+    cudaStream_t s = e->stream;
+    cudaMemsetAsync(e->st, 0, sizeof(EngineDevState), s);
+    unsigned sieve_grid = (unsigned)((tiles + 7) / 8);
+    if (tiles) {
+        k_bgzf_sieve<<<sieve_grid, 256, 0, s>>>(e->in, len, SIEVE_TILE, e->tile_counts, nullptr, nullptr, 0);
+        frt_launch_scan_u32(e->tile_counts, tiles, (u32 *)e->scan_parts, e->tile_base, e->tile_base + tiles + 1, s);
+    } else {
+        cudaMemsetAsync(e->tile_base, 0, 8, s);
+    }
+    u32 n_cand = 0;
+    cudaMemcpyAsync(&n_cand, e->tile_base + tiles, 4, cudaMemcpyDeviceToHost, s);
+    cudaError_t ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "discovery");
+    // Capacity: the candidates, or (if they do not tile) what a walk can find.
+    e->n_cap = n_cand ? n_cand : 1;
+    // Pass 2: size the member arrays, run discovery + plan + queue + inflate.
+    u64 n = e->n_cap;
+    u64 parts64 = n / 4096 + 2;
+    if (parts64 > tiles / 4096 + 3) {
+        if ((rc = ealloc(e, &e->scan_parts, parts64 + 1, err))) return rc;
+    }
+    if ((rc = ealloc(e, &e->cand, n, err)) || (rc = ealloc(e, &e->in_off, n, err)) ||
+        (rc = ealloc(e, &e->coffset, n + 1, err)) || (rc = ealloc(e, &e->out_off, n + 1, err)) ||
+        (rc = ealloc(e, &e->in_len, n, err)) || (rc = ealloc(e, &e->isize, n, err)) ||
+        (rc = ealloc(e, &e->crc_expect, n, err)) || (rc = ealloc(e, &e->order, n, err)) ||
+        (rc = ealloc(e, &e->hist, 1024, err)) || (rc = ealloc(e, &e->cursor, 1024, err)) ||
+        (rc = ealloc(e, &e->status, n, err)) || (rc = ealloc(e, &e->produced, n, err)) ||
+        (rc = ealloc(e, &e->crc, n, err)))
+        return rc;
+    // plan once to learn the inflated size
+    e->out_cap = 0;
+    e->out = nullptr;
+    if ((ce = enqueue_front(e)) != cudaSuccess) return cuda_fail(err, ce, "planning");
+    EngineDevState h{};
+    cudaMemcpyAsync(&h, e->st, sizeof h, cudaMemcpyDeviceToHost, s);
+    if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(err, ce, "planning");
+    if (h.tiling_failed && h.n_members > n) {
+        set_error(err, FRT_ERR_INVALID_BLOCK, 0, 0, 0, 0, nullptr, "BGZF members do not tile the buffer");
+        return FRT_ERR_INVALID_BLOCK;
+    }
+    e->out_cap = h.inflated_total;
+    if ((rc = ealloc(e, &e->out, e->out_cap + 64, err))) return rc;
+    if ((ce = enqueue_inflate(e)) != cudaSuccess) return cuda_fail(err, ce, "inflate");
+    // Record scan once to learn the record count.
+    if ((rc = ealloc(e, &e->entry, n, err)) || (rc = ealloc(e, &e->land, n, err)) ||
+        (rc = ealloc(e, &e->count, n, err)) || (rc = ealloc(e, &e->first, n, err)) ||
+        (rc = ealloc(e, &e->flags, n, err)) || (rc = ealloc(e, &e->scratch, n * FRT_SCAN_CAP, err)))
+        return rc;
+    if ((ce = enqueue_records(e, false)) != cudaSuccess) return cuda_fail(err, ce, "record scan");
+    cudaMemcpyAsync(&h, e->st, sizeof h, cudaMemcpyDeviceToHost, s);
+    if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(err, ce, "record scan");
+    e->host_state = h;
+    if ((rc = stats_from_state(e, nullptr, err))) return rc;
+    e->rec_cap = h.totals[0];
+    layout(e);
+    if ((rc = ealloc(e, &e->cols, layout_total(e), err))) return rc;
+    if ((rc = ealloc(e, &e->aux_parts, e->rec_cap / 4096 + 2, err))) return rc;
+    // aux count: decode once with no directory capacity, then size it
+    e->aux_cap = 0;
+    e->aux_entries = nullptr;
+    if ((ce = enqueue_records(e, true)) != cudaSuccess) return cuda_fail(err, ce, "decode");
+    cudaMemcpyAsync(&h, e->st, sizeof h, cudaMemcpyDeviceToHost, s);
+    if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(err, ce, "decode");
+    e->aux_cap = h.n_aux;
+    if ((rc = ealloc(e, &e->aux_entries, 3 * (e->aux_cap + 1), err))) return rc;
+    e->col_bytes[FRT_COL_AUX_ENTRIES] = 12 * e->aux_cap;
+    // Capture the steady state.
+    if (e->cfg.use_graph) {
+        ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (ce == cudaSuccess) {
+            enqueue_front(e);
+            enqueue_inflate(e);
+            enqueue_records(e, true);
+            ce = cudaStreamEndCapture(s, &e->graph);
+        }
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&e->exec, e->graph, 0);
+        if (ce != cudaSuccess) return cuda_fail(err, ce, "capturing the engine graph");
+    }
+    return FRT_OK;
+}
+
+extern "C" int frt_engine_run(frt_engine *e, frt_error *err)
+{
+    DeviceGuardLite g(e->device);
+    if (!e->in && e->len) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "no file bound");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    cudaError_t ce;
+    if (e->exec) {
+        ce = cudaGraphLaunch(e->exec, e->stream);
+    } else {
+        enqueue_front(e);
+        enqueue_inflate(e);
+        ce = enqueue_records(e, true);
+    }
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "launching the engine");
+    return FRT_OK;
+}
+
+extern "C" int frt_engine_finish(frt_engine *e, frt_engine_stats *stats, frt_error *err)
+{
+    DeviceGuardLite g(e->device);
+    cudaMemcpyAsync(&e->host_state, e->st, sizeof(EngineDevState), cudaMemcpyDeviceToHost, e->stream);
+    cudaError_t ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "engine run");
+    return stats_from_state(e, stats, err);
+}
+
+extern "C" int frt_engine_run_host(frt_engine *e, const uint8_t *host, size_t len, frt_engine_stats *stats,
+                                   frt_error *err)
+{
+    DeviceGuardLite g(e->device);
+    if (!e->in || len != e->len) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr,
+                  "bind a device buffer of this length first; run_host refills it from host memory");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    cudaError_t ce = cudaMemcpyAsync((void *)e->in, host, len, cudaMemcpyHostToDevice, e->stream);
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "uploading the file");
+    int rc = frt_engine_run(e, err);
+    if (rc) return rc;
+    return frt_engine_finish(e, stats, err);
+}
+
+extern "C" int frt_engine_column(const frt_engine *e, int column, void **ptr, size_t *bytes, size_t *width)
+{
+    if (!e || column < 0 || column >= FRT_COL_COUNT) return FRT_ERR_INVALID_ARGUMENT;
+    u64 n = e->host_state.totals[0] < e->rec_cap ? e->host_state.totals[0] : e->rec_cap;
+    if (ptr) *ptr = column == FRT_COL_AUX_ENTRIES ? (void *)e->aux_entries : (void *)(e->cols + e->col_off[column]);
+    if (bytes) {
+        if (column == FRT_COL_AUX_ENTRIES) *bytes = 12ull * e->host_state.n_aux;
+        else if (column == FRT_COL_AUX_FIRST) *bytes = 4ull * (n + 1);
+        else *bytes = bam_column_width(column) * n;
+    }
+    if (width) *width = bam_column_width(column);
+    return FRT_OK;
+}
+
+extern "C" int frt_engine_column_to_host(const frt_engine *e, int column, void *dst, size_t cap, frt_error *err)
+{
+    void *p = nullptr;
+    size_t bytes = 0;
+    if (frt_engine_column(e, column, &p, &bytes, nullptr)) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "bad column %d", column);
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    if (cap < bytes) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "destination too small");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    DeviceGuardLite g(e->device);
+    cudaError_t ce = cudaMemcpyAsync(dst, p, bytes, cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "downloading column");
+    return FRT_OK;
+}
+
+extern "C" const uint8_t *frt_engine_inflated(const frt_engine *e, size_t *len)
+{
+    if (len) *len = e ? e->host_state.inflated_total : 0;
+    return e ? e->out : nullptr;
+}
+
+extern "C" void *frt_engine_stream(const frt_engine *e) { return e ? (void *)e->stream : nullptr; }
+
+// Per-stage timing of an eager run (front / inflate / records), averaged over
+// `repeats` runs, with CUDA events on the engine stream.
+extern "C" int frt_engine_time_stages(frt_engine *e, float *ms, int repeats, frt_error *err)
+{
+    DeviceGuardLite g(e->device);
+    if (repeats < 1) repeats = 1;
+    cudaEvent_t ev[4];
+    for (auto &x : ev) cudaEventCreate(&x);
+    float acc[3] = {0, 0, 0};
+    cudaError_t ce = cudaSuccess;
+    for (int r = 0; r < repeats && ce == cudaSuccess; ++r) {
+        cudaEventRecord(ev[0], e->stream);
+        enqueue_front(e);
+        cudaEventRecord(ev[1], e->stream);
+        enqueue_inflate(e);
+        cudaEventRecord(ev[2], e->stream);
+        enqueue_records(e, true);
+        cudaEventRecord(ev[3], e->stream);
+        ce = cudaStreamSynchronize(e->stream);
+        for (int k = 0; k < 3 && ce == cudaSuccess; ++k) {
+            float t = 0;
+            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            acc[k] += t;
+        }
+    }
+    for (auto &x : ev) cudaEventDestroy(x);
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "timing stages");
+    for (int k = 0; k < 3; ++k) ms[k] = acc[k] / repeats;
+    return frt_engine_finish(e, nullptr, err);
+}
+
+// Kernels this library launches per engine run (the graph's kernel nodes).
+extern "C" uint64_t frt_engine_launches(const frt_engine *e)
+{
+    if (!e || !e->graph) return 0;
+    size_t n = 0;
+    cudaGraphGetNodes(e->graph, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    cudaGraphGetNodes(e->graph, nodes.data(), &n);
+    uint64_t k = 0;
+    for (auto &nd : nodes) {
+        cudaGraphNodeType t;
+        cudaGraphNodeGetType(nd, &t);
+        if (t == cudaGraphNodeTypeKernel) ++k;
+    }
+    return k;
+}

@@ -3,13 +3,23 @@
 
 #include "common.cuh"
 
-// Warps per CTA of the inflate kernels, decoded-output staging chunk and the
-// back-reference queue length per chunk.
+// Warps per CTA of the inflate kernels; per warp, the shared-memory ring of
+// recent output, the flush interval, and the queue of deferred matches.
 #ifndef INF_WARPS_PER_CTA
-#define INF_WARPS_PER_CTA 8
+#define INF_WARPS_PER_CTA 4
 #endif
-#define INF_CHUNK 2048
-#define INF_MAXM 192
+#ifndef INF_RING
+#define INF_RING 8192
+#endif
+#ifndef INF_FLUSH
+#define INF_FLUSH 2048
+#endif
+#ifndef INF_SEG
+#define INF_SEG 128
+#endif
+#ifndef INF_MAXQ
+#define INF_MAXQ 384
+#endif
 
 __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, void *smem, const u32 *crc_tab,
                                    u32 *produced_out, u32 *crc_out);
@@ -23,8 +33,10 @@ cudaError_t frt_launch_inflate_members(const u8 *in, const u64 *in_off, const u3
                                        const u64 *out_off, const u32 *out_cap, u32 *status, u32 *produced,
                                        u32 *crc, u32 n, cudaStream_t s);
 cudaError_t frt_launch_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out,
-                                          const u64 *out_off, const u32 *out_cap, u32 *status, u32 *produced,
-                                          u32 *crc, const u32 *order, const u32 *n_ptr, u32 *queue_head,
-                                          u32 chunk, u32 grid, cudaStream_t s);
+                                          const u64 *out_off, const u32 *isize, const u32 *crc_expect, u32 *status,
+                                          u32 *produced, u32 *crc, const u32 *order, const u64 *n_ptr, u64 n_cap,
+                                          u64 out_capacity, u32 *queue_head, u32 chunk, u32 grid,
+                                          unsigned long long *block_err, cudaStream_t s);
+int frt_inflate_persistent_grid();
 cudaError_t frt_launch_crc32_members(const u8 *data, const u64 *offsets, const u32 *lengths, u32 *out, u32 n,
                                      cudaStream_t s);

@@ -771,3 +771,38 @@ extern "C" void frt_reader_close(frt_reader *r)
     if (r->fd >= 0) close(r->fd);
     delete r;
 }
+
+// ===========================================================================
+// BAM header (crates/fritillaria-bam/src/columnar/header.rs:43-101)
+// ===========================================================================
+extern "C" int frt_bam_parse_header(const uint8_t *buf, size_t len, uint64_t *records_start, int32_t *n_ref,
+                                    frt_error *err)
+{
+    auto bad = [&](uint64_t pos, const char *why) {
+        set_error(err, FRT_ERR_MALFORMED, 0, 0, 0, pos, "bam header", "%s", why);
+        return FRT_ERR_MALFORMED;
+    };
+    if (len < 12) return bad(0, "truncated header");
+    if (memcmp(buf, "BAM\1", 4) != 0) return bad(0, "bad magic; expected BAM\\1");
+    int32_t l_text = (int32_t)rd32(buf + 4);
+    if (l_text < 0) return bad(4, "negative l_text");
+    uint64_t text_end = 8 + (uint64_t)l_text;
+    if (text_end > len) return bad(4, "l_text runs past the end of the buffer");
+    if (text_end + 4 > len) return bad(text_end, "truncated n_ref");
+    int32_t nr = (int32_t)rd32(buf + text_end);
+    if (nr < 0) return bad(text_end, "negative n_ref");
+    uint64_t pos = text_end + 4;
+    for (int32_t i = 0; i < nr; ++i) {
+        if (pos + 4 > len) return bad(pos, "truncated l_name");
+        int32_t l_name = (int32_t)rd32(buf + pos);
+        if (l_name < 0) return bad(pos, "negative l_name");
+        pos += 4;
+        if (pos + (uint64_t)l_name > len) return bad(pos, "truncated name");
+        pos += (uint64_t)l_name;
+        if (pos + 4 > len) return bad(pos, "truncated l_ref");
+        pos += 4;
+    }
+    if (records_start) *records_start = pos;
+    if (n_ref) *n_ref = nr;
+    return FRT_OK;
+}

@@ -157,6 +157,11 @@ void frt_reader_close(frt_reader *r);
 int frt_bgzf_discover(const uint8_t *buf, size_t len, uint64_t base_offset, frt_span *spans, size_t cap,
                       size_t *n_spans, size_t *consumed, frt_error *err);
 
+/* ---- BAM header, crates/fritillaria-bam/src/columnar/header.rs:43-101 ------
+ * Host parse of the header at the start of the first batch: where records
+ * begin and how many references there are. */
+int frt_bam_parse_header(const uint8_t *buf, size_t len, uint64_t *records_start, int32_t *n_ref, frt_error *err);
+
 /* ---- BamDecoder, crates/fritillaria-cuda/src/bam.rs:113-187 --------------- */
 
 int frt_bam_decoder_create(int device, void *stream, frt_bam_decoder **out, frt_error *err);
@@ -250,7 +255,13 @@ int frt_engine_finish(frt_engine *e, frt_engine_stats *stats, frt_error *err);
 int frt_engine_run_host(frt_engine *e, const uint8_t *host_bgzf, size_t len, frt_engine_stats *stats,
                         frt_error *err);
 int frt_engine_column(const frt_engine *e, int column, void **ptr, size_t *bytes, size_t *width);
+int frt_engine_column_to_host(const frt_engine *e, int column, void *dst, size_t cap, frt_error *err);
 const uint8_t *frt_engine_inflated(const frt_engine *e, size_t *len);
+void *frt_engine_stream(const frt_engine *e);
+/* Per-stage milliseconds (front, inflate, records) of eager runs. */
+int frt_engine_time_stages(frt_engine *e, float *ms, int repeats, frt_error *err);
+/* Kernel launches per run (kernel nodes of the captured graph). */
+uint64_t frt_engine_launches(const frt_engine *e);
 
 #ifdef __cplusplus
 }

@@ -29,8 +29,8 @@ def drive(frt, bgzf, blocks):
         if header is None:
             host = batch.data.to_host()
             try:
-                header = oracle.bam_header(host)
-            except oracle.OracleError:
+                header = frt.parse_header(host)
+            except frt.Malformed:
                 reader.carry_from(0)
                 continue
             decoder.set_reference_count(header[1])
