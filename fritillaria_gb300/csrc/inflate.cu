@@ -2,29 +2,27 @@
 // of the output folded in.
 //
 // A DEFLATE stream is a serial chain: a symbol's bit position is known only
-// once the previous symbol is decoded.  So one lane (lane 0) walks the chain,
-// and the other 31 lanes take everything that is not on it.  What the
-// measurements of BGZF'd BAM drove the design to:
+// once the previous symbol is decoded, and on GB300 one link of that chain --
+// a shared-memory table lookup feeding a 64-bit shift feeding the next lookup
+// -- costs ~120 cycles.  So lane 0 walks the chain and does nothing else, and
+// the other 31 lanes take all the work that is not on it:
 //
-//   * a 64 KiB member of short reads holds ~20k literals and ~10k matches of
-//     4.4 bytes on average, with distances spread over the whole 32 KiB
-//     window (62% within 4 KiB, 84% within 16 KiB).  Matches, not literals,
-//     dominate if each one is a round trip to L2.
-//   * So output goes through a shared-memory ring of the last INF_RING bytes.
-//     Lane 0 writes literals into it and copies a match whose source is in
-//     the ring immediately (ring to ring).  A match reaching further back
-//     ("far") is queued and its destination marked pending in a bitmap; a
-//     near match whose source touches a pending byte is queued behind it.
-//   * Every INF_FLUSH bytes the warp services the ring: far matches are
-//     copied in parallel (one lane each) from the member's output already in
-//     HBM, queued near matches in order, then the chunk is written to HBM
-//     with coalesced stores and its CRC-32 is computed from shared memory in
-//     32 slices merged by the GF(2) shift-and-xor combine.
-//   * Decode tables are 16-bit entries in shared memory: a 10-bit
-//     literal/length table and an 8-bit distance table, built by the whole
-//     warp (counts by shared atomics, symbols sorted by __match_any_sync
-//     ranking, entries filled in parallel from canonical-code limits); codes
-//     longer than the root take a canonical-limit search.
+//   * Decode tables are 32-bit entries in shared memory that carry a symbol
+//     with its extra bits (one lookup and one shift per literal, two per
+//     match): a 10-bit literal/length root and an 8-bit distance root side by
+//     side, codes longer than the root taking a canonical-limit search.  The
+//     warp builds them (counts by shared atomics, symbols ranked with
+//     __match_any_sync, entries filled in parallel from canonical limits).
+//   * Lane 0 writes literals into a shared-memory window buffer and queues
+//     matches.  A 64 KiB member of short reads holds ~20k literals and ~10k
+//     matches of 4.4 bytes whose sources spread over the whole 32 KiB window,
+//     so copying them on the chain would stall it on L2 round trips.
+//   * When the buffer or the queue is full, the warp resolves the queued
+//     matches in parallel rounds (each copied once its source bytes are
+//     final; sources before the window come from the member's output already
+//     in HBM, loaded in groups so the loads overlap), writes the window to HBM
+//     with coalesced stores and folds its CRC-32 in, computed from shared
+//     memory in 32 slices merged by the GF(2) shift-and-xor combine.
 //   * Stored blocks are copied by the whole warp.
 //
 // RFC 1951 is the specification; the checks and status codes follow the
@@ -36,18 +34,14 @@
 
 namespace {
 
-constexpr int LIT_BITS = 10;
-constexpr int DIST_BITS = 8;
+constexpr int LIT_BITS = INF_LIT_BITS;
+constexpr int DIST_BITS = INF_DIST_BITS;
 constexpr int CL_BITS = 7;
-constexpr u32 RING = INF_RING;
-constexpr u32 RMASK = RING - 1;
-constexpr u32 FLUSH = INF_FLUSH;
-constexpr u32 SEG = INF_SEG;   // bits of one lane's segment in a window
-constexpr u32 MAXQ = INF_MAXQ; // matches queued per window
-static_assert((RING & (RING - 1)) == 0, "ring size must be a power of two");
-static_assert(RING >= FLUSH + 6144, "the ring holds the unflushed bytes plus a window's output");
-static_assert(SEG % 32 == 0, "a segment is whole mark words");
+constexpr u32 DIST_BASE = 1u << LIT_BITS; // distance entries follow the literal/length ones
+constexpr u32 WB = INF_WINBUF;            // window output buffer (bytes)
+constexpr u32 MAXQ = INF_MAXQ;            // matches per window
 static_assert(MAXQ <= 32 * 32, "a lane tracks at most 32 queued matches");
+static_assert(WB % 32 == 0, "pending bits cover whole words");
 
 struct CodeState {
     u32 count[16];
@@ -55,30 +49,28 @@ struct CodeState {
     u16 offs[16];  // index in `sorted` of the first symbol of each length
 };
 
-// Decode-table entries (32 bits), so the serial chain does one lookup and one
-// shift per symbol:
-//   [4:0]   bits to consume: the code, plus a length/distance code's extra bits
+// Decode-table entries (32 bits), so one lookup and one shift take a symbol
+// with its extra bits:
+//   [4:0]   bits to consume: the code plus its extra bits
 //   [7:5]   kind: 0 literal (or a valid distance), 1 length, 2 end of block,
 //           3 invalid symbol
 //   [11:8]  the code's own length (where its extra bits start)
 //   [15:12] extra bits
 //   [31:16] literal byte, or length/distance base
-// An entry of 0 means no code of at most the table's root length matches:
-// the long-code path.
+// An entry of 0 means no code of at most the root length matches: the
+// long-code path.
 struct WarpSmem {
-    u32 lit[1 << LIT_BITS];
-    u32 dist[1 << DIST_BITS];
+    u32 tab[DIST_BASE + (1u << DIST_BITS)];
     CodeState lcode;
     CodeState dcode;
     u16 lsorted[288];
     u16 dsorted[32];
     u32 run[16];
-    u32 pend[RING / 32]; // unresolved match destinations, relative to the last flush
-    u32 marks[SEG];      // token starts found by each lane in its own segment
-    u32 q_dst[MAXQ];     // matches of the current window: destination
-    u32 q_ld[MAXQ];      //   len | dist << 9
+    u32 pend[WB / 32];    // unresolved match destinations in the window
+    u32 q_dst[MAXQ];      // matches of the window: destination (member offset)
+    u32 q_ld[MAXQ];       //   len | dist << 9
     u8 lens[320];
-    u8 ring[RING];
+    u8 win[WB + 264];
 };
 
 __device__ __forceinline__ u32 lit_entry(u32 sym, u32 L)
@@ -237,56 +229,8 @@ struct LaneBits {
     }
 };
 
-enum : u32 { TK_LIT = 0, TK_MATCH = 1, TK_EOB = 2, TK_BADCODE = 3, TK_BADDIST = 4 };
-
-// One token of a Huffman block: a literal, a length/distance pair or the
-// end of block.  Returns the kind; *v is the literal or the length.
-__device__ __forceinline__ u32 decode_token(LaneBits &r, const WarpSmem *sm, u32 *v, u32 *dist)
-{
-    r.refill();
-    u32 e = sm->lit[(u32)r.buf & ((1u << LIT_BITS) - 1u)];
-    if (e == 0) {
-        u32 sym, L = decode_long(r.buf, LIT_BITS, &sm->lcode, sm->lsorted, &sym);
-        if (L == 0) {
-            r.drop(15); // the reference reads 15 bits before giving up
-            return TK_BADCODE;
-        }
-        e = lit_entry(sym, L);
-    }
-    u32 kind = (e >> 5) & 7u;
-    if (kind == 0) {
-        *v = e >> 16;
-        r.drop((int)(e & 31u));
-        return TK_LIT;
-    }
-    if (kind != 1) {
-        r.drop((int)(e & 31u));
-        return kind == 2 ? TK_EOB : TK_BADCODE;
-    }
-    u32 len = (e >> 16) + ((u32)(r.buf >> ((e >> 8) & 15u)) & ((1u << ((e >> 12) & 15u)) - 1u));
-    r.drop((int)(e & 31u));
-    r.refill();
-    u32 d = sm->dist[(u32)r.buf & ((1u << DIST_BITS) - 1u)];
-    if (d == 0) {
-        u32 sym, L = decode_long(r.buf, DIST_BITS, &sm->dcode, sm->dsorted, &sym);
-        if (L == 0) {
-            r.drop(15);
-            return TK_BADDIST;
-        }
-        d = dist_entry(sym, L);
-    }
-    if ((d >> 5) & 7u) {
-        r.drop((int)(d & 31u));
-        return TK_BADDIST;
-    }
-    *dist = (d >> 16) + ((u32)(r.buf >> ((d >> 8) & 15u)) & ((1u << ((d >> 12) & 15u)) - 1u));
-    r.drop((int)(d & 31u));
-    *v = len;
-    return TK_MATCH;
-}
-
-// Pending-bit helpers over the ring (offsets relative to the last flush).
-// Destinations of different matches can share a word, hence the atomics.
+// Pending-bit helpers over the window buffer.  Destinations of different
+// matches can share a word, hence the atomics.
 __device__ __forceinline__ void pend_set(u32 *pend, u32 a, u32 b, bool on)
 {
     while (a < b) {
@@ -314,19 +258,18 @@ __device__ __forceinline__ bool pend_any(const u32 *pend, u32 a, u32 b)
 // Resolves the window's nq queued matches in parallel rounds: in each round
 // every match whose source bytes are final is copied, one lane per match.
 // The earliest unresolved match is always ready, so rounds make progress.
-// A source byte still in the ring (at or after pos - RING) is read there;
-// anything older has been flushed and is read from HBM.
-__device__ void resolve(WarpSmem *sm, const u8 *out, u32 flushed, u32 pos, u32 nq)
+// A source byte before the window (wstart) is read from HBM, where earlier
+// windows were written; a byte inside it from the window buffer.
+__device__ void resolve(WarpSmem *sm, const u8 *out, u32 wstart, u32 nq)
 {
     const u32 lane = lane_id();
     for (u32 k = lane; k < nq; k += 32) {
         u32 d = sm->q_dst[k];
-        pend_set(sm->pend, d - flushed, d + (sm->q_ld[k] & 511u) - flushed, true);
+        pend_set(sm->pend, d - wstart, d + (sm->q_ld[k] & 511u) - wstart, true);
     }
     __syncwarp();
     u32 todo = 0;
     for (u32 j = 0; lane + 32 * j < nq; ++j) todo |= 1u << j;
-    const u32 ring_lo = pos > RING ? pos - RING : 0u;
     while (__any_sync(FRT_FULL_MASK, todo != 0)) {
         u32 ready = 0;
         for (u32 t = todo; t; t &= t - 1) {
@@ -334,41 +277,50 @@ __device__ void resolve(WarpSmem *sm, const u8 *out, u32 flushed, u32 pos, u32 n
             u32 d = sm->q_dst[k], ld = sm->q_ld[k];
             u32 len = ld & 511u, dist = ld >> 9;
             u32 s = d - dist, e = s + min(len, dist);
-            if (e <= flushed || !pend_any(sm->pend, max(s, flushed) - flushed, e - flushed)) ready |= 1u << j;
+            if (e <= wstart || !pend_any(sm->pend, max(s, wstart) - wstart, e - wstart)) ready |= 1u << j;
         }
         __syncwarp();
         for (u32 t = ready; t; t &= t - 1) {
             u32 j = __ffs(t) - 1, k = lane + 32 * j;
             u32 d = sm->q_dst[k], ld = sm->q_ld[k];
             u32 len = ld & 511u, s = d - (ld >> 9);
-            for (u32 i = 0; i < len; ++i) {
-                u32 p = s + i;
-                u8 b = p >= ring_lo ? sm->ring[p & RMASK] : out[p];
-                sm->ring[(d + i) & RMASK] = b;
+            u32 i = 0;
+            // bytes before the window: gather in groups so the HBM loads overlap
+            while (i < len && s + i < wstart) {
+                u32 n = min(min(8u, len - i), wstart - (s + i));
+                u8 b[8];
+#pragma unroll
+                for (u32 x = 0; x < 8; ++x)
+                    if (x < n) b[x] = out[s + i + x];
+#pragma unroll
+                for (u32 x = 0; x < 8; ++x)
+                    if (x < n) sm->win[d + i + x - wstart] = b[x];
+                i += n;
             }
+            for (; i < len; ++i) sm->win[d + i - wstart] = sm->win[s + i - wstart];
         }
         __syncwarp();
         for (u32 t = ready; t; t &= t - 1) {
             u32 j = __ffs(t) - 1, k = lane + 32 * j;
             u32 d = sm->q_dst[k];
-            pend_set(sm->pend, d - flushed, d + (sm->q_ld[k] & 511u) - flushed, false);
+            pend_set(sm->pend, d - wstart, d + (sm->q_ld[k] & 511u) - wstart, false);
         }
         todo &= ~ready;
         __syncwarp();
     }
 }
 
-// Writes [flushed, pos) to HBM with coalesced stores and folds its CRC into
-// *crc: 32 slices from shared memory, merged pairwise by the GF(2) combine.
-__device__ void flush_crc(const WarpSmem *sm, u8 *out, u32 flushed, u32 pos, const u32 *crc_tab, u32 *crc)
+// Writes the window's n bytes to out[wstart, wstart + n) with coalesced
+// stores and folds their CRC into *crc: 32 slices from shared memory, merged
+// pairwise by the GF(2) combine.
+__device__ void write_window(const WarpSmem *sm, u8 *out, u32 wstart, u32 n, const u32 *crc_tab, u32 *crc)
 {
     const u32 lane = lane_id();
-    u32 F = pos - flushed;
-    for (u32 j = lane; j < F; j += 32) out[flushed + j] = sm->ring[(flushed + j) & RMASK];
-    u32 slice = (F + 31) / 32;
-    u32 b0 = min(F, lane * slice), b1 = min(F, b0 + slice);
+    for (u32 j = lane; j < n; j += 32) out[wstart + j] = sm->win[j];
+    u32 slice = (n + 31) / 32;
+    u32 b0 = min(n, lane * slice), b1 = min(n, b0 + slice);
     u32 c = 0xffffffffu;
-    for (u32 i = b0; i < b1; ++i) c = crc_tab[(c ^ sm->ring[(flushed + i) & RMASK]) & 0xffu] ^ (c >> 8);
+    for (u32 i = b0; i < b1; ++i) c = crc_tab[(c ^ sm->win[i]) & 0xffu] ^ (c >> 8);
     c = ~c;
     u32 mylen = b1 - b0;
     for (int d = 1; d < 32; d <<= 1) {
@@ -380,295 +332,100 @@ __device__ void flush_crc(const WarpSmem *sm, u8 *out, u32 flushed, u32 pos, con
         }
     }
     c = __shfl_sync(FRT_FULL_MASK, c, 0);
-    *crc = crc_combine(*crc, c, F);
+    *crc = crc_combine(*crc, c, n);
     __syncwarp();
 }
 
-// Errors found on the true chain, ranked by bit position so the earliest
-// one is reported, as a sequential decoder would.
-__device__ __forceinline__ u64 err_key(u32 bitpos, u32 code) { return ((u64)bitpos << 8) | code; }
-
-struct Window {
-    u32 next;   // bit position where decoding continues
-    u32 status; // INF_OK or the first error
-    int eob;    // the block ended in this window
-};
-
-// One window of a Huffman block, decoded by all 32 lanes.
-//
-//   A  lane k decodes the tokens that start in its segment
-//      [bitpos + k*SEG, bitpos + (k+1)*SEG) from the segment start -- a
-//      guess, except for lane 0 -- and marks each token start.
-//   B  lane k continues its chain into segment k+1 until it reaches a start
-//      that lane k+1 marked.  From there the two decodings agree (decoding is
-//      deterministic from a true boundary), so lane k+1's chain is proven by
-//      lane k's, and by induction from lane 0 every lane up to the first one
-//      that did not synchronise is on the true chain.
-//   C  each proven lane re-decodes its true range, counting output bytes and
-//      matches and finding the end of block or an error.
-//   D  after a warp scan places every range in the output, each lane decodes
-//      its range once more, writing literals into the ring and queueing
-//      matches; then the matches are resolved in parallel rounds.
-// A lane that did not synchronise within the next segment ends the window at
-// its last proven token; the next window starts there.
-__device__ Window decode_window(WarpSmem *sm, LaneBits &r, u32 bitpos, u32 total, u8 *out, u32 flushed, u32 *pos_io,
-                                u32 cap)
+// One window of a Huffman block.  Lane 0 walks the serial chain -- one
+// table lookup and one shift per symbol, literals into the window buffer,
+// matches into the queue -- until the buffer or the queue is full or the
+// block ends; the warp then resolves the queued matches in parallel rounds
+// and writes the window to HBM with its CRC.  Truncation is checked once per
+// burst: bits past the payload read as zero, and a symbol that used one is
+// where a sequential decoder reports it.
+__device__ u32 decode_burst(WarpSmem *sm, LaneBits &r, u32 total, u8 *out, u32 *pos_io, u32 cap, const u32 *crc_tab,
+                            u32 *crc, int *eob_out)
 {
     const u32 lane = lane_id();
     const u32 pos = *pos_io;
-    for (u32 w = lane; w < SEG; w += 32) sm->marks[w] = 0;
-    __syncwarp();
-    // ---- A
-    const u32 s0 = bitpos + lane * SEG, s1 = s0 + SEG;
-    u32 exitp = s0;
-    if (s0 < total) {
-        u32 p = s0;
-        r.seek(p);
-        while (p < s1 && p < total) {
-            u32 v, dd;
-            u32 k = decode_token(r, sm, &v, &dd);
-            if (k >= TK_BADCODE) { // not a token start: slide one bit
-                ++p;
-                r.seek(p);
+    u32 o = 0, nq = 0, status = INF_OK;
+    int eob = 0;
+    if (lane == 0) {
+        const bool checked = cap - pos < WB; // near the declared size: check every symbol
+        while (o < WB - 258u && nq < MAXQ) {
+            r.refill();
+            u32 e = sm->tab[(u32)r.buf & ((1u << LIT_BITS) - 1u)];
+            if (e == 0) {
+                u32 sym, L = decode_long(r.buf, LIT_BITS, &sm->lcode, sm->lsorted, &sym);
+                if (L == 0) {
+                    r.drop(15); // the reference reads 15 bits before giving up
+                    status = INF_BAD_CODE;
+                    break;
+                }
+                e = lit_entry(sym, L);
+            }
+            const u32 kind = (e >> 5) & 7u;
+            if (kind == 0) {
+                if (checked && pos + o >= cap) {
+                    status = INF_OUTPUT_OVERFLOW;
+                    break;
+                }
+                sm->win[o++] = (u8)(e >> 16);
+                r.drop((int)(e & 31u));
                 continue;
             }
-            u32 rel = p - bitpos;
-            sm->marks[rel >> 5] |= 1u << (rel & 31u);
-            p = r.tell();
-        }
-        exitp = p;
-    }
-    __syncwarp();
-    // ---- B
-    enum { SYNC = 0, FAIL = 1, END = 2, STOP = 3, LAST = 4 };
-    u32 outcome = END, q = exitp;
-    if (lane < 31) {
-        const u32 s2 = s1 + SEG;
-        r.seek(q);
-        while (true) {
-            if (q >= total) {
-                outcome = END;
+            if (kind != 1) {
+                r.drop((int)(e & 31u));
+                if (kind == 2) eob = 1;
+                else status = INF_BAD_CODE;
                 break;
             }
-            if (q >= s2) {
-                outcome = FAIL;
-                break;
-            }
-            u32 rel = q - bitpos;
-            if ((sm->marks[rel >> 5] >> (rel & 31u)) & 1u) {
-                outcome = SYNC;
-                break;
-            }
-            u32 v, dd;
-            u32 k = decode_token(r, sm, &v, &dd);
-            if (k >= TK_EOB) { // end of block or an error: pass C reports it
-                outcome = STOP;
-                break;
-            }
-            q = r.tell();
-        }
-    } else {
-        outcome = LAST; // lane 31's range ends with its segment
-        q = exitp;
-    }
-    u32 notsync = __ballot_sync(FRT_FULL_MASK, outcome != SYNC);
-    const u32 V = __ffs(notsync) - 1; // lanes 0..V are on the true chain
-    u32 prevq = __shfl_up_sync(FRT_FULL_MASK, q, 1);
-    const u32 start = lane == 0 ? bitpos : prevq;
-    u32 end = q;
-    if (lane == V && (outcome == STOP || outcome == END)) end = 0xffffffffu; // run until the stop itself
-    // ---- C
-    u32 nbytes = 0, nmatch = 0, cstop = 0, cpos = 0; // cstop: 0 none, 1 eob, else an INF_ error
-    if (lane <= V) {
-        u32 p = start;
-        r.seek(p);
-        while (p < end) {
-            if (p >= total) {
-                cstop = INF_TRUNCATED;
-                cpos = p;
-                break;
-            }
-            u32 v, dd;
-            u32 k = decode_token(r, sm, &v, &dd);
-            u32 np = r.tell();
-            if (np > total) {
-                cstop = INF_TRUNCATED;
-                cpos = p;
-                break;
-            }
-            if (k == TK_EOB) {
-                cstop = 1;
-                cpos = np;
-                break;
-            }
-            if (k == TK_BADCODE) {
-                cstop = INF_BAD_CODE;
-                cpos = p;
-                break;
-            }
-            if (k == TK_BADDIST) {
-                cstop = INF_BAD_DISTANCE;
-                cpos = p;
-                break;
-            }
-            nbytes += k == TK_LIT ? 1u : v;
-            nmatch += k == TK_MATCH ? 1u : 0u;
-            p = np;
-        }
-        if (!cstop) cpos = p;
-    }
-    // the first lane that stopped ends the true chain
-    u32 stopped = __ballot_sync(FRT_FULL_MASK, lane <= V && cstop != 0);
-    u32 last = stopped ? (u32)(__ffs(stopped) - 1) : V;
-    // place the ranges; keep the prefix that fits the ring and the queue
-    u32 inc_b = lane <= last ? nbytes : 0u, inc_m = lane <= last ? nmatch : 0u;
-    for (int d = 1; d < 32; d <<= 1) {
-        u32 yb = __shfl_up_sync(FRT_FULL_MASK, inc_b, d), ym = __shfl_up_sync(FRT_FULL_MASK, inc_m, d);
-        if (lane >= (u32)d) {
-            inc_b += yb;
-            inc_m += ym;
-        }
-    }
-    const u32 budget = RING - 258u - (pos - flushed);
-    u32 fits = __ballot_sync(FRT_FULL_MASK, lane <= last && inc_b <= budget && inc_m <= MAXQ);
-    u32 cut = fits == 0xffffffffu ? 32u : (u32)(__ffs(~fits) - 1); // lanes [0, cut) kept; fits is a prefix
-    if (cut > last + 1) cut = last + 1;
-    Window w;
-    w.status = INF_OK;
-    w.eob = 0;
-    if (cut == 0) {
-        // lane 0's range alone overflows the ring: only lane 0 proceeds, one
-        // token at a time, through the serial path of the caller
-        w.next = bitpos;
-        w.status = 0xffffffffu;
-        return w;
-    }
-    const u32 base_b = inc_b - (lane <= last ? nbytes : 0u);
-    const u32 base_m = inc_m - (lane <= last ? nmatch : 0u);
-    const u32 tot_b = __shfl_sync(FRT_FULL_MASK, inc_b, cut - 1);
-    const u32 tot_m = __shfl_sync(FRT_FULL_MASK, inc_m, cut - 1);
-    // ---- D
-    u64 ekey = ~0ull;
-    if (lane < cut) {
-        u32 p = start, o = pos + base_b, m = base_m;
-        u32 lim = lane == last ? cpos : end;
-        r.seek(p);
-        while (p < lim) {
-            u32 v, dd;
-            u32 k = decode_token(r, sm, &v, &dd);
-            if (k == TK_LIT) {
-                if (o >= cap) {
-                    ekey = err_key(p, INF_OUTPUT_OVERFLOW);
+            u32 len = (e >> 16) + ((u32)(r.buf >> ((e >> 8) & 15u)) & ((1u << ((e >> 12) & 15u)) - 1u));
+            r.drop((int)(e & 31u));
+            r.refill();
+            u32 d = sm->tab[DIST_BASE + ((u32)r.buf & ((1u << DIST_BITS) - 1u))];
+            if (d == 0) {
+                u32 sym, L = decode_long(r.buf, DIST_BITS, &sm->dcode, sm->dsorted, &sym);
+                if (L == 0) {
+                    r.drop(15);
+                    status = INF_BAD_DISTANCE;
                     break;
                 }
-                sm->ring[o & RMASK] = (u8)v;
-                ++o;
-            } else if (k == TK_MATCH) {
-                if (dd > o) {
-                    ekey = err_key(p, INF_BAD_DISTANCE);
-                    break;
-                }
-                if (o + v > cap) {
-                    ekey = err_key(p, INF_OUTPUT_OVERFLOW);
-                    break;
-                }
-                sm->q_dst[m] = o;
-                sm->q_ld[m] = v | (dd << 9);
-                ++m;
-                o += v;
-            } else {
-                break; // the end of block (only in the last lane's range)
+                d = dist_entry(sym, L);
             }
-            p = r.tell();
-        }
-        if (lane == last && lane < cut && cstop > 1 && ekey == ~0ull) ekey = err_key(cpos, cstop);
-    }
-    // earliest error on the chain
-    for (int d = 16; d; d >>= 1) {
-        u64 o = __shfl_xor_sync(FRT_FULL_MASK, ekey, d);
-        ekey = o < ekey ? o : ekey;
-    }
-    __syncwarp();
-    if (ekey != ~0ull) {
-        w.status = (u32)(ekey & 0xffu);
-        w.next = (u32)(ekey >> 8);
-        return w;
-    }
-    resolve(sm, out, flushed, pos + tot_b, tot_m);
-    *pos_io = pos + tot_b;
-    u32 nextp = __shfl_sync(FRT_FULL_MASK, start, cut < 32 ? cut : 0);
-    if (cut <= last) {
-        w.next = nextp; // continue at the first range that did not fit
-    } else {
-        u32 lastp = __shfl_sync(FRT_FULL_MASK, cpos, last);
-        u32 lasts = __shfl_sync(FRT_FULL_MASK, cstop, last);
-        w.next = lastp;
-        w.eob = lasts == 1;
-    }
-    return w;
-}
-
-// The rare path for a range whose output does not fit a window: lane 0
-// decodes token by token, the warp flushing the ring between tokens.
-__device__ u32 decode_serial_range(WarpSmem *sm, LaneBits &r, u32 *bitpos_io, u32 total, u8 *out, u32 *flushed_io,
-                                   u32 *pos_io, u32 cap, u32 tokens, const u32 *crc_tab, u32 *crc, int *eob)
-{
-    const u32 lane = lane_id();
-    u32 bitpos = *bitpos_io, status = INF_OK;
-    for (u32 t = 0; t < tokens; ++t) {
-        u32 kind = 0, v = 0, dd = 0, np = 0;
-        if (lane == 0) {
-            r.seek(bitpos);
-            kind = decode_token(r, sm, &v, &dd);
-            np = r.tell();
-        }
-        kind = __shfl_sync(FRT_FULL_MASK, kind, 0);
-        v = __shfl_sync(FRT_FULL_MASK, v, 0);
-        dd = __shfl_sync(FRT_FULL_MASK, dd, 0);
-        np = __shfl_sync(FRT_FULL_MASK, np, 0);
-        if (np > total) status = INF_TRUNCATED;
-        else if (kind == TK_BADCODE) status = INF_BAD_CODE;
-        else if (kind == TK_BADDIST) status = INF_BAD_DISTANCE;
-        if (status != INF_OK) break;
-        if (kind == TK_EOB) {
-            *eob = 1;
-            bitpos = np;
-            break;
-        }
-        u32 n = kind == TK_LIT ? 1u : v;
-        if (*pos_io - *flushed_io + n > RING - 258u) {
-            flush_crc(sm, out, *flushed_io, *pos_io, crc_tab, crc);
-            *flushed_io = *pos_io;
-        }
-        u32 o = *pos_io;
-        if (kind == TK_LIT) {
-            if (o >= cap) {
-                status = INF_OUTPUT_OVERFLOW;
-                break;
-            }
-            if (lane == 0) sm->ring[o & RMASK] = (u8)v;
-        } else {
-            if (dd > o) {
+            if ((d >> 5) & 7u) {
+                r.drop((int)(d & 31u));
                 status = INF_BAD_DISTANCE;
                 break;
             }
-            if (o + v > cap) {
+            u32 dist = (d >> 16) + ((u32)(r.buf >> ((d >> 8) & 15u)) & ((1u << ((d >> 12) & 15u)) - 1u));
+            r.drop((int)(d & 31u));
+            const u32 dst = pos + o;
+            if (dist > dst) {
+                status = INF_BAD_DISTANCE;
+                break;
+            }
+            if (checked && dst + len > cap) {
                 status = INF_OUTPUT_OVERFLOW;
                 break;
             }
-            if (lane == 0) {
-                sm->q_dst[0] = o;
-                sm->q_ld[0] = v | (dd << 9);
-            }
-            __syncwarp();
-            resolve(sm, out, *flushed_io, o + v, 1);
+            sm->q_dst[nq] = dst;
+            sm->q_ld[nq] = len | (dist << 9);
+            ++nq;
+            o += len;
         }
-        __syncwarp();
-        *pos_io = o + n;
-        bitpos = np;
+        if (r.tell() > total) status = INF_TRUNCATED; // a symbol needed bits past the payload
     }
-    *bitpos_io = bitpos;
-    return status;
+    status = __shfl_sync(FRT_FULL_MASK, status, 0);
+    *eob_out = __shfl_sync(FRT_FULL_MASK, eob, 0);
+    o = __shfl_sync(FRT_FULL_MASK, o, 0);
+    nq = __shfl_sync(FRT_FULL_MASK, nq, 0);
+    __syncwarp();
+    if (status != INF_OK) return status;
+    resolve(sm, out, pos, nq);
+    write_window(sm, out, pos, o, crc_tab, crc);
+    *pos_io = pos + o;
+    return INF_OK;
 }
 
 } // namespace
@@ -682,13 +439,12 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
     const u32 lane = lane_id();
     LaneBits r;
     r.attach(in, in_len);
-    for (u32 w = lane; w < RING / 32; w += 32) sm->pend[w] = 0;
+    for (u32 w = lane; w < WB / 32; w += 32) sm->pend[w] = 0;
     __syncwarp();
     const u32 total = 8u * in_len;
-    u32 bitpos = 0;  // next unread bit of the stream (warp-uniform)
-    u32 pos = 0;     // bytes decoded
-    u32 flushed = 0; // bytes written to HBM
-    u32 crc = 0;     // CRC-32 of [0, flushed)
+    u32 bitpos = 0; // next unread bit of the stream (warp-uniform)
+    u32 pos = 0;    // bytes produced and written
+    u32 crc = 0;    // CRC-32 of [0, pos)
     u32 status = INF_OK;
     int last = 0;
 
@@ -714,7 +470,7 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
         }
 
         if (type == 0) {
-            // ---- stored block: copied by the whole warp through the ring ----
+            // ---- stored block: copied by the whole warp -----------------------
             u32 bytepos = (bitpos + 7) / 8, len = 0;
             if (lane == 0) {
                 if (bytepos + 4 > in_len) {
@@ -734,13 +490,10 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
             const u8 *src = in + bytepos + 4;
             bitpos = 8u * (bytepos + 4 + len);
             while (len) {
-                if (pos - flushed >= FLUSH) {
-                    flush_crc(sm, out, flushed, pos, crc_tab, &crc);
-                    flushed = pos;
-                }
-                u32 n = min(len, FLUSH - (pos - flushed));
-                for (u32 j = lane; j < n; j += 32) sm->ring[(pos + j) & RMASK] = src[j];
+                u32 n = min(len, WB);
+                for (u32 j = lane; j < n; j += 32) sm->win[j] = src[j];
                 __syncwarp();
+                write_window(sm, out, pos, n, crc_tab, &crc);
                 pos += n;
                 src += n;
                 len -= n;
@@ -753,10 +506,10 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
         if (type == 1) {
             for (int s = lane; s < 288; s += 32) sm->lens[s] = s < 144 ? 8 : (s < 256 ? 9 : (s < 280 ? 7 : 8));
             __syncwarp();
-            build_table(sm->lens, 288, LIT_BITS, sm->lit, sm->lsorted, &sm->lcode, sm->run, 0);
+            build_table(sm->lens, 288, LIT_BITS, sm->tab, sm->lsorted, &sm->lcode, sm->run, 0);
             sm->lens[lane] = 5;
             __syncwarp();
-            build_table(sm->lens, 32, DIST_BITS, sm->dist, sm->dsorted, &sm->dcode, sm->run, 1);
+            build_table(sm->lens, 32, DIST_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode, sm->run, 1);
         } else {
             int nlen = 0, ndist = 0, ncode = 0;
             u32 bp = bitpos;
@@ -794,7 +547,7 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
             __syncwarp();
             // the code-length code must be complete (all-zero counts as
             // complete and fails at first use, as in the reference)
-            if (build_table(sm->lens, 19, CL_BITS, sm->dist, sm->dsorted, &sm->dcode, sm->run, 2) != 0) {
+            if (build_table(sm->lens, 19, CL_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode, sm->run, 2) != 0) {
                 status = INF_BAD_TABLE;
                 break;
             }
@@ -803,7 +556,7 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
                 r.seek(bp);
                 while (index < nlen + ndist) {
                     r.refill();
-                    u32 e = sm->dist[r.peek(CL_BITS)];
+                    u32 e = sm->tab[DIST_BASE + r.peek(CL_BITS)];
                     u32 L = e & 31u;
                     u32 left = total - min(total, r.tell());
                     if (L == 0) {
@@ -848,12 +601,13 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
             if (status != INF_OK) break;
             bitpos = __shfl_sync(FRT_FULL_MASK, bp, 0);
             __syncwarp();
-            int rl = build_table(sm->lens, nlen, LIT_BITS, sm->lit, sm->lsorted, &sm->lcode, sm->run, 0);
+            int rl = build_table(sm->lens, nlen, LIT_BITS, sm->tab, sm->lsorted, &sm->lcode, sm->run, 0);
             if (rl != 0 && (rl < 0 || nlen != (int)sm->lcode.count[0] + 1)) { // incomplete only with one code
                 status = INF_BAD_TABLE;
                 break;
             }
-            int rd = build_table(sm->lens + nlen, ndist, DIST_BITS, sm->dist, sm->dsorted, &sm->dcode, sm->run, 1);
+            int rd = build_table(sm->lens + nlen, ndist, DIST_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode,
+                                 sm->run, 1);
             if (rd != 0 && (rd < 0 || ndist != (int)sm->dcode.count[0] + 1)) {
                 status = INF_BAD_TABLE;
                 break;
@@ -861,34 +615,18 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
         }
 
         // ---- Huffman block: symbols, a window at a time ----------------------
+        if (lane == 0) r.seek(bitpos);
         while (true) {
-            if (pos - flushed >= FLUSH) {
-                flush_crc(sm, out, flushed, pos, crc_tab, &crc);
-                flushed = pos;
-            }
-            if (bitpos >= total) { // the stream ended before the end of block
-                status = INF_TRUNCATED;
-                break;
-            }
-            Window w = decode_window(sm, r, bitpos, total, out, flushed, &pos, cap);
-            if (w.status == 0xffffffffu) {
-                int eob = 0;
-                status = decode_serial_range(sm, r, &bitpos, total, out, &flushed, &pos, cap, 16, crc_tab, &crc, &eob);
-                if (status != INF_OK || eob) break;
-                continue;
-            }
-            if (w.status != INF_OK) {
-                status = w.status;
-                break;
-            }
-            bitpos = w.next;
-            if (w.eob) break;
+            int eob = 0;
+            status = decode_burst(sm, r, total, out, &pos, cap, crc_tab, &crc, &eob);
+            if (status != INF_OK || eob) break;
         }
+        if (status != INF_OK) break;
+        if (lane == 0) bitpos = r.tell();
+        bitpos = __shfl_sync(FRT_FULL_MASK, bitpos, 0);
         if (status != INF_OK) break;
         if (last) break;
     }
-    if (status == INF_OK) flush_crc(sm, out, flushed, pos, crc_tab, &crc);
-    // on error nothing more is written: the member's output is discarded
     *produced_out = pos;
     *crc_out = crc;
     return status;

@@ -3,19 +3,19 @@
 
 #include "common.cuh"
 
-// Warps per CTA of the inflate kernels; per warp, the shared-memory ring of
-// recent output, the flush interval, and the queue of deferred matches.
+// Warps per CTA of the inflate kernels; table roots; per warp, the window
+// output buffer and the window's match queue.
 #ifndef INF_WARPS_PER_CTA
-#define INF_WARPS_PER_CTA 4
+#define INF_WARPS_PER_CTA 3
 #endif
-#ifndef INF_RING
-#define INF_RING 8192
+#ifndef INF_LIT_BITS
+#define INF_LIT_BITS 10
 #endif
-#ifndef INF_FLUSH
-#define INF_FLUSH 2048
+#ifndef INF_DIST_BITS
+#define INF_DIST_BITS 8
 #endif
-#ifndef INF_SEG
-#define INF_SEG 128
+#ifndef INF_WINBUF
+#define INF_WINBUF 2048
 #endif
 #ifndef INF_MAXQ
 #define INF_MAXQ 384
