@@ -208,6 +208,8 @@ def lib():
         "frt_bam_decoder_destroy": (None, [_P]),
         "frt_bam_decode": (C.c_int, [_P, _P, C.c_uint64, _P, _P]),
         "frt_bam_decoder_last_fallbacks": (C.c_uint64, [_P]),
+        "frt_bam_scan_noalloc": (C.c_int, [_P, C.c_uint64, _P, C.c_uint32, C.c_uint64, C.c_int32, _P, C.c_uint64, _P,
+                                           _P, _P, _P]),
         "frt_record_batch_len": (C.c_uint64, [_P]),
         "frt_record_batch_tail": (C.c_uint64, [_P]),
         "frt_record_batch_aux_fields": (C.c_uint64, [_P]),
@@ -512,6 +514,24 @@ class BamDecoder:
         if h and _lib is not None:
             _lib.frt_bam_decoder_destroy(h)
             self._h = None
+
+
+NOALLOC_MAX_MEMBERS = 1024
+
+
+def bam_scan_noalloc(data_ptr: int, length: int, member_offsets_ptr: int, n_members: int, start: int,
+                     record_offsets_ptr: int, record_cap: int, n_ref: int = -1, stream: int | None = None):
+    """Record boundaries of device-resident inflated bytes without any
+    allocation by the library (frt_bam_scan_noalloc): the caller's device
+    arrays hold the member offsets (n_members + 1) and receive the record
+    offsets.  Returns (n_records, tail)."""
+    n = C.c_uint64()
+    tail = C.c_uint64()
+    err = _Err()
+    _raise(lib().frt_bam_scan_noalloc(data_ptr, length, member_offsets_ptr, n_members, start, n_ref,
+                                      record_offsets_ptr, record_cap, C.byref(n), C.byref(tail), stream,
+                                      C.byref(err)), err)
+    return n.value, tail.value
 
 
 class DeviceRecordBatch:
