@@ -1,0 +1,96 @@
+"""The C ABI without a GPU: the library loads, exports every function that
+include/frt.h declares, refuses to run without a GB300 (no CPU fallback), and
+its host-side parts -- BGZF member discovery (discover.rs:51-109) and the BAM
+header parse (header.rs:43-101) -- agree with the oracle, including the errors
+and their offsets."""
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+CASES = sorted(p.stem for p in GOLDEN.glob("*.npz"))
+
+
+@pytest.fixture(scope="module")
+def frt():
+    import fritillaria_gb300 as frt
+    from fritillaria_gb300 import build
+
+    if not build.LIB.exists():
+        build.build_cuda()
+    frt.lib()
+    return frt
+
+
+def test_library_exports_every_declared_function(frt):
+    names = frt.header_functions()
+    assert len(names) >= 50  # the parse found the declarations
+    raw = C.CDLL(str(frt.LIB_PATH))
+    missing = [n for n in names if not hasattr(raw, n)]
+    assert not missing, missing
+
+
+def test_every_declared_function_has_a_binding(frt):
+    L = frt.lib()
+    for n in frt.header_functions():
+        fn = getattr(L, n)
+        assert fn.argtypes is not None or n == "frt_reader_open", n
+
+
+def test_no_cpu_fallback_without_a_gpu(frt):
+    if frt.cuda_is_usable():
+        pytest.skip("a GPU is present")
+    for backend in (frt.Backend.AUTO, frt.Backend.CUDA, frt.Backend.NVCOMP):
+        with pytest.raises(frt.CudaUnavailable):
+            frt.select_codec(backend)
+    with pytest.raises(frt.InvalidArgument):
+        frt.select_codec(frt.Backend.CPU)
+    with pytest.raises(frt.CudaUnavailable):
+        frt.CudaCodec(0)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_host_discovery_matches_oracle(frt, case):
+    b = np.load(GOLDEN / f"{case}.npz")["bgzf"]
+    got, used = frt.discover_blocks(b)
+    want, wused = oracle.discover(b)
+    assert used == wused
+    for f in ("compressed_offset", "payload_start", "payload_len", "isize", "crc32"):
+        assert np.array_equal(got[f], want[f]), f
+    # a window that ends inside a member stops before it
+    cut = b[: int(want["compressed_offset"][-1]) + 5]
+    got, used = frt.discover_blocks(cut, base_offset=1000)
+    assert used == int(want["compressed_offset"][-1])
+    assert np.array_equal(got["compressed_offset"], want["compressed_offset"][:-1] + 1000)
+
+
+def test_host_discovery_errors_match_oracle(frt):
+    b = np.load(GOLDEN / "bam_short_full.npz")["bgzf"].copy()
+    spans, _ = oracle.discover(b)
+    at = int(spans["compressed_offset"][3])
+    for pos, val in ((at + 2, 7), (at + 3, 0), (at + 12, 9), (at + 16, 0xFF)):
+        bad = b.copy()
+        bad[pos] = val
+        with pytest.raises(oracle.OracleError) as want:
+            oracle.discover(bad)
+        with pytest.raises(frt.FrtError) as got:
+            frt.discover_blocks(bad)
+        assert got.value.code == want.value.code == 2
+        assert got.value.offset == want.value.offset == at
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c.startswith("bam_")])
+def test_host_header_parse_matches_oracle(frt, case):
+    g = np.load(GOLDEN / f"{case}.npz")
+    data, _ = oracle.inflate_batch(g["bgzf"], oracle.discover(g["bgzf"])[0])
+    assert frt.parse_header(data) == oracle.bam_header(data) == (int(g["records_start"]), int(g["n_ref"]))
+    # a window ending inside the header is Malformed until more bytes arrive
+    with pytest.raises(frt.Malformed):
+        frt.parse_header(data[: int(g["records_start"]) - 1])
+    with pytest.raises(frt.Malformed):
+        frt.parse_header(b"BAM\x02")
