@@ -230,6 +230,26 @@ def lib():
         "frt_engine_stream": (_P, [_P]),
         "frt_engine_time_stages": (C.c_int, [_P, _P, C.c_int, _P]),
         "frt_engine_launches": (C.c_uint64, [_P]),
+        "frt_fastq_scanner_create": (C.c_int, [C.c_int, _P, _P, _P]),
+        "frt_fastq_scanner_destroy": (None, [_P]),
+        "frt_fastq_decode": (C.c_int, [_P, _P, C.c_uint64, _P, _P]),
+        "frt_bcf_parse_header": (C.c_int, [_P, C.c_size_t, _P, _P, _P, _P]),
+        "frt_bcf_scanner_create": (C.c_int, [C.c_int, _P, _P, _P]),
+        "frt_bcf_scanner_destroy": (None, [_P]),
+        "frt_bcf_decode": (C.c_int, [_P, _P, C.c_uint64, C.c_uint32, C.c_uint32, _P, _P]),
+        "frt_fasta_compactor_create": (C.c_int, [C.c_int, _P, _P, _P]),
+        "frt_fasta_compactor_destroy": (None, [_P]),
+        "frt_fasta_compact": (C.c_int, [_P, _P, _P, _P]),
+        "frt_columns_len": (C.c_uint64, [_P]),
+        "frt_columns_tail": (C.c_uint64, [_P]),
+        "frt_columns_total_bases": (C.c_uint64, [_P]),
+        "frt_columns_count": (C.c_int, [_P]),
+        "frt_columns_device_ordinal": (C.c_int, [_P]),
+        "frt_columns_scan_info": (None, [_P, _P, _P, _P]),
+        "frt_columns_column": (C.c_int, [_P, C.c_int, _P, _P, _P]),
+        "frt_columns_column_to_host": (C.c_int, [_P, C.c_int, _P, C.c_size_t, _P]),
+        "frt_columns_ready_event": (_P, [_P]),
+        "frt_columns_free": (None, [_P]),
     }
     for name, (res, args) in sig.items():
         if hasattr(L, name):
@@ -581,6 +601,165 @@ class DeviceRecordBatch:
 
     def __del__(self):
         self.free()
+
+
+# ---------------------------------------------------------------------------
+# FASTQ, BCF, FASTA
+# ---------------------------------------------------------------------------
+
+FASTQ_COLUMNS = {"record_offsets": (0, np.uint64), "sequence_start": (1, np.uint32), "plus_start": (2, np.uint32),
+                 "quality_start": (3, np.uint32), "sequence_len": (4, np.uint32), "record_end": (5, np.uint32)}
+BCF_COLUMNS = {"chromosome_id": (0, np.int32), "position": (1, np.int32), "reference_span": (2, np.int32),
+               "quality": (3, np.uint32), "info_count": (4, np.uint16), "allele_count": (5, np.uint16),
+               "sample_count": (6, np.uint32), "format_count": (7, np.uint8), "record_offsets": (8, np.uint64),
+               "alleles_start": (9, np.uint32), "filters_start": (10, np.uint32), "info_start": (11, np.uint32),
+               "genotypes_start": (12, np.uint32), "record_end": (13, np.uint32)}
+FASTA_COLUMNS = {"sequence": (0, np.uint8), "sequence_offsets": (1, np.uint64), "sequence_lengths": (2, np.uint64),
+                 "record_offsets": (3, np.uint64)}
+
+
+class Proof(enum.IntEnum):
+    """How a scan's boundaries were established (speculative.rs, Proof)."""
+    TILED = 0
+    WALKED = 1
+
+
+class SpeculativeScan:
+    """SpeculativeScan: offsets, tail, survivors and the proof."""
+
+    def __init__(self, offsets, tail, survivors, validated, proof):
+        self.offsets = offsets
+        self.tail = tail
+        self.survivors = survivors
+        self.validated = validated
+        self.proof = Proof(proof)
+
+
+class ColumnBatch:
+    """Device columns of a FASTQ or BCF batch, or a compacted FASTA reference
+    (DeviceRecordBatch / DeviceReference); keeps its inflate batch alive."""
+
+    def __init__(self, handle, columns: dict):
+        self._h = handle
+        self._cols = columns
+
+    def __len__(self):
+        return lib().frt_columns_len(self._h)
+
+    def is_empty(self) -> bool:
+        return len(self) == 0
+
+    def tail(self) -> int:
+        return lib().frt_columns_tail(self._h)
+
+    def total_bases(self) -> int:
+        return lib().frt_columns_total_bases(self._h)
+
+    def device_ordinal(self) -> int:
+        return lib().frt_columns_device_ordinal(self._h)
+
+    def scan_info(self):
+        proof, surv, val = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        lib().frt_columns_scan_info(self._h, C.byref(proof), C.byref(surv), C.byref(val))
+        return proof.value, surv.value, val.value
+
+    def column_ptr(self, name: str):
+        cid = self._cols[name][0]
+        p, nb, w = _P(), C.c_size_t(), C.c_size_t()
+        lib().frt_columns_column(self._h, cid, C.byref(p), C.byref(nb), C.byref(w))
+        return p.value or 0, nb.value, w.value
+
+    def column(self, name: str) -> np.ndarray:
+        cid, dt = self._cols[name]
+        _, nb, _ = self.column_ptr(name)
+        out = np.empty(nb // np.dtype(dt).itemsize, dtype=dt)
+        err = _Err()
+        _raise(lib().frt_columns_column_to_host(self._h, cid, out.ctypes.data, out.nbytes, C.byref(err)), err)
+        return out
+
+    def to_host(self) -> dict:
+        return {name: self.column(name) for name in self._cols}
+
+    def free(self):
+        if self._h and _lib is not None:
+            _lib.frt_columns_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        self.free()
+
+
+class _Scanner:
+    _create = _destroy = None
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        h = _P()
+        err = _Err()
+        _raise(getattr(lib(), self._create)(device, stream, C.byref(h), C.byref(err)), err)
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            getattr(_lib, self._destroy)(h)
+            self._h = None
+
+
+class FastqScanner(_Scanner):
+    """FastqScanner (crates/fritillaria-cuda/src/fastq.rs:46-140)."""
+    _create, _destroy = "frt_fastq_scanner_create", "frt_fastq_scanner_destroy"
+
+    def decode(self, batch: DeviceInflateBatch | None, start: int) -> ColumnBatch:
+        out = _P()
+        err = _Err()
+        _raise(lib().frt_fastq_decode(self._h, batch.handle if batch is not None else None, int(start), C.byref(out),
+                                      C.byref(err)), err)
+        return ColumnBatch(out, FASTQ_COLUMNS)
+
+    def scan(self, batch: DeviceInflateBatch | None, start: int) -> SpeculativeScan:
+        cb = self.decode(batch, start)
+        proof, surv, val = cb.scan_info()
+        return SpeculativeScan(cb.column("record_offsets"), cb.tail(), surv, val, proof)
+
+
+def parse_bcf_header(data):
+    """BCF parse_header (header.rs:111-160): (records_start, samples, contigs).
+    Raises Malformed when the bytes do not hold the whole header."""
+    b = _u8(data)
+    rs, ns, nc = C.c_uint64(), C.c_uint32(), C.c_uint32()
+    err = _Err()
+    _raise(lib().frt_bcf_parse_header(b.ctypes.data, b.size, C.byref(rs), C.byref(ns), C.byref(nc), C.byref(err)),
+           err)
+    return rs.value, ns.value, nc.value
+
+
+class BcfScanner(_Scanner):
+    """BcfScanner (crates/fritillaria-cuda/src/bcf.rs:38-150)."""
+    _create, _destroy = "frt_bcf_scanner_create", "frt_bcf_scanner_destroy"
+
+    def decode(self, batch: DeviceInflateBatch | None, start: int, samples: int, contigs: int) -> ColumnBatch:
+        out = _P()
+        err = _Err()
+        _raise(lib().frt_bcf_decode(self._h, batch.handle if batch is not None else None, int(start), int(samples),
+                                    int(contigs), C.byref(out), C.byref(err)), err)
+        return ColumnBatch(out, BCF_COLUMNS)
+
+    def scan(self, batch: DeviceInflateBatch | None, start: int, samples: int, contigs: int) -> SpeculativeScan:
+        cb = self.decode(batch, start, samples, contigs)
+        proof, surv, val = cb.scan_info()
+        return SpeculativeScan(cb.column("record_offsets"), cb.tail(), surv, val, proof)
+
+
+class FastaCompactor(_Scanner):
+    """FastaCompactor (crates/fritillaria-cuda/src/fasta.rs:30-80)."""
+    _create, _destroy = "frt_fasta_compactor_create", "frt_fasta_compactor_destroy"
+
+    def compact(self, batch: DeviceInflateBatch | None) -> ColumnBatch:
+        out = _P()
+        err = _Err()
+        _raise(lib().frt_fasta_compact(self._h, batch.handle if batch is not None else None, C.byref(out),
+                                       C.byref(err)), err)
+        return ColumnBatch(out, FASTA_COLUMNS)
 
 
 class BatchEngine:

@@ -1,0 +1,1539 @@
+// FASTQ, BCF and FASTA on the same container: record boundaries and columns
+// of a device-resident inflated batch.
+//
+//   FASTQ  FastqScanner::scan/decode  (crates/fritillaria-cuda/src/fastq.rs:94-140, 486-560)
+//   BCF    BcfScanner::scan/decode    (crates/fritillaria-cuda/src/bcf.rs:94-150, 280-420)
+//   FASTA  FastaCompactor::compact    (crates/fritillaria-cuda/src/fasta.rs:60-80, 212-300)
+//
+// Results are the reference launchers' results; the way there is different.
+//
+// FASTQ.  A newline index of the batch is built in two streaming passes (count
+// per 16 KiB tile, scan, emit in order).  With every line start indexed, the
+// four-line test of a record start (fastq record.rs:79-130) is O(1) per line,
+// so every line start is validated in parallel and the valid ones compacted in
+// order.  The reference proves a tiling of those survivors on the host and
+// otherwise walks one record at a time on one thread; here both its tiling
+// and its walk are checked for every adjacent pair in parallel (the walk
+// differs from the tiling only by blank lines between records), and a serial
+// walk over the index runs only when a decoy breaks the chain.
+//
+// BCF.  The reference's device result always equals its length-prefix walk
+// from `start` (the tiling, when it holds, is that chain; when it does not,
+// the walk runs).  Here the sieve of every byte offset runs over tiles staged
+// in shared memory, survivors are validated inline and emitted in order, the
+// tiling and the whole-record probe at its end are checked in parallel, and
+// the serial walk runs only when they fail.
+//
+// FASTA.  Three streaming passes over the batch with a line-state machine
+// (before any record / definition line / sequence line) carried across tiles
+// by a scan of composed per-tile transfer functions; pass three writes the
+// bases of sequence lines, newlines dropped, through a shared-memory staging
+// buffer with coalesced stores, plus each contig's record and sequence offset.
+
+#include <cstring>
+
+#include "bam.cuh"
+#include "common.cuh"
+#include "runtime.h"
+
+using namespace frt;
+
+namespace {
+
+constexpr int TB = 256;          // threads per tile
+constexpr int CH = 64;           // bytes per thread
+constexpr u64 TILE = TB * CH;    // bytes per tile
+constexpr u32 SIEVE_TILE = 8192; // BCF positions per tile
+constexpr u32 SIEVE_LIST = 1024; // survivors a BCF tile can order in shared memory
+
+// ---- block helpers (256 threads) -------------------------------------------
+
+template <typename T> __device__ T block_excl_sum(T v, T *s_warp, T *total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    T x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T y = __shfl_up_sync(FRT_FULL_MASK, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        T w = lane < TB / 32 ? s_warp[lane] : (T)0;
+#pragma unroll
+        for (int o = 1; o < TB / 32; o <<= 1) {
+            T y = __shfl_up_sync(FRT_FULL_MASK, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < TB / 32) s_warp[lane] = w;
+    }
+    __syncthreads();
+    T excl = x - v + (wid ? s_warp[wid - 1] : (T)0);
+    if (total) *total = s_warp[TB / 32 - 1];
+    __syncthreads();
+    return excl;
+}
+
+// Loads bytes [p0, p0 + 64) into 16 little-endian words; bytes outside
+// [lo, hi) read as 0.  Vector loads when the whole chunk is in range and
+// 16-byte aligned.
+__device__ __forceinline__ void load64(const u8 *buf, u64 p0, u64 lo, u64 hi, bool aligned, u32 w[16])
+{
+    if (aligned && p0 >= lo && p0 + 64 <= hi) {
+        const uint4 *q = reinterpret_cast<const uint4 *>(buf + p0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            uint4 x = __ldg(q + k);
+            w[4 * k] = x.x;
+            w[4 * k + 1] = x.y;
+            w[4 * k + 2] = x.z;
+            w[4 * k + 3] = x.w;
+        }
+        return;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        u32 v = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            u64 i = p0 + 4 * k + b;
+            u32 c = (i >= lo && i < hi) ? (u32)buf[i] : 0u;
+            v |= c << (8 * b);
+        }
+        w[k] = v;
+    }
+}
+
+__device__ __forceinline__ u32 byte_of(const u32 w[16], int i) { return (w[i >> 2] >> (8 * (i & 3))) & 0xffu; }
+
+// =============================================================================
+// FASTQ
+// =============================================================================
+
+__global__ void __launch_bounds__(TB) k_fq_nl_count(const u8 *buf, u64 lo, u64 hi, u64 tbase, bool aligned,
+                                                    u32 *tile_count)
+{
+    __shared__ u32 s_warp[TB / 32];
+    u64 p0 = tbase + (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
+    u32 w[16];
+    load64(buf, p0, lo, hi, aligned, w);
+    u32 c = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) c += __popc(__vcmpeq4(w[k], 0x0a0a0a0au)) >> 3;
+    u32 tot;
+    block_excl_sum<u32>(c, s_warp, &tot);
+    if (threadIdx.x == 0) tile_count[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(TB) k_fq_nl_emit(const u8 *buf, u64 lo, u64 hi, u64 tbase, bool aligned,
+                                                   const u32 *tile_base, u64 *nl)
+{
+    __shared__ u32 s_warp[TB / 32];
+    u64 p0 = tbase + (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
+    u32 w[16];
+    load64(buf, p0, lo, hi, aligned, w);
+    u32 m[16], c = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        m[k] = __vcmpeq4(w[k], 0x0a0a0a0au);
+        c += __popc(m[k]) >> 3;
+    }
+    u32 at = tile_base[blockIdx.x] + block_excl_sum<u32>(c, s_warp, nullptr);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        u32 mk = m[k];
+        while (mk) {
+            int b = __ffs(mk) - 1;
+            nl[at++] = p0 + 4 * k + (b >> 3);
+            mk &= ~(0xffu << (b & ~7));
+        }
+    }
+}
+
+struct FqIndex {
+    const u8 *buf;
+    u64 start, len;
+    const u64 *nl;
+    u32 n_nl, n_lines;
+    __device__ __forceinline__ u64 ls(u32 k) const { return k == 0 ? start : nl[k - 1] + 1; }
+    // end of the record whose definition is line k (valid record assumed)
+    __device__ __forceinline__ u64 rec_end(u32 k) const { return k + 3 < n_nl ? nl[k + 3] + 1 : len; }
+    __device__ __forceinline__ bool blank(u32 k) const { return buf[ls(k)] == '\n'; }
+    // bounds_at (fastq record.rs:79-130) from the index
+    __device__ __forceinline__ bool valid(u32 k) const
+    {
+        u64 p = ls(k);
+        if (buf[p] != '@' || k + 2 >= n_nl) return false;
+        if (buf[nl[k + 1] + 1] != '+') return false;
+        u64 seq_len = nl[k + 1] - nl[k] - 1;
+        u64 qs = nl[k + 2] + 1, qe = k + 3 < n_nl ? nl[k + 3] : len;
+        return qe - qs == seq_len;
+    }
+};
+
+__global__ void k_fq_lines(FqIndex ix, u32 *flags)
+{
+    u32 k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ix.n_lines) return;
+    flags[k] = ix.valid(k) ? 1u : 0u;
+}
+
+__global__ void k_fq_compact(const u32 *flags, const u32 *pos, u32 n_lines, u32 *S)
+{
+    u32 k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n_lines && flags[k]) S[pos[k]] = k;
+}
+
+// bit 0: the survivors do not tile (fastq.rs:585-598); bit 1: they are not the
+// walk's chain either (a gap between records holds something besides newlines).
+__global__ void k_fq_check(FqIndex ix, const u32 *S, u32 n_s, u32 *fails)
+{
+    u32 j = blockIdx.x * blockDim.x + threadIdx.x;
+    u32 f = 0;
+    if (j + 1 < n_s) {
+        u32 k0 = S[j], k1 = S[j + 1];
+        u64 e0 = ix.rec_end(k0), p1 = ix.ls(k1);
+        if (p1 != e0) f |= 1u;
+        if (k1 < k0 + 4 || e0 > p1 || p1 - e0 != (u64)(k1 - k0 - 4)) f |= 2u;
+    }
+    u32 any = __reduce_or_sync(FRT_FULL_MASK, f);
+    if ((threadIdx.x & 31) == 0 && any) atomicOr(fails, any);
+}
+
+// totals: n, tail, proof, survivors, use_walk_list
+__global__ void k_fq_finalize(FqIndex ix, const u32 *flags, const u32 *S, const u32 *n_s_dev, const u32 *fails,
+                              u32 *W, u64 *totals)
+{
+    u32 n_s = *n_s_dev;
+    u32 a = 0;
+    while (a < ix.n_lines && ix.blank(a)) ++a;
+    u64 anchor = a < ix.n_lines ? ix.ls(a) : ix.len;
+    u64 n = 0, tail = anchor, proof = 1, use_w = 0;
+    if (n_s > 0 && ix.ls(S[0]) == anchor) {
+        u64 e = ix.rec_end(S[n_s - 1]);
+        if (!(*fails & 1u)) {
+            n = n_s;
+            tail = e;
+            proof = 0;
+        } else if (!(*fails & 2u)) {
+            n = n_s;
+            if (e >= ix.len) {
+                tail = ix.len;
+            } else {
+                u32 c = S[n_s - 1] + 4;
+                while (c < ix.n_lines && ix.blank(c)) ++c;
+                tail = c < ix.n_lines ? ix.ls(c) : ix.len;
+            }
+        } else {
+            // a decoy among the survivors: the walk of fastq_scan.cu:173-215
+            u32 c = a, m = 0;
+            tail = ix.len;
+            while (c < ix.n_lines) {
+                if (!flags[c]) {
+                    tail = ix.ls(c);
+                    break;
+                }
+                W[m++] = c;
+                if (c + 3 >= ix.n_nl) { // unterminated last record ends the batch
+                    tail = ix.len;
+                    c = ix.n_lines;
+                    break;
+                }
+                c += 4;
+                while (c < ix.n_lines && ix.blank(c)) ++c;
+            }
+            n = m;
+            use_w = 1;
+        }
+    }
+    totals[0] = n;
+    totals[1] = tail;
+    totals[2] = proof;
+    totals[3] = n_s;
+    totals[4] = use_w;
+}
+
+__global__ void k_fq_decode(FqIndex ix, const u32 *list, u32 n, u64 *rec_off, u32 *seq_start, u32 *plus_start,
+                            u32 *qual_start, u32 *seq_len, u32 *rec_end)
+{
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    u32 k = list[i];
+    u64 p = ix.ls(k);
+    u64 qe = k + 3 < ix.n_nl ? ix.nl[k + 3] : ix.len;
+    u64 e = qe < ix.len ? qe + 1 : qe;
+    rec_off[i] = p;
+    seq_start[i] = (u32)(ix.nl[k] + 1 - p);
+    plus_start[i] = (u32)(ix.nl[k + 1] + 1 - p);
+    qual_start[i] = (u32)(ix.nl[k + 2] + 1 - p);
+    seq_len[i] = (u32)(ix.nl[k + 1] - ix.nl[k] - 1);
+    rec_end[i] = (u32)(e - p);
+}
+
+// =============================================================================
+// BCF (typed values: crates/fritillaria-bcf/src/columnar/typed.rs:381-447)
+// =============================================================================
+
+__device__ __forceinline__ u32 bcf_type_size(u32 code)
+{
+    // 0 missing, 1 int8, 2 int16, 3 int32, 5 float, 7 char; others reserved
+    switch (code) {
+    case 0: return 0;
+    case 1: case 7: return 1;
+    case 2: return 2;
+    case 3: case 5: return 4;
+    default: return 0xffffffffu;
+    }
+}
+
+// Descriptor at pos: header length (0 if malformed); count and kind out.
+__device__ u32 bcf_descriptor(const u8 *buf, u64 lim, u64 pos, u32 *count, u32 *kind)
+{
+    if (pos >= lim) return 0;
+    u32 d = buf[pos], code = d & 15u;
+    if (bcf_type_size(code) == 0xffffffffu) return 0;
+    *kind = code;
+    if ((d >> 4) < 15u) {
+        *count = d >> 4;
+        return 1;
+    }
+    if (pos + 1 >= lim) return 0;
+    u32 inner = buf[pos + 1], ic = inner & 15u;
+    if ((inner >> 4) != 1u || (ic != 1u && ic != 2u && ic != 3u)) return 0;
+    u32 wdt = bcf_type_size(ic);
+    if (pos + 2 + wdt > lim) return 0;
+    const u8 *p = buf + pos + 2;
+    int v = ic == 1u ? (int)(signed char)p[0] : ic == 2u ? (int)(short)ld_u16le(p) : (int)ld_u32le(p);
+    if (v < 15) return 0;
+    *count = (u32)v;
+    return 2 + wdt;
+}
+
+__device__ __forceinline__ u64 bcf_skip(const u8 *buf, u64 lim, u64 pos)
+{
+    u32 count = 0, kind = 0;
+    u32 h = bcf_descriptor(buf, lim, pos, &count, &kind);
+    if (!h) return 0;
+    u64 e = pos + h + (u64)count * bcf_type_size(kind);
+    return e > lim ? 0 : e;
+}
+
+// Record::validate (crates/fritillaria-bcf/src/columnar/record.rs:427-489).
+__device__ bool bcf_validate(const u8 *buf, u64 len, u64 pos)
+{
+    if (pos + 32 > len) return false;
+    u64 l_shared = ld_u32le(buf + pos), l_indiv = ld_u32le(buf + pos + 4);
+    u64 indiv = pos + 8 + l_shared, end = indiv + l_indiv;
+    if (l_shared < 24 || end > len) return false;
+    u32 n_info = ld_u16le(buf + pos + 24), n_allele = ld_u16le(buf + pos + 26);
+    u32 n_sample = ld_u16le(buf + pos + 28) | ((u32)buf[pos + 30] << 16), n_fmt = buf[pos + 31];
+    u64 at = bcf_skip(buf, indiv, pos + 32);
+    if (!at) return false;
+    for (u32 i = 0; i < n_allele; ++i)
+        if (!(at = bcf_skip(buf, indiv, at))) return false;
+    if (!(at = bcf_skip(buf, indiv, at))) return false;
+    for (u32 i = 0; i < n_info; ++i) {
+        if (!(at = bcf_skip(buf, indiv, at))) return false;
+        if (!(at = bcf_skip(buf, indiv, at))) return false;
+    }
+    if (at != indiv) return false;
+    for (u32 i = 0; i < n_fmt; ++i) {
+        if (!(at = bcf_skip(buf, end, at))) return false;
+        u32 count = 0, kind = 0;
+        u32 h = bcf_descriptor(buf, end, at, &count, &kind);
+        if (!h) return false;
+        at += h + (u64)count * bcf_type_size(kind) * n_sample;
+        if (at > end) return false;
+    }
+    return at == end;
+}
+
+// looks_like_a_record (record.rs:149-206) over a staged copy: `s` holds the
+// bytes from position `base`; `pos` is absolute.
+__device__ __forceinline__ bool bcf_plausible(const u8 *s, u64 off, u64 pos, u64 len, u32 samples, u32 contigs)
+{
+    if (pos + 32 > len) return false;
+    const u8 *p = s + off;
+    u32 n_sample = (u32)p[28] | ((u32)p[29] << 8) | ((u32)p[30] << 16);
+    if (n_sample != samples) return false;
+    u32 l_shared = (u32)p[0] | ((u32)p[1] << 8) | ((u32)p[2] << 16) | ((u32)p[3] << 24);
+    u32 l_indiv = (u32)p[4] | ((u32)p[5] << 8) | ((u32)p[6] << 16) | ((u32)p[7] << 24);
+    if (l_shared < 24) return false;
+    if (pos + 8 + (u64)l_shared + l_indiv > len) return false;
+    int chrom = (int)((u32)p[8] | ((u32)p[9] << 8) | ((u32)p[10] << 16) | ((u32)p[11] << 24));
+    int position = (int)((u32)p[12] | ((u32)p[13] << 8) | ((u32)p[14] << 16) | ((u32)p[15] << 24));
+    int rlen = (int)((u32)p[16] | ((u32)p[17] << 8) | ((u32)p[18] << 16) | ((u32)p[19] << 24));
+    if (chrom < 0 || (u32)chrom >= contigs || position < -1 || rlen < 0) return false;
+    u32 n_allele = (u32)p[26] | ((u32)p[27] << 8), n_fmt = p[31];
+    if (n_allele == 0) return false;
+    if (n_fmt == 0) return l_indiv == 0;
+    return (u64)l_indiv >= (u64)n_fmt * 2;
+}
+
+// mode 0: survivors per tile.  mode 1: survivors emitted in position order at
+// tile_base[tile] (a tile with more than SIEVE_LIST survivors sets *overflow
+// and emits nothing; the caller then takes the walk).
+__global__ void __launch_bounds__(TB) k_bcf_sieve(const u8 *buf, u64 start, u64 len, u32 samples, u32 contigs,
+                                                  int mode, u32 *tile_count, const u32 *tile_base, u64 *out,
+                                                  u32 *overflow)
+{
+    __shared__ __align__(16) u8 s[SIEVE_TILE + 48];
+    __shared__ u64 s_list[SIEVE_LIST];
+    __shared__ u32 s_n, s_warp[TB / 32];
+    const u64 base = start + (u64)blockIdx.x * SIEVE_TILE;
+    for (u32 i = threadIdx.x; i < SIEVE_TILE + 32; i += TB) {
+        u64 p = base + i;
+        s[i] = p < len ? buf[p] : 0;
+    }
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    u32 c = 0;
+    for (u32 i = threadIdx.x; i < SIEVE_TILE; i += TB) {
+        u64 pos = base + i;
+        if (pos >= len) break;
+        if (!bcf_plausible(s, i, pos, len, samples, contigs)) continue;
+        if (!bcf_validate(buf, len, pos)) continue;
+        if (mode == 0) {
+            ++c;
+        } else {
+            u32 slot = atomicAdd(&s_n, 1u);
+            if (slot < SIEVE_LIST) s_list[slot] = pos;
+        }
+    }
+    if (mode == 0) {
+        u32 tot;
+        block_excl_sum<u32>(c, s_warp, &tot);
+        if (threadIdx.x == 0) tile_count[blockIdx.x] = tot;
+        return;
+    }
+    __syncthreads();
+    u32 n = s_n;
+    if (n > SIEVE_LIST) {
+        // the tile cannot order its survivors: mark its slots out of range
+        // so nothing reads through them, and send the batch to the walk
+        if (threadIdx.x == 0) atomicOr(overflow, 1u);
+        for (u32 i = tile_base[blockIdx.x] + threadIdx.x; i < tile_base[blockIdx.x + 1]; i += TB) out[i] = len;
+        return;
+    }
+    // rank sort: survivors per tile are few (one per record at most)
+    u32 at = tile_base[blockIdx.x];
+    for (u32 i = threadIdx.x; i < n; i += TB) {
+        u64 v = s_list[i];
+        u32 r = 0;
+        for (u32 j = 0; j < n; ++j) r += s_list[j] < v;
+        out[at + r] = v;
+    }
+}
+
+__device__ __forceinline__ u64 bcf_end(const u8 *buf, u64 pos)
+{
+    return pos + 8 + (u64)ld_u32le(buf + pos) + (u64)ld_u32le(buf + pos + 4);
+}
+
+__global__ void k_bcf_check(const u8 *buf, u64 start, u64 len, const u64 *V, u32 nv, u32 *fails)
+{
+    u32 j = blockIdx.x * blockDim.x + threadIdx.x;
+    u32 f = 0;
+    if (j < nv) {
+        u64 p = V[j];
+        if (p + 32 > len) f = 1; // an overflowed tile's sentinel
+        else {
+            if (j == 0 && p != start) f = 1;
+            if (j + 1 < nv && V[j + 1] != bcf_end(buf, p)) f = 1;
+        }
+    }
+    u32 any = __reduce_or_sync(FRT_FULL_MASK, f);
+    if ((threadIdx.x & 31) == 0 && any) atomicOr(fails, 1u);
+}
+
+// totals: n, tail, proof, sieved(validated), need_walk
+__global__ void k_bcf_finalize(const u8 *buf, u64 start, u64 len, const u64 *V, const u32 *nv_dev, const u32 *fails,
+                               const u32 *overflow, u64 *totals)
+{
+    u32 nv = *nv_dev;
+    bool tiled = !*fails && !*overflow;
+    u64 at = start;
+    if (tiled && nv) at = bcf_end(buf, V[nv - 1]); // every survivor passed the range checks
+    if (tiled && at + 8 <= len && bcf_end(buf, at) <= len) tiled = false; // a whole record the sieve missed
+    totals[0] = tiled ? nv : 0;
+    totals[1] = at;
+    totals[2] = tiled ? 0 : 1;
+    totals[3] = nv;
+    totals[4] = tiled ? 0 : 1;
+}
+
+// The length-prefix walk of bcf_scan.cu:374-410; `out` null counts only.
+__global__ void k_bcf_walk(const u8 *buf, u64 start, u64 len, u64 *out, u64 *totals)
+{
+    u64 pos = start, n = 0;
+    for (;;) {
+        if (pos + 8 > len) break;
+        u64 ls = ld_u32le(buf + pos), li = ld_u32le(buf + pos + 4);
+        if (ls < 24) break;
+        u64 end = pos + 8 + ls + li;
+        if (end > len) break;
+        if (out) out[n] = pos;
+        ++n;
+        pos = end;
+    }
+    totals[0] = n;
+    totals[1] = pos;
+}
+
+struct BcfCols {
+    int *chrom, *pos, *rlen;
+    u32 *qual;
+    u16 *n_info, *n_allele;
+    u32 *n_sample;
+    u8 *n_fmt;
+    u64 *rec_off;
+    u32 *alleles, *filters, *info, *genotypes, *end;
+};
+
+// bcf_decode (bcf_scan.cu:432-510): the site core and the field offsets.
+__global__ void k_bcf_decode(const u8 *buf, u64 len, const u64 *offsets, u32 n, BcfCols c, u32 *errors)
+{
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    u64 pos = offsets[i];
+    c.rec_off[i] = pos;
+    if (pos + 32 > len) {
+        atomicAdd(errors, 1u);
+        return;
+    }
+    u64 ls = ld_u32le(buf + pos), li = ld_u32le(buf + pos + 4);
+    u64 end = pos + 8 + ls + li;
+    if (ls < 24 || end > len) {
+        atomicAdd(errors, 1u);
+        return;
+    }
+    u32 n_allele = ld_u16le(buf + pos + 26);
+    c.chrom[i] = (int)ld_u32le(buf + pos + 8);
+    c.pos[i] = (int)ld_u32le(buf + pos + 12);
+    c.rlen[i] = (int)ld_u32le(buf + pos + 16);
+    c.qual[i] = ld_u32le(buf + pos + 20);
+    c.n_info[i] = (u16)ld_u16le(buf + pos + 24);
+    c.n_allele[i] = (u16)n_allele;
+    c.n_sample[i] = ld_u16le(buf + pos + 28) | ((u32)buf[pos + 30] << 16);
+    c.n_fmt[i] = buf[pos + 31];
+    c.genotypes[i] = (u32)(8 + ls);
+    c.end[i] = (u32)(end - pos);
+    u64 w = bcf_skip(buf, end, pos + 32);
+    if (!w) {
+        atomicAdd(errors, 1u);
+        return;
+    }
+    c.alleles[i] = (u32)(w - pos);
+    for (u32 a = 0; a < n_allele; ++a) {
+        w = bcf_skip(buf, end, w);
+        if (!w) {
+            atomicAdd(errors, 1u);
+            return;
+        }
+    }
+    c.filters[i] = (u32)(w - pos);
+    w = bcf_skip(buf, end, w);
+    if (!w) {
+        atomicAdd(errors, 1u);
+        return;
+    }
+    c.info[i] = (u32)(w - pos);
+}
+
+// =============================================================================
+// FASTA
+// =============================================================================
+//
+// Line states: 0 before any record, 1 definition line, 2 sequence line.  A
+// line start beginning with '>' enters 1; any other line start enters 2
+// unless no record has begun.  Over a span of bytes the effect on the state is
+// one of four functions: identity (no line start), OTHER (only non-'>' line
+// starts: 0 stays 0, else 2), or a constant 1 or 2 (the last '>' line start
+// and what follows it decide).
+
+enum : u32 { F_ID = 0, F_OTHER = 1, F_HDR = 2, F_SEQ = 3 };
+
+__device__ __forceinline__ u32 f_apply(u32 f, u32 s)
+{
+    return f == F_ID ? s : f == F_OTHER ? (s == 0 ? 0u : 2u) : f == F_HDR ? 1u : 2u;
+}
+// the function "f, then g"
+__device__ __forceinline__ u32 f_then(u32 f, u32 g)
+{
+    if (g == F_HDR || g == F_SEQ) return g;
+    if (g == F_ID) return f;
+    return f == F_HDR || f == F_SEQ ? F_SEQ : F_OTHER;
+}
+__device__ __forceinline__ u32 f_step(u32 f, bool gt) { return gt ? F_HDR : f_then(f, F_OTHER); }
+
+// Exclusive scan of transfer functions across the block (composition).
+__device__ u32 block_excl_compose(u32 f, u32 *s_warp)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    u32 x = f;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        u32 y = __shfl_up_sync(FRT_FULL_MASK, x, o);
+        if (lane >= o) x = f_then(y, x);
+    }
+    u32 ex = __shfl_up_sync(FRT_FULL_MASK, x, 1);
+    if (lane == 0) ex = F_ID;
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        u32 wv = lane < TB / 32 ? s_warp[lane] : F_ID;
+#pragma unroll
+        for (int o = 1; o < TB / 32; o <<= 1) {
+            u32 y = __shfl_up_sync(FRT_FULL_MASK, wv, o);
+            if (lane >= o) wv = f_then(y, wv);
+        }
+        if (lane < TB / 32) s_warp[lane] = wv;
+    }
+    __syncthreads();
+    u32 pre = wid ? s_warp[wid - 1] : F_ID;
+    u32 r = f_then(pre, ex);
+    __syncthreads();
+    return r;
+}
+
+struct FaChunk {
+    u32 w[16];
+    u32 prev; // the byte before the chunk (or '\n' at the buffer start)
+    u32 n;    // valid bytes in the chunk
+};
+
+__device__ __forceinline__ void fa_load(const u8 *buf, u64 len, bool aligned, u64 p0, FaChunk &c)
+{
+    load64(buf, p0, 0, len, aligned, c.w);
+    c.prev = p0 == 0 ? (u32)'\n' : (p0 - 1 < len ? (u32)buf[p0 - 1] : 0u);
+    c.n = p0 >= len ? 0u : (u32)min((u64)CH, len - p0);
+}
+
+// The chunk's transfer function and its count of record starts.
+__device__ __forceinline__ void fa_summary(const FaChunk &c, u32 *f_out, u32 *contigs)
+{
+    u32 f = F_ID, k = 0, prev = c.prev;
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+        if ((u32)i < c.n) {
+            u32 b = byte_of(c.w, i);
+            if (prev == '\n') {
+                f = f_step(f, b == '>');
+                k += b == '>';
+            }
+            prev = b;
+        }
+    }
+    *f_out = f;
+    *contigs = k;
+}
+
+// Bases the chunk keeps, entering in state s.
+__device__ __forceinline__ u32 fa_kept(const FaChunk &c, u32 s)
+{
+    u32 kept = 0, prev = c.prev;
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+        if ((u32)i < c.n) {
+            u32 b = byte_of(c.w, i);
+            if (prev == '\n') s = b == '>' ? 1u : (s == 0 ? 0u : 2u);
+            kept += (s == 2u && b != '\n');
+            prev = b;
+        }
+    }
+    return kept;
+}
+
+__global__ void __launch_bounds__(TB) k_fa_pass1(const u8 *buf, u64 len, bool aligned, u8 *tile_f, u32 *tile_contigs,
+                                                 unsigned long long *last_contig)
+{
+    __shared__ u32 s_warp[TB / 32];
+    FaChunk c;
+    u64 p0 = (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
+    fa_load(buf, len, aligned, p0, c);
+    u32 f, k;
+    fa_summary(c, &f, &k);
+    if (k) {
+        // position of the chunk's last record start, for the final-header check
+        u32 prev = c.prev;
+        u64 last = 0;
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+            if ((u32)i < c.n) {
+                u32 b = byte_of(c.w, i);
+                if (prev == '\n' && b == '>') last = p0 + i;
+                prev = b;
+            }
+        }
+        atomicMax(last_contig, (unsigned long long)last + 1);
+    }
+    u32 tot;
+    block_excl_sum<u32>(k, s_warp, &tot);
+    u32 ex = block_excl_compose(f, s_warp);
+    if (threadIdx.x == TB - 1) {
+        tile_f[blockIdx.x] = (u8)f_then(ex, f);
+        tile_contigs[blockIdx.x] = tot;
+    }
+}
+
+// One block: per tile its entry state and first contig index; the contig
+// count, and whether the last record's definition line is unterminated (such a
+// record is not a record, fasta record.rs:101-110).
+__global__ void __launch_bounds__(1024) k_fa_tiles(const u8 *buf, u64 len, const u8 *tile_f, const u32 *tile_contigs,
+                                                   u32 n_tiles, u8 *tile_state, u32 *contig_base,
+                                                   const unsigned long long *last_contig, u64 *totals)
+{
+    __shared__ u32 s_a[32], s_b[32];
+    u32 carry_f = F_ID, carry_c = 0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (u32 b0 = 0; b0 < n_tiles; b0 += 1024) {
+        u32 t = b0 + threadIdx.x;
+        u32 f = t < n_tiles ? tile_f[t] : F_ID, c = t < n_tiles ? tile_contigs[t] : 0u;
+        u32 xf = f, xc = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            u32 yf = __shfl_up_sync(FRT_FULL_MASK, xf, o), yc = __shfl_up_sync(FRT_FULL_MASK, xc, o);
+            if (lane >= o) {
+                xf = f_then(yf, xf);
+                xc += yc;
+            }
+        }
+        if (lane == 31) {
+            s_a[wid] = xf;
+            s_b[wid] = xc;
+        }
+        __syncthreads();
+        if (wid == 0) {
+            u32 wf = s_a[lane], wc = s_b[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                u32 yf = __shfl_up_sync(FRT_FULL_MASK, wf, o), yc = __shfl_up_sync(FRT_FULL_MASK, wc, o);
+                if (lane >= o) {
+                    wf = f_then(yf, wf);
+                    wc += yc;
+                }
+            }
+            s_a[lane] = wf;
+            s_b[lane] = wc;
+        }
+        __syncthreads();
+        // exclusive prefix for this thread within the chunk of 1024
+        u32 ef = __shfl_up_sync(FRT_FULL_MASK, xf, 1), ec = __shfl_up_sync(FRT_FULL_MASK, xc, 1);
+        if (lane == 0) {
+            ef = F_ID;
+            ec = 0;
+        }
+        u32 pf = wid ? s_a[wid - 1] : F_ID, pc = wid ? s_b[wid - 1] : 0u;
+        u32 before = f_then(carry_f, f_then(pf, ef));
+        if (t < n_tiles) {
+            tile_state[t] = (u8)f_apply(before, 0u);
+            contig_base[t] = carry_c + pc + ec;
+        }
+        u32 all_f = s_a[31], all_c = s_b[31];
+        __syncthreads();
+        carry_f = f_then(carry_f, all_f);
+        carry_c += all_c;
+    }
+    if (threadIdx.x == 0) {
+        u64 n = carry_c;
+        u64 drop = 0;
+        if (n && *last_contig) {
+            u64 p = *last_contig - 1;
+            while (p < len && buf[p] != '\n') ++p;
+            drop = p >= len;
+        }
+        totals[0] = n - drop; // contigs
+        totals[2] = drop;
+    }
+}
+
+__global__ void __launch_bounds__(TB) k_fa_pass2(const u8 *buf, u64 len, bool aligned, const u8 *tile_state,
+                                                 u32 *tile_kept)
+{
+    __shared__ u32 s_warp[TB / 32];
+    FaChunk c;
+    u64 p0 = (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
+    fa_load(buf, len, aligned, p0, c);
+    u32 f, k;
+    fa_summary(c, &f, &k);
+    u32 ex = block_excl_compose(f, s_warp);
+    u32 s = f_apply(ex, tile_state[blockIdx.x]);
+    u32 kept = fa_kept(c, s), tot;
+    block_excl_sum<u32>(kept, s_warp, &tot);
+    if (threadIdx.x == 0) tile_kept[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(TB) k_fa_pass3(const u8 *buf, u64 len, bool aligned, const u8 *tile_state,
+                                                 const u32 *contig_base, const u64 *out_base, u64 n_contigs, u8 *seq,
+                                                 u64 *seq_off, u64 *rec_off)
+{
+    __shared__ u32 s_warp[TB / 32];
+    __shared__ __align__(16) u8 s_out[TILE];
+    FaChunk c;
+    u64 p0 = (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
+    fa_load(buf, len, aligned, p0, c);
+    u32 f, k;
+    fa_summary(c, &f, &k);
+    u32 ex = block_excl_compose(f, s_warp);
+    u32 s = f_apply(ex, tile_state[blockIdx.x]);
+    u32 kept = fa_kept(c, s), tile_total;
+    u32 at = block_excl_sum<u32>(kept, s_warp, &tile_total);
+    u32 ci = contig_base[blockIdx.x] + block_excl_sum<u32>(k, s_warp, nullptr);
+    const u64 obase = out_base[blockIdx.x];
+    u32 prev = c.prev, o = at;
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+        if ((u32)i < c.n) {
+            u32 b = byte_of(c.w, i);
+            if (prev == '\n') {
+                if (b == '>') {
+                    if (ci < n_contigs) {
+                        rec_off[ci] = p0 + i;
+                        seq_off[ci] = obase + o;
+                    }
+                    ++ci;
+                    s = 1u;
+                } else if (s != 0u) {
+                    s = 2u;
+                }
+            }
+            if (s == 2u && b != '\n') s_out[o++] = (u8)b;
+            prev = b;
+        }
+    }
+    __syncthreads();
+    for (u32 i = threadIdx.x; i < tile_total; i += TB) seq[obase + i] = s_out[i];
+}
+
+__global__ void k_fa_lengths(const u64 *seq_off, u64 n, u64 total, u64 *seq_len)
+{
+    u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) seq_len[i] = (i + 1 < n ? seq_off[i + 1] : total) - seq_off[i];
+}
+
+// Exclusive u64 scan of u32 tile values, one block (tiles number in the
+// hundreds of thousands at most).
+__global__ void __launch_bounds__(1024) k_scan_tiles64(const u32 *in, u32 n, u64 *out, u64 *total)
+{
+    __shared__ u64 s_w[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    u64 carry = 0;
+    for (u32 b0 = 0; b0 < n; b0 += 1024) {
+        u32 t = b0 + threadIdx.x;
+        u64 v = t < n ? in[t] : 0, x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            u64 y = __shfl_up_sync(FRT_FULL_MASK, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_w[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            u64 w = s_w[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                u64 y = __shfl_up_sync(FRT_FULL_MASK, w, o);
+                if (lane >= o) w += y;
+            }
+            s_w[lane] = w;
+        }
+        __syncthreads();
+        if (t < n) out[t] = carry + x - v + (wid ? s_w[wid - 1] : 0);
+        u64 all = s_w[31];
+        __syncthreads();
+        carry += all;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+unsigned grid_for(u64 n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+} // namespace
+
+// =============================================================================
+// host side
+// =============================================================================
+
+namespace {
+
+enum { FMT_FASTQ = 1, FMT_BCF = 2, FMT_FASTA = 3 };
+
+const size_t kFastqWidths[FRT_FASTQ_COL_COUNT] = {8, 4, 4, 4, 4, 4};
+const size_t kBcfWidths[FRT_BCF_COL_COUNT] = {4, 4, 4, 4, 2, 2, 4, 1, 8, 4, 4, 4, 4, 4};
+const size_t kFastaWidths[FRT_FASTA_COL_COUNT] = {1, 8, 8, 8};
+
+struct Scanner {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    SharedStream *shared = nullptr;
+    std::mutex mu;
+};
+
+int scanner_create(int device, void *stream, Scanner *s, frt_error *err)
+{
+    int rc = check_device(device, err);
+    if (rc) return rc;
+    DeviceGuardLite g(device);
+    configure_pool(device);
+    SharedStream *ss = stream_create(device, stream, err);
+    if (!ss) return FRT_ERR_CUDA;
+    s->device = device;
+    s->shared = ss;
+    s->stream = ss->s;
+    return FRT_OK;
+}
+
+} // namespace
+
+struct frt_fastq_scanner {
+    Scanner s;
+};
+struct frt_bcf_scanner {
+    Scanner s;
+};
+struct frt_fasta_compactor {
+    Scanner s;
+};
+
+struct frt_columns {
+    int device = 0;
+    int format = 0;
+    cudaStream_t stream = nullptr;
+    SharedStream *shared = nullptr;
+    uint64_t n = 0, tail = 0, total = 0;
+    uint64_t info[3] = {0, 0, 0}; // proof, survivors, validated
+    int n_cols = 0;
+    const size_t *widths = nullptr;
+    uint8_t *cols = nullptr;
+    uint8_t *seq = nullptr; // FASTA bases
+    size_t col_off[16] = {}, col_bytes[16] = {};
+    const frt_inflate_batch *source = nullptr;
+    cudaEvent_t ready = nullptr;
+};
+
+namespace {
+
+// Work buffers of one call, freed on every return path.
+struct Work {
+    cudaStream_t st;
+    std::vector<void *> ptrs;
+    explicit Work(cudaStream_t s) : st(s) {}
+    ~Work()
+    {
+        for (void *p : ptrs) dev_free(p, st);
+    }
+    template <typename T> int get(T **p, size_t count, frt_error *err)
+    {
+        void *q = nullptr;
+        int rc = dev_alloc(&q, count * sizeof(T) + 16, st, err);
+        if (rc) return rc;
+        ptrs.push_back(q);
+        *p = (T *)q;
+        return FRT_OK;
+    }
+};
+
+frt_columns *columns_new(const Scanner &s, int format, const size_t *widths, int n_cols, uint64_t n)
+{
+    frt_columns *c = new frt_columns;
+    c->device = s.device;
+    c->format = format;
+    c->stream = s.stream;
+    c->shared = stream_retain(s.shared);
+    c->widths = widths;
+    c->n_cols = n_cols;
+    c->n = n;
+    size_t off = 0;
+    for (int k = 0; k < n_cols; ++k) {
+        c->col_off[k] = off;
+        c->col_bytes[k] = widths[k] * n;
+        off += (c->col_bytes[k] + 255) & ~(size_t)255;
+    }
+    return c;
+}
+
+size_t columns_bytes(const frt_columns *c)
+{
+    size_t t = 0;
+    for (int k = 0; k < c->n_cols; ++k) t += (c->col_bytes[k] + 255) & ~(size_t)255;
+    return t;
+}
+
+void columns_discard(frt_columns *c)
+{
+    if (!c) return;
+    dev_free(c->cols, c->stream);
+    dev_free(c->seq, c->stream);
+    stream_release(c->shared);
+    delete c;
+}
+
+int columns_finish(frt_columns *c, const frt_inflate_batch *src, frt_columns **out)
+{
+    if (src) {
+        const_cast<frt_inflate_batch *>(src)->refs.fetch_add(1);
+        c->source = src;
+    }
+    cudaEventCreateWithFlags(&c->ready, cudaEventDisableTiming);
+    cudaEventRecord(c->ready, c->stream);
+    *out = c;
+    return FRT_OK;
+}
+
+int columns_alloc(frt_columns *c, frt_error *err)
+{
+    return dev_alloc((void **)&c->cols, columns_bytes(c) + 256, c->stream, err);
+}
+
+template <typename T> T *colp(frt_columns *c, int k) { return (T *)(c->cols + c->col_off[k]); }
+
+int check_batch(const Scanner &s, const frt_inflate_batch *b, frt_error *err)
+{
+    if (b->device != s.device) {
+        set_error(err, FRT_ERR_INVALID_DEVICE_BATCH, 0, 0, 0, 0, nullptr, "batch is on device %d but this scanner is on %d",
+                  b->device, s.device);
+        return FRT_ERR_INVALID_DEVICE_BATCH;
+    }
+    cudaError_t e = cudaStreamWaitEvent(s.stream, b->ready, 0);
+    if (e != cudaSuccess) return cuda_fail(err, e, "ordering after the inflate");
+    return FRT_OK;
+}
+
+int read_back(cudaStream_t st, const void *src, void *dst, size_t bytes, frt_error *err, const char *what)
+{
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(err, e, what);
+    return FRT_OK;
+}
+
+#define LAUNCH_OK(what)                                                                                                \
+    do {                                                                                                               \
+        cudaError_t le_ = cudaGetLastError();                                                                          \
+        if (le_ != cudaSuccess) return cuda_fail(err, le_, what);                                                      \
+    } while (0)
+
+} // namespace
+
+// ---- FASTQ -------------------------------------------------------------------
+
+extern "C" int frt_fastq_scanner_create(int device, void *stream, frt_fastq_scanner **out, frt_error *err)
+{
+    if (!out) return FRT_ERR_INVALID_ARGUMENT;
+    frt_fastq_scanner *s = new frt_fastq_scanner;
+    int rc = scanner_create(device, stream, &s->s, err);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return FRT_OK;
+}
+
+extern "C" void frt_fastq_scanner_destroy(frt_fastq_scanner *s)
+{
+    if (!s) return;
+    stream_release(s->s.shared);
+    delete s;
+}
+
+extern "C" int frt_fastq_decode(frt_fastq_scanner *sc, const frt_inflate_batch *b, uint64_t start, frt_columns **out,
+                                frt_error *err)
+{
+    if (!sc || !out) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    Scanner &s = sc->s;
+    DeviceGuardLite g(s.device);
+    std::lock_guard<std::mutex> lk(s.mu);
+    uint64_t len = b && b->data ? b->len : 0;
+    if (start >= len) { // empty(start.min(len)), fastq.rs:487-492
+        frt_columns *c = columns_new(s, FMT_FASTQ, kFastqWidths, FRT_FASTQ_COL_COUNT, 0);
+        c->tail = start < len ? start : len;
+        int rc = columns_alloc(c, err);
+        if (rc) {
+            columns_discard(c);
+            return rc;
+        }
+        return columns_finish(c, b, out);
+    }
+    int rc = check_batch(s, b, err);
+    if (rc) return rc;
+    if (len - start >= 0xffffffffull) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "FASTQ batch of %llu bytes exceeds 4 GiB",
+                  (unsigned long long)(len - start));
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    cudaStream_t st = s.stream;
+    Work w(st);
+    const u64 tbase = start & ~15ull;
+    const u64 n_tiles = (len - tbase + TILE - 1) / TILE;
+    const bool aligned = ((uintptr_t)b->data & 15) == 0;
+    u32 *tile_count, *tile_base, *partials, *d_u32;
+    u64 *totals;
+    if ((rc = w.get(&tile_count, n_tiles, err)) || (rc = w.get(&tile_base, n_tiles + 1, err)) ||
+        (rc = w.get(&partials, frt_scan_partials_len(n_tiles) + frt_scan_partials_len(len) + 8, err)) ||
+        (rc = w.get(&d_u32, 8, err)) || (rc = w.get(&totals, 8, err)))
+        return rc;
+    k_fq_nl_count<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, tbase, aligned, tile_count);
+    LAUNCH_OK("launching the newline count");
+    cudaError_t e = frt_launch_scan_u32(tile_count, n_tiles, partials, tile_base, d_u32, st);
+    if (e != cudaSuccess) return cuda_fail(err, e, "scanning newline counts");
+    uint32_t n_nl = 0;
+    if ((rc = read_back(st, d_u32, &n_nl, 4, err, "newline count"))) return rc;
+    u64 *nl;
+    if ((rc = w.get(&nl, (size_t)n_nl + 1, err))) return rc;
+    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, tbase, aligned, tile_base, nl);
+    LAUNCH_OK("launching the newline index");
+    // line starts: start, and one past every newline that is not the last byte
+    uint32_t n_lines = n_nl + 1;
+    {
+        uint64_t last_nl = 0;
+        if (n_nl && (rc = read_back(st, nl + n_nl - 1, &last_nl, 8, err, "last newline"))) return rc;
+        if (n_nl && last_nl + 1 >= len) n_lines = n_nl;
+    }
+    FqIndex ix{b->data, start, len, nl, n_nl, n_lines};
+    u32 *flags, *pos, *S, *W, *fails;
+    if ((rc = w.get(&flags, n_lines, err)) || (rc = w.get(&pos, (size_t)n_lines + 1, err)) ||
+        (rc = w.get(&fails, 4, err)))
+        return rc;
+    cudaMemsetAsync(fails, 0, 16, st);
+    k_fq_lines<<<grid_for(n_lines, 256), 256, 0, st>>>(ix, flags);
+    LAUNCH_OK("launching the line validation");
+    if ((e = frt_launch_scan_u32(flags, n_lines, partials, pos, d_u32, st)) != cudaSuccess)
+        return cuda_fail(err, e, "scanning record starts");
+    uint32_t n_s = 0;
+    if ((rc = read_back(st, d_u32, &n_s, 4, err, "record starts"))) return rc;
+    if ((rc = w.get(&S, (size_t)n_s + 1, err)) || (rc = w.get(&W, (size_t)n_s + 1, err))) return rc;
+    k_fq_compact<<<grid_for(n_lines, 256), 256, 0, st>>>(flags, pos, n_lines, S);
+    k_fq_check<<<grid_for(n_s + 1, 256), 256, 0, st>>>(ix, S, n_s, fails);
+    k_fq_finalize<<<1, 1, 0, st>>>(ix, flags, S, d_u32, fails, W, totals);
+    LAUNCH_OK("launching the tiling checks");
+    uint64_t tot[5];
+    if ((rc = read_back(st, totals, tot, sizeof tot, err, "FASTQ scan"))) return rc;
+    frt_columns *c = columns_new(s, FMT_FASTQ, kFastqWidths, FRT_FASTQ_COL_COUNT, tot[0]);
+    c->tail = tot[1];
+    c->info[0] = tot[2];
+    c->info[1] = tot[3];
+    c->info[2] = tot[3];
+    if ((rc = columns_alloc(c, err))) {
+        columns_discard(c);
+        return rc;
+    }
+    if (c->n) {
+        k_fq_decode<<<grid_for(c->n, 256), 256, 0, st>>>(
+            ix, tot[4] ? W : S, (u32)c->n, colp<u64>(c, FRT_FASTQ_COL_RECORD_OFFSETS),
+            colp<u32>(c, FRT_FASTQ_COL_SEQUENCE_START), colp<u32>(c, FRT_FASTQ_COL_PLUS_START),
+            colp<u32>(c, FRT_FASTQ_COL_QUALITY_START), colp<u32>(c, FRT_FASTQ_COL_SEQUENCE_LEN),
+            colp<u32>(c, FRT_FASTQ_COL_RECORD_END));
+        if ((e = cudaGetLastError()) != cudaSuccess) {
+            columns_discard(c);
+            return cuda_fail(err, e, "launching the FASTQ decode");
+        }
+    }
+    return columns_finish(c, b, out);
+}
+
+// ---- BCF ---------------------------------------------------------------------
+
+extern "C" int frt_bcf_scanner_create(int device, void *stream, frt_bcf_scanner **out, frt_error *err)
+{
+    if (!out) return FRT_ERR_INVALID_ARGUMENT;
+    frt_bcf_scanner *s = new frt_bcf_scanner;
+    int rc = scanner_create(device, stream, &s->s, err);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return FRT_OK;
+}
+
+extern "C" void frt_bcf_scanner_destroy(frt_bcf_scanner *s)
+{
+    if (!s) return;
+    stream_release(s->s.shared);
+    delete s;
+}
+
+extern "C" int frt_bcf_decode(frt_bcf_scanner *sc, const frt_inflate_batch *b, uint64_t start, uint32_t samples,
+                              uint32_t contigs, frt_columns **out, frt_error *err)
+{
+    if (!sc || !out) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    Scanner &s = sc->s;
+    DeviceGuardLite g(s.device);
+    std::lock_guard<std::mutex> lk(s.mu);
+    uint64_t len = b && b->data ? b->len : 0;
+    if (start >= len) { // empty(start.min(len)), bcf.rs:284-290
+        frt_columns *c = columns_new(s, FMT_BCF, kBcfWidths, FRT_BCF_COL_COUNT, 0);
+        c->tail = start < len ? start : len;
+        int rc = columns_alloc(c, err);
+        if (rc) {
+            columns_discard(c);
+            return rc;
+        }
+        return columns_finish(c, b, out);
+    }
+    int rc = check_batch(s, b, err);
+    if (rc) return rc;
+    if (len - start >= 0xffffffffull) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "BCF batch of %llu bytes exceeds 4 GiB",
+                  (unsigned long long)(len - start));
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    cudaStream_t st = s.stream;
+    Work w(st);
+    const u64 n_tiles = (len - start + SIEVE_TILE - 1) / SIEVE_TILE;
+    u32 *tile_count, *tile_base, *partials, *d_u32;
+    u64 *totals;
+    if ((rc = w.get(&tile_count, n_tiles, err)) || (rc = w.get(&tile_base, n_tiles + 1, err)) ||
+        (rc = w.get(&partials, frt_scan_partials_len(n_tiles) + 8, err)) || (rc = w.get(&d_u32, 8, err)) ||
+        (rc = w.get(&totals, 8, err)))
+        return rc;
+    cudaMemsetAsync(d_u32, 0, 32, st);
+    k_bcf_sieve<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, samples, contigs, 0, tile_count, nullptr,
+                                                  nullptr, nullptr);
+    LAUNCH_OK("launching the BCF sieve");
+    cudaError_t e = frt_launch_scan_u32(tile_count, n_tiles, partials, tile_base, d_u32, st);
+    if (e != cudaSuccess) return cuda_fail(err, e, "scanning survivors");
+    uint32_t nv = 0;
+    if ((rc = read_back(st, d_u32, &nv, 4, err, "survivor count"))) return rc;
+    u64 *V;
+    if ((rc = w.get(&V, (size_t)nv + 1, err))) return rc;
+    u32 *fails = d_u32 + 2, *overflow = d_u32 + 3;
+    k_bcf_sieve<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, samples, contigs, 1, tile_count, tile_base, V,
+                                                  overflow);
+    k_bcf_check<<<grid_for(nv + 1, 256), 256, 0, st>>>(b->data, start, len, V, nv, fails);
+    k_bcf_finalize<<<1, 1, 0, st>>>(b->data, start, len, V, d_u32, fails, overflow, totals);
+    LAUNCH_OK("launching the BCF tiling proof");
+    uint64_t tot[5];
+    if ((rc = read_back(st, totals, tot, sizeof tot, err, "BCF scan"))) return rc;
+    const u64 *list = V;
+    if (tot[4]) { // the walk (bcf.rs:376-410): count, then emit
+        k_bcf_walk<<<1, 1, 0, st>>>(b->data, start, len, nullptr, totals);
+        LAUNCH_OK("launching the BCF walk");
+        uint64_t wt[2];
+        if ((rc = read_back(st, totals, wt, sizeof wt, err, "BCF walk"))) return rc;
+        u64 *Wl;
+        if ((rc = w.get(&Wl, wt[0] + 1, err))) return rc;
+        k_bcf_walk<<<1, 1, 0, st>>>(b->data, start, len, Wl, totals);
+        LAUNCH_OK("launching the BCF walk");
+        tot[0] = wt[0];
+        tot[1] = wt[1];
+        list = Wl;
+    }
+    frt_columns *c = columns_new(s, FMT_BCF, kBcfWidths, FRT_BCF_COL_COUNT, tot[0]);
+    c->tail = tot[1];
+    c->info[0] = tot[2];
+    c->info[1] = tot[3];
+    c->info[2] = tot[3];
+    if ((rc = columns_alloc(c, err))) {
+        columns_discard(c);
+        return rc;
+    }
+    if (c->n) {
+        BcfCols bc{colp<int>(c, FRT_BCF_COL_CHROMOSOME_ID), colp<int>(c, FRT_BCF_COL_POSITION),
+                   colp<int>(c, FRT_BCF_COL_REFERENCE_SPAN), colp<u32>(c, FRT_BCF_COL_QUALITY),
+                   colp<u16>(c, FRT_BCF_COL_INFO_COUNT), colp<u16>(c, FRT_BCF_COL_ALLELE_COUNT),
+                   colp<u32>(c, FRT_BCF_COL_SAMPLE_COUNT), colp<u8>(c, FRT_BCF_COL_FORMAT_COUNT),
+                   colp<u64>(c, FRT_BCF_COL_RECORD_OFFSETS), colp<u32>(c, FRT_BCF_COL_ALLELES_START),
+                   colp<u32>(c, FRT_BCF_COL_FILTERS_START), colp<u32>(c, FRT_BCF_COL_INFO_START),
+                   colp<u32>(c, FRT_BCF_COL_GENOTYPES_START), colp<u32>(c, FRT_BCF_COL_RECORD_END)};
+        u32 *errors = d_u32 + 4;
+        k_bcf_decode<<<grid_for(c->n, 256), 256, 0, st>>>(b->data, len, list, (u32)c->n, bc, errors);
+        uint32_t n_err = 0;
+        if ((e = cudaGetLastError()) != cudaSuccess) {
+            columns_discard(c);
+            return cuda_fail(err, e, "launching the BCF decode");
+        }
+        if ((rc = read_back(st, errors, &n_err, 4, err, "BCF decode"))) {
+            columns_discard(c);
+            return rc;
+        }
+        if (n_err) { // bcf.rs:343-356
+            columns_discard(c);
+            set_error(err, FRT_ERR_MALFORMED, 0, 0, 0, 0, "bcf", "%u of %llu records failed to decode", n_err,
+                      (unsigned long long)tot[0]);
+            return FRT_ERR_MALFORMED;
+        }
+    }
+    return columns_finish(c, b, out);
+}
+
+// BCF header (crates/fritillaria-bcf/src/columnar/header.rs:111-310): where
+// records start, the sample count and the contig count.
+namespace {
+bool ws(uint8_t c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\f' || c == '\v'; }
+
+const uint8_t *attr(const uint8_t *b, const uint8_t *be, const char *key, const uint8_t **ve)
+{
+    size_t kl = strlen(key);
+    const uint8_t *p = b;
+    while (p < be) {
+        const uint8_t *s0 = p, *eq = nullptr;
+        bool quoted = false;
+        while (p < be) {
+            if (*p == '"') quoted = !quoted;
+            else if (*p == '=' && !quoted && !eq) eq = p;
+            else if (*p == ',' && !quoted) break;
+            ++p;
+        }
+        if (eq) {
+            const uint8_t *ns = s0, *ne = eq;
+            while (ns < ne && ws(*ns)) ++ns;
+            while (ne > ns && ws(ne[-1])) --ne;
+            if ((size_t)(ne - ns) == kl && memcmp(ns, key, kl) == 0) {
+                const uint8_t *v = eq + 1, *vend = p;
+                while (v < vend && ws(*v)) ++v;
+                while (vend > v && ws(vend[-1])) --vend;
+                if (vend - v >= 2 && *v == '"' && vend[-1] == '"') {
+                    ++v;
+                    --vend;
+                }
+                *ve = vend;
+                return v;
+            }
+        }
+        ++p;
+    }
+    return nullptr;
+}
+
+bool has_prefix(const uint8_t *s, const uint8_t *e, const char *pfx)
+{
+    size_t n = strlen(pfx);
+    return (size_t)(e - s) >= n && memcmp(s, pfx, n) == 0;
+}
+} // namespace
+
+extern "C" int frt_bcf_parse_header(const uint8_t *buf, size_t len, uint64_t *records_start, uint32_t *samples,
+                                    uint32_t *contigs, frt_error *err)
+{
+    auto bad = [&](uint64_t pos, const char *why) {
+        set_error(err, FRT_ERR_MALFORMED, 0, 0, 0, pos, "bcf header", "%s", why);
+        return FRT_ERR_MALFORMED;
+    };
+    if (!buf || len < 9) return bad(0, "truncated header");
+    if (memcmp(buf, "BCF", 3) != 0) return bad(0, "bad magic; expected BCF");
+    if (buf[3] != 2) return bad(3, "unsupported major version; expected 2");
+    uint64_t l_text = (uint64_t)buf[5] | ((uint64_t)buf[6] << 8) | ((uint64_t)buf[7] << 16) | ((uint64_t)buf[8] << 24);
+    if (9 + l_text > len) return bad(5, "l_text runs past the end of the buffer");
+    const uint8_t *t = buf + 9, *te = buf + 9 + l_text;
+    while (te > t && te[-1] == 0) --te;
+    uint32_t n_samples = 0, n_contigs = 0;
+    std::vector<std::pair<const uint8_t *, size_t>> seen;
+    for (const uint8_t *line = t; line < te;) {
+        const uint8_t *le = (const uint8_t *)memchr(line, '\n', (size_t)(te - line));
+        if (!le) le = te;
+        const uint8_t *next = le < te ? le + 1 : te;
+        if (le > line && le[-1] == '\r') --le;
+        if (le == line) {
+            line = next;
+            continue;
+        }
+        if (has_prefix(line, le, "#CHROM")) {
+            size_t pieces = 1;
+            for (const uint8_t *p = line + 6; p < le; ++p) pieces += *p == '\t';
+            n_samples = pieces > 9 ? (uint32_t)(pieces - 9) : 0;
+            line = next;
+            continue;
+        }
+        const uint8_t *open = (const uint8_t *)memchr(line, '<', (size_t)(le - line)), *close = nullptr;
+        for (const uint8_t *p = le; p > line; --p)
+            if (p[-1] == '>') {
+                close = p - 1;
+                break;
+            }
+        const uint8_t *ide = nullptr, *id = (open && close && close > open) ? attr(open + 1, close, "ID", &ide) : nullptr;
+        if (!id) {
+            line = next;
+            continue;
+        }
+        if (has_prefix(line, le, "##contig=")) {
+            ++n_contigs;
+        } else if (has_prefix(line, le, "##FILTER=") || has_prefix(line, le, "##INFO=") ||
+                   has_prefix(line, le, "##FORMAT=")) {
+            size_t il = (size_t)(ide - id);
+            bool dup = il == 4 && memcmp(id, "PASS", 4) == 0;
+            for (auto &p : seen)
+                if (!dup && p.second == il && memcmp(p.first, id, il) == 0) dup = true;
+            if (!dup) {
+                const uint8_t *xe = nullptr, *x = attr(open + 1, close, "IDX", &xe);
+                if (x) {
+                    bool ok = xe > x;
+                    for (const uint8_t *p = x; p < xe && ok; ++p) ok = *p >= '0' && *p <= '9';
+                    if (!ok) return bad(0, "unparseable IDX on header line");
+                }
+                seen.emplace_back(id, il);
+            }
+        }
+        line = next;
+    }
+    if (records_start) *records_start = 9 + l_text;
+    if (samples) *samples = n_samples;
+    if (contigs) *contigs = n_contigs;
+    return FRT_OK;
+}
+
+// ---- FASTA -------------------------------------------------------------------
+
+extern "C" int frt_fasta_compactor_create(int device, void *stream, frt_fasta_compactor **out, frt_error *err)
+{
+    if (!out) return FRT_ERR_INVALID_ARGUMENT;
+    frt_fasta_compactor *s = new frt_fasta_compactor;
+    int rc = scanner_create(device, stream, &s->s, err);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return FRT_OK;
+}
+
+extern "C" void frt_fasta_compactor_destroy(frt_fasta_compactor *s)
+{
+    if (!s) return;
+    stream_release(s->s.shared);
+    delete s;
+}
+
+extern "C" int frt_fasta_compact(frt_fasta_compactor *sc, const frt_inflate_batch *b, frt_columns **out,
+                                 frt_error *err)
+{
+    if (!sc || !out) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    Scanner &s = sc->s;
+    DeviceGuardLite g(s.device);
+    std::lock_guard<std::mutex> lk(s.mu);
+    uint64_t len = b && b->data ? b->len : 0;
+    auto empty = [&]() {
+        frt_columns *c = columns_new(s, FMT_FASTA, kFastaWidths, FRT_FASTA_COL_COUNT, 0);
+        c->col_bytes[FRT_FASTA_COL_SEQUENCE] = 0;
+        int rc = columns_alloc(c, err);
+        if (rc) {
+            columns_discard(c);
+            return rc;
+        }
+        return columns_finish(c, b, out);
+    };
+    if (len == 0) return empty();
+    int rc = check_batch(s, b, err);
+    if (rc) return rc;
+    cudaStream_t st = s.stream;
+    Work w(st);
+    const u64 n_tiles = (len + TILE - 1) / TILE;
+    if (n_tiles >= 0xffffffffull) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "FASTA batch too large");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    const bool aligned = ((uintptr_t)b->data & 15) == 0;
+    u8 *tile_f, *tile_state;
+    u32 *tile_contigs, *contig_base, *tile_kept;
+    u64 *out_base, *totals;
+    unsigned long long *last_contig;
+    if ((rc = w.get(&tile_f, n_tiles, err)) || (rc = w.get(&tile_state, n_tiles, err)) ||
+        (rc = w.get(&tile_contigs, n_tiles, err)) || (rc = w.get(&contig_base, n_tiles, err)) ||
+        (rc = w.get(&tile_kept, n_tiles, err)) || (rc = w.get(&out_base, n_tiles + 1, err)) ||
+        (rc = w.get(&totals, 8, err)) || (rc = w.get(&last_contig, 2, err)))
+        return rc;
+    cudaMemsetAsync(last_contig, 0, 16, st);
+    cudaMemsetAsync(totals, 0, 64, st);
+    k_fa_pass1<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, len, aligned, tile_f, tile_contigs, last_contig);
+    k_fa_tiles<<<1, 1024, 0, st>>>(b->data, len, tile_f, tile_contigs, (u32)n_tiles, tile_state, contig_base,
+                                   last_contig, totals);
+    k_fa_pass2<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, len, aligned, tile_state, tile_kept);
+    k_scan_tiles64<<<1, 1024, 0, st>>>(tile_kept, (u32)n_tiles, out_base, totals + 1);
+    LAUNCH_OK("launching the FASTA scans");
+    uint64_t tot[3];
+    if ((rc = read_back(st, totals, tot, sizeof tot, err, "FASTA layout"))) return rc;
+    const uint64_t n = tot[0], total = tot[1];
+    if (n == 0) return empty();
+    frt_columns *c = columns_new(s, FMT_FASTA, kFastaWidths, FRT_FASTA_COL_COUNT, n);
+    c->total = total;
+    c->col_bytes[FRT_FASTA_COL_SEQUENCE] = 0; // the bases have their own allocation
+    if ((rc = columns_alloc(c, err)) || (rc = dev_alloc((void **)&c->seq, total + 16, st, err))) {
+        columns_discard(c);
+        return rc;
+    }
+    c->col_bytes[FRT_FASTA_COL_SEQUENCE] = total;
+    u64 *seq_off = colp<u64>(c, FRT_FASTA_COL_SEQUENCE_OFFSETS), *seq_len = colp<u64>(c, FRT_FASTA_COL_SEQUENCE_LENGTHS),
+        *rec_off = colp<u64>(c, FRT_FASTA_COL_RECORD_OFFSETS);
+    k_fa_pass3<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, len, aligned, tile_state, contig_base, out_base, n, c->seq,
+                                                 seq_off, rec_off);
+    k_fa_lengths<<<grid_for(n, 256), 256, 0, st>>>(seq_off, n, total, seq_len);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        columns_discard(c);
+        return cuda_fail(err, e, "launching the FASTA compaction");
+    }
+    return columns_finish(c, b, out);
+}
+
+// ---- column batches ------------------------------------------------------------
+
+extern "C" uint64_t frt_columns_len(const frt_columns *c) { return c ? c->n : 0; }
+extern "C" uint64_t frt_columns_tail(const frt_columns *c) { return c ? c->tail : 0; }
+extern "C" uint64_t frt_columns_total_bases(const frt_columns *c) { return c ? c->total : 0; }
+extern "C" int frt_columns_count(const frt_columns *c) { return c ? c->n_cols : 0; }
+extern "C" int frt_columns_device_ordinal(const frt_columns *c) { return c ? c->device : -1; }
+extern "C" void *frt_columns_ready_event(const frt_columns *c) { return c ? (void *)c->ready : nullptr; }
+
+extern "C" void frt_columns_scan_info(const frt_columns *c, uint64_t *proof, uint64_t *survivors, uint64_t *validated)
+{
+    if (proof) *proof = c ? c->info[0] : 0;
+    if (survivors) *survivors = c ? c->info[1] : 0;
+    if (validated) *validated = c ? c->info[2] : 0;
+}
+
+static const uint8_t *column_base(const frt_columns *c, int k)
+{
+    if (c->format == FMT_FASTA && k == FRT_FASTA_COL_SEQUENCE) return c->seq;
+    return c->cols + c->col_off[k];
+}
+
+extern "C" int frt_columns_column(const frt_columns *c, int column, void **ptr, size_t *bytes, size_t *width)
+{
+    if (!c || column < 0 || column >= c->n_cols) return FRT_ERR_INVALID_ARGUMENT;
+    if (ptr) *ptr = (void *)column_base(c, column);
+    if (bytes) *bytes = c->col_bytes[column];
+    if (width) *width = c->widths[column];
+    return FRT_OK;
+}
+
+extern "C" int frt_columns_column_to_host(const frt_columns *c, int column, void *dst, size_t cap, frt_error *err)
+{
+    if (!c || column < 0 || column >= c->n_cols) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "bad column %d", column);
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    size_t bytes = c->col_bytes[column];
+    if (cap < bytes) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "destination holds %zu bytes, column has %zu",
+                  cap, bytes);
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    if (!bytes) return FRT_OK;
+    DeviceGuardLite g(c->device);
+    cudaError_t e = cudaMemcpyAsync(dst, column_base(c, column), bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(err, e, "downloading column");
+    return FRT_OK;
+}
+
+extern "C" void frt_columns_free(frt_columns *c)
+{
+    if (!c) return;
+    {
+        DeviceGuardLite g(c->device);
+        if (c->ready) cudaEventDestroy(c->ready);
+    }
+    const frt_inflate_batch *src = c->source;
+    {
+        DeviceGuardLite g(c->device);
+        columns_discard(c);
+    }
+    if (src) batch_release(src);
+}

@@ -210,7 +210,7 @@ void short_record(std::vector<uint8_t> &out, uint64_t i, uint64_t n_records,
     int64_t mpos = reverse ? std::max<int64_t>(0, pos - insert + L) : pos + insert - L;
     int32_t tlen = reverse ? -insert : insert;
 
-    char name[16];
+    char name[24];
     snprintf(name, sizeof name, "r%09llu", (unsigned long long)(i / 2));
     size_t name_len = strlen(name) + 1;
 
@@ -364,6 +364,219 @@ void long_record(std::vector<uint8_t> &out, uint64_t i, uint32_t l_seq, uint64_t
     if (ch <= 255) { out.push_back('C'); out.push_back((uint8_t)ch); }
     else { out.push_back('S'); put16(out, (uint16_t)ch); }
     patch32(out, start, (uint32_t)(out.size() - start - 4));
+}
+
+
+// ---- FASTQ ---------------------------------------------------------------
+// Illumina-like (kind 0): 40-60 character names, 150 bases (0.1% N), Phred+33
+// qualities ~ N(35, 5) clipped to 2..41, so '@' (Q31) starts about one quality
+// line in twenty -- the decoys a record-start scan must reject.  Ultra-long
+// (kind 1): log-normal lengths (median 15 kb), qualities ~ N(15, 5) in 1..50.
+void fastq_record(std::vector<uint8_t> &out, uint64_t i, int kind, uint64_t seed)
+{
+    Rng r(seed, 0x20000000ull + i);
+    char name[160];
+    int nl;
+    uint32_t len;
+    if (kind == 0) {
+        nl = snprintf(name, sizeof name, "@A%05u:%u:H%07uDSXX:%u:%u:%u:%u %u:N:0:%s", 100 + r.below(900),
+                      1 + r.below(99), r.below(9999999), 1 + r.below(4), 1101 + r.below(2600),
+                      1000 + r.below(30000), 1000 + r.below(30000), 1 + (uint32_t)(i & 1),
+                      (i % 3) ? "ACGTACGT+TTGACCAA" : "GGCCTTAA");
+        len = 150;
+    } else {
+        nl = snprintf(name, sizeof name, "@%08x-%04x-%04x-%04x-%012llx runid=%08x read=%llu ch=%u", (uint32_t)r.next(),
+                      r.below(65536), r.below(65536), r.below(65536), (unsigned long long)(r.next() >> 16),
+                      (uint32_t)r.next(), (unsigned long long)i, 1 + r.below(512));
+        double l = std::exp(std::log(15000.0) + 0.8 * r.normal());
+        len = (uint32_t)std::min(400000.0, std::max(1.0, std::floor(l)));
+    }
+    out.insert(out.end(), name, name + nl);
+    out.push_back('\n');
+    static const char bases[4] = {'A', 'C', 'G', 'T'};
+    for (uint32_t k = 0; k < len; ++k) out.push_back(r.below(1000) == 0 ? 'N' : bases[r.next() >> 62]);
+    out.push_back('\n');
+    out.push_back('+');
+    out.push_back('\n');
+    for (uint32_t k = 0; k < len; ++k) {
+        double q = kind == 0 ? 35.0 + 5.0 * r.normal() : 15.0 + 5.0 * r.normal();
+        int qi = (int)std::lround(q);
+        qi = kind == 0 ? std::min(41, std::max(2, qi)) : std::min(50, std::max(1, qi));
+        out.push_back((uint8_t)(33 + qi));
+    }
+    out.push_back('\n');
+}
+
+// ---- BCF -----------------------------------------------------------------
+// Sites over human-proportioned contigs; REF/ALT 90% SNV, else an indel of
+// 1-20 bases; QUAL float (1% missing); INFO DP (int8/int16/int32 by value)
+// and AF (float), plus every tenth site an ANN string of 16-80 characters so
+// the typed-value length escape fires; FORMAT GT (int8 x 2, phased diploid,
+// alt allele frequency ~ Beta(0.5, 2)) and DP (int16 ~ N(30, 5.5)) per sample.
+const uint8_t T_INT8 = 1, T_INT16 = 2, T_INT32 = 3, T_FLOAT = 5, T_CHAR = 7;
+
+void typed_len(std::vector<uint8_t> &b, uint32_t n, uint8_t type)
+{
+    if (n < 15) {
+        b.push_back((uint8_t)(n << 4 | type));
+        return;
+    }
+    b.push_back((uint8_t)(15 << 4 | type));
+    if (n < 128) {
+        b.push_back(0x10 | T_INT8);
+        b.push_back((uint8_t)n);
+    } else if (n < 32768) {
+        b.push_back(0x10 | T_INT16);
+        put16(b, (uint16_t)n);
+    } else {
+        b.push_back(0x10 | T_INT32);
+        put32(b, n);
+    }
+}
+
+void typed_string(std::vector<uint8_t> &b, const std::string &s)
+{
+    typed_len(b, (uint32_t)s.size(), T_CHAR);
+    b.insert(b.end(), s.begin(), s.end());
+}
+
+void typed_int(std::vector<uint8_t> &b, int32_t v)
+{
+    if (v > -120 && v < 128) {
+        b.push_back(0x10 | T_INT8);
+        b.push_back((uint8_t)(int8_t)v);
+    } else if (v > -32760 && v < 32768) {
+        b.push_back(0x10 | T_INT16);
+        put16(b, (uint16_t)(int16_t)v);
+    } else {
+        b.push_back(0x10 | T_INT32);
+        put32(b, (uint32_t)v);
+    }
+}
+
+std::vector<uint8_t> bcf_header(const std::vector<Contig> &contigs, uint32_t n_samples)
+{
+    std::string t = "##fileformat=VCFv4.2\n##FILTER=<ID=PASS,Description=\"All filters passed\">\n";
+    for (auto &c : contigs) t += "##contig=<ID=" + c.name + ",length=" + std::to_string(c.length) + ">\n";
+    t += "##INFO=<ID=DP,Number=1,Type=Integer,Description=\"Total depth\">\n"
+         "##INFO=<ID=AF,Number=A,Type=Float,Description=\"Allele frequency\">\n"
+         "##INFO=<ID=ANN,Number=.,Type=String,Description=\"Annotation\">\n"
+         "##FORMAT=<ID=GT,Number=1,Type=String,Description=\"Genotype\">\n"
+         "##FORMAT=<ID=DP,Number=1,Type=Integer,Description=\"Read depth\">\n"
+         "#CHROM\tPOS\tID\tREF\tALT\tQUAL\tFILTER\tINFO";
+    if (n_samples) t += "\tFORMAT";
+    for (uint32_t s = 0; s < n_samples; ++s) t += "\tS" + std::to_string(s);
+    t += "\n";
+    std::vector<uint8_t> h = {'B', 'C', 'F', 2, 2};
+    put32(h, (uint32_t)t.size() + 1);
+    h.insert(h.end(), t.begin(), t.end());
+    h.push_back(0);
+    return h;
+}
+
+// Dictionary numbering of the header above: PASS 0, DP 1, AF 2, ANN 3, GT 4.
+void bcf_record(std::vector<uint8_t> &out, uint64_t i, int32_t chrom, int32_t pos, uint32_t n_samples,
+                uint64_t seed)
+{
+    Rng r(seed, 0x30000000ull + i);
+    static const char bases[4] = {'A', 'C', 'G', 'T'};
+    std::string ref(1, bases[r.next() >> 62]), alt(1, bases[r.next() >> 62]);
+    if (alt == ref) alt = ref == "A" ? "G" : "A";
+    if (r.below(10) == 0) {
+        uint32_t l = 1 + r.below(20);
+        std::string ins;
+        for (uint32_t k = 0; k < l; ++k) ins.push_back(bases[r.next() >> 62]);
+        if (r.below(2)) alt = ref + ins;
+        else ref = ref + ins;
+    }
+    size_t base = out.size();
+    put32(out, 0); // l_shared
+    put32(out, 0); // l_indiv
+    put32(out, (uint32_t)chrom);
+    put32(out, (uint32_t)pos);
+    put32(out, (uint32_t)ref.size());
+    float q = (float)(10.0 + 990.0 * r.uniform());
+    uint32_t qb;
+    memcpy(&qb, &q, 4);
+    if (r.below(100) == 0) qb = 0x7F800001u;
+    put32(out, qb);
+    bool ann = i % 10 == 0;
+    put16(out, ann ? 3 : 2);
+    put16(out, 2);
+    put32(out, n_samples | ((n_samples ? 2u : 0u) << 24));
+    if (r.below(10) < 3) typed_string(out, "rs" + std::to_string(1000 + r.below(90000000)));
+    else out.push_back(T_CHAR); // '.'
+    typed_string(out, ref);
+    typed_string(out, alt);
+    out.push_back(0x10 | T_INT8); // FILTER: PASS
+    out.push_back(0);
+    double af = std::pow(r.uniform(), 2.0); // Beta(0.5, 1)-like skew toward rare alleles
+    uint32_t dp = 20 * n_samples + r.below(1 + 10 * n_samples);
+    typed_int(out, 1);
+    typed_int(out, (int32_t)std::min<uint32_t>(dp, 2000000000u));
+    typed_int(out, 2);
+    out.push_back(0x10 | T_FLOAT);
+    float aff = (float)af;
+    uint32_t afb;
+    memcpy(&afb, &aff, 4);
+    put32(out, afb);
+    if (ann) {
+        typed_int(out, 3);
+        std::string a = "T|missense_variant|MODERATE|GENE" + std::to_string(r.below(20000));
+        uint32_t extra = r.below(48);
+        for (uint32_t k = 0; k < extra; ++k) a.push_back((char)('a' + r.below(26)));
+        typed_string(out, a);
+    }
+    uint32_t l_shared = (uint32_t)(out.size() - base - 8);
+    size_t indiv = out.size();
+    if (n_samples) {
+        typed_int(out, 4); // GT
+        out.push_back(0x20 | T_INT8);
+        for (uint32_t s = 0; s < n_samples; ++s) {
+            for (int h = 0; h < 2; ++h) {
+                uint32_t allele = r.uniform() < af ? 1 : 0;
+                out.push_back((uint8_t)(((allele + 1) << 1) | (h ? 1 : 0)));
+            }
+        }
+        typed_int(out, 1); // DP
+        out.push_back(0x10 | T_INT16);
+        for (uint32_t s = 0; s < n_samples; ++s) {
+            int d = (int)std::lround(30.0 + 5.5 * r.normal());
+            put16(out, (uint16_t)std::max(0, d));
+        }
+    }
+    patch32(out, base, l_shared);
+    patch32(out, base + 4, (uint32_t)(out.size() - indiv));
+}
+
+// ---- FASTA ---------------------------------------------------------------
+// Contigs with lengths proportional to the human chromosomes, `line_width`
+// bases per line, soft-masked (lowercase) runs covering about half the bases,
+// runs of N of 1 kb - 1 Mb covering about 5%, an NCBI-style definition line
+// and, when asked, a blank line between records.  Bases are drawn in
+// fixed-size chunks, each from its own stream, so generation is parallel.
+void fasta_chunk(uint8_t *dst, uint64_t contig, uint64_t chunk_index, uint64_t n, uint64_t seed)
+{
+    Rng r(seed, 0x40000000ull + (contig << 24) + chunk_index);
+    static const char upper[4] = {'A', 'C', 'G', 'T'}, lower[4] = {'a', 'c', 'g', 't'};
+    uint64_t k = 0;
+    bool masked = r.below(2);
+    while (k < n) {
+        uint64_t run;
+        if (r.below(1000) == 0) { // an N run
+            run = 1000 + (uint64_t)(std::exp(r.uniform() * std::log(1000.0)) * 1000.0) - 1000;
+            run = std::min(run, n - k);
+            memset(dst + k, 'N', run);
+            k += run;
+            continue;
+        }
+        run = 50 + r.below(4000);
+        run = std::min(run, n - k);
+        const char *tab = masked ? lower : upper;
+        for (uint64_t j = 0; j < run; ++j) dst[k + j] = (uint8_t)tab[r.next() >> 62];
+        k += run;
+        masked = !masked;
+    }
 }
 
 void run_parallel(int threads, size_t n, const std::function<void(size_t)> &fn)
@@ -542,6 +755,146 @@ int frt_synth_bgzf(const uint8_t *raw, size_t raw_len, int mode, uint32_t member
     *out = o;
     *out_len = total;
     if (n_members_out) *n_members_out = nm + 1;
+    return 0;
+}
+
+
+// Joins per-chunk parts after `head`; optional record end offsets.
+static int join_parts(const std::vector<uint8_t> &head, std::vector<std::vector<uint8_t>> &parts,
+                      std::vector<std::vector<uint64_t>> &ends, int threads, uint8_t **raw, size_t *raw_len,
+                      uint64_t **record_ends, size_t *n_ends)
+{
+    size_t n_chunks = parts.size();
+    std::vector<size_t> base(n_chunks + 1, head.size());
+    for (size_t c = 0; c < n_chunks; ++c) base[c + 1] = base[c] + parts[c].size();
+    size_t total = base[n_chunks];
+    uint8_t *buf = (uint8_t *)malloc(total ? total : 1);
+    if (!buf) return -1;
+    if (!head.empty()) memcpy(buf, head.data(), head.size());
+    run_parallel(threads, n_chunks, [&](size_t c) {
+        memcpy(buf + base[c], parts[c].data(), parts[c].size());
+        std::vector<uint8_t>().swap(parts[c]);
+    });
+    if (record_ends) {
+        size_t n = 1;
+        for (auto &e : ends) n += e.size();
+        uint64_t *re = (uint64_t *)malloc(sizeof(uint64_t) * n);
+        re[0] = head.size();
+        size_t k = 1;
+        for (size_t c = 0; c < n_chunks; ++c)
+            for (uint64_t v : ends[c]) re[k++] = base[c] + v;
+        *record_ends = re;
+        *n_ends = k;
+    }
+    *raw = buf;
+    *raw_len = total;
+    return 0;
+}
+
+// FASTQ stream of `n_records` (kind 0 Illumina-like, 1 ultra-long).
+int frt_synth_fastq(int kind, uint64_t n_records, uint64_t seed, int threads, uint8_t **raw, size_t *raw_len,
+                    uint64_t **record_ends, size_t *n_ends)
+{
+    const uint64_t chunk = kind == 0 ? 65536 : 64;
+    size_t n_chunks = (size_t)((n_records + chunk - 1) / chunk);
+    std::vector<std::vector<uint8_t>> parts(n_chunks);
+    std::vector<std::vector<uint64_t>> ends(n_chunks);
+    run_parallel(threads, n_chunks, [&](size_t c) {
+        for (uint64_t i = c * chunk, e = std::min(n_records, (c + 1) * chunk); i < e; ++i) {
+            fastq_record(parts[c], i, kind, seed);
+            if (record_ends) ends[c].push_back(parts[c].size());
+        }
+    });
+    return join_parts({}, parts, ends, threads, raw, raw_len, record_ends, n_ends);
+}
+
+// BCF stream (header + records) of `n_sites` over `n_contigs` contigs of a
+// 3.1 Gb genome with `n_samples` samples.
+int frt_synth_bcf(uint64_t n_sites, uint32_t n_samples, int n_contigs, uint64_t seed, int threads, uint8_t **raw,
+                  size_t *raw_len, uint64_t **record_ends, size_t *n_ends)
+{
+    std::vector<Contig> contigs = make_contigs(n_contigs, 3100000000ull);
+    std::vector<uint8_t> head = bcf_header(contigs, n_samples);
+    // sites per contig in proportion to length, evenly spaced with jitter
+    std::vector<uint64_t> first(contigs.size() + 1, 0);
+    uint64_t glen = 0;
+    for (auto &c : contigs) glen += c.length;
+    for (size_t k = 0; k < contigs.size(); ++k)
+        first[k + 1] = k + 1 == contigs.size() ? n_sites
+                                               : first[k] + (uint64_t)((double)n_sites * contigs[k].length / glen);
+    const uint64_t chunk = n_samples > 64 ? 1024 : 16384;
+    size_t n_chunks = (size_t)((n_sites + chunk - 1) / chunk);
+    std::vector<std::vector<uint8_t>> parts(n_chunks);
+    std::vector<std::vector<uint64_t>> ends(n_chunks);
+    run_parallel(threads, n_chunks, [&](size_t c) {
+        for (uint64_t i = c * chunk, e = std::min(n_sites, (c + 1) * chunk); i < e; ++i) {
+            size_t k = (size_t)(std::upper_bound(first.begin(), first.end(), i) - first.begin() - 1);
+            uint64_t n_here = std::max<uint64_t>(1, first[k + 1] - first[k]);
+            double step = (double)contigs[k].length / (double)n_here;
+            Rng j(seed, 0x50000000ull + i);
+            int32_t pos = (int32_t)std::min<double>(contigs[k].length - 1.0,
+                                                    (double)(i - first[k]) * step + j.uniform() * step * 0.5);
+            bcf_record(parts[c], i, (int32_t)k, pos, n_samples, seed);
+            if (record_ends) ends[c].push_back(parts[c].size());
+        }
+    });
+    return join_parts(head, parts, ends, threads, raw, raw_len, record_ends, n_ends);
+}
+
+// FASTA text of `n_contigs` contigs totalling about `total_bases`, wrapped at
+// `line_width`; `blank_lines` puts an empty line between records.
+int frt_synth_fasta(int n_contigs, uint64_t total_bases, uint32_t line_width, int blank_lines, uint64_t seed,
+                    int threads, uint8_t **raw, size_t *raw_len)
+{
+    if (line_width == 0) return -1;
+    std::vector<Contig> contigs = make_contigs(n_contigs, total_bases);
+    uint64_t sum = 0;
+    for (auto &c : contigs) sum += c.length;
+    for (auto &c : contigs) c.length = (uint32_t)std::max<uint64_t>(1, (uint64_t)((double)c.length * total_bases / sum));
+    // chunks of whole lines, about 1 Mb each
+    const uint64_t chunk = (uint64_t)line_width * std::max<uint64_t>(1, (1u << 20) / line_width);
+    // each contig: definition line, wrapped bases, optional blank line
+    struct Piece { uint64_t contig, first, n, dst, index; };
+    std::vector<std::string> defs;
+    std::vector<uint64_t> contig_at;
+    uint64_t at = 0;
+    std::vector<Piece> pieces;
+    for (size_t k = 0; k < contigs.size(); ++k) {
+        Rng r(seed, 0x60000000ull + k);
+        std::string d = ">" + contigs[k].name + " AC:CM" + std::to_string(100000 + r.below(900000)) +
+                        ".2 LN:" + std::to_string(contigs[k].length) + " rl:Chromosome AS:synthetic\n";
+        defs.push_back(d);
+        contig_at.push_back(at);
+        uint64_t L = contigs[k].length, lines = (L + line_width - 1) / line_width;
+        uint64_t seq_at = at + d.size();
+        for (uint64_t f = 0; f < L; f += chunk)
+            pieces.push_back({k, f, std::min<uint64_t>(chunk, L - f), seq_at + f + f / line_width, f / chunk});
+        at = seq_at + L + lines + (blank_lines && k + 1 < contigs.size() ? 1 : 0);
+    }
+    uint8_t *buf = (uint8_t *)malloc(at ? at : 1);
+    if (!buf) return -1;
+    for (size_t k = 0; k < contigs.size(); ++k) {
+        memcpy(buf + contig_at[k], defs[k].data(), defs[k].size());
+        uint64_t L = contigs[k].length, lines = (L + line_width - 1) / line_width;
+        uint64_t end = contig_at[k] + defs[k].size() + L + lines;
+        if (blank_lines && k + 1 < contigs.size()) buf[end] = '\n';
+    }
+    run_parallel(threads, pieces.size(), [&](size_t i) {
+        const Piece &p = pieces[i];
+        std::vector<uint8_t> tmp(p.n);
+        fasta_chunk(tmp.data(), p.contig, p.index, p.n, seed);
+        uint8_t *d = buf + p.dst;
+        uint64_t L = contigs[p.contig].length;
+        for (uint64_t j = 0; j < p.n;) {
+            uint64_t g = p.first + j, in_line = g % line_width, take = std::min<uint64_t>(line_width - in_line, p.n - j);
+            memcpy(d, tmp.data() + j, take);
+            d += take;
+            j += take;
+            if ((g + take) % line_width == 0 || g + take == L) *d++ = '\n';
+        }
+    });
+    *raw = buf;
+    *raw_len = at;
     return 0;
 }
 

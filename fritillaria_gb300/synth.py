@@ -42,6 +42,12 @@ def _load():
         _lib.frt_synth_bgzf.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_uint32, C.c_void_p, C.c_size_t,
                                         C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.frt_synth_free.argtypes = [C.c_void_p]
+        _lib.frt_synth_fastq.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_int, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p]
+        _lib.frt_synth_bcf.argtypes = [C.c_uint64, C.c_uint32, C.c_int, C.c_uint64, C.c_int, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p]
+        _lib.frt_synth_fasta.argtypes = [C.c_int, C.c_uint64, C.c_uint32, C.c_int, C.c_uint64, C.c_int, C.c_void_p,
+                                         C.c_void_p]
     return _lib
 
 
@@ -104,6 +110,67 @@ def ultra_long_bam(n_records: int, n_long_extra: int = 0, seed: int = 3, levels=
                    member_payload: int = 65495):
     raw, ends = raw_bam("ultra_long", n_records, 1, 0, seed, n_long_extra)
     return raw, bgzf(raw, packing, levels, ends, member_payload)
+
+
+def _with_ends(fn, *args):
+    lib = _load()
+    raw = C.c_void_p()
+    raw_len = C.c_size_t()
+    ends = C.c_void_p()
+    n_ends = C.c_size_t()
+    if fn(*args, C.byref(raw), C.byref(raw_len), C.byref(ends), C.byref(n_ends)) != 0:
+        raise MemoryError("synthetic generation failed")
+    data = _take(raw, raw_len.value)
+    e = np.empty(n_ends.value, dtype=np.uint64)
+    C.memmove(e.ctypes.data, ends, 8 * n_ends.value)
+    lib.frt_synth_free(ends)
+    return data, e
+
+
+def raw_fastq(n_records: int, kind: str = "illumina", seed: int = 1, threads: int | None = None):
+    """FASTQ text and the end offset of every record (first entry 0)."""
+    return _with_ends(_load().frt_synth_fastq, 0 if kind == "illumina" else 1, n_records, seed,
+                      threads or os.cpu_count() or 1)
+
+
+def fastq(n_records: int, kind: str = "illumina", seed: int = 1, levels=(6, 6), packing: str = "full",
+          member_payload: int = 65495):
+    """(FASTQ text, bgzipped FASTQ)."""
+    raw, ends = raw_fastq(n_records, kind, seed)
+    return raw, bgzf(raw, packing, levels, ends, member_payload)
+
+
+def raw_bcf(n_sites: int, n_samples: int = 500, n_contigs: int = 24, seed: int = 1, threads: int | None = None):
+    """Uncompressed BCF (header + records) and the end offsets of the header
+    and of every record."""
+    return _with_ends(_load().frt_synth_bcf, n_sites, n_samples, n_contigs, seed, threads or os.cpu_count() or 1)
+
+
+def bcf(n_sites: int, n_samples: int = 500, n_contigs: int = 24, seed: int = 1, levels=(6, 6),
+        packing: str = "full", member_payload: int = 65280):
+    """(uncompressed BCF, BGZF-compressed BCF); bcftools packs members full."""
+    raw, ends = raw_bcf(n_sites, n_samples, n_contigs, seed)
+    return raw, bgzf(raw, packing, levels, ends, member_payload)
+
+
+def raw_fasta(n_contigs: int = 24, total_bases: int = 3_100_000_000, line_width: int = 60, blank_lines: bool = False,
+              seed: int = 1, threads: int | None = None) -> np.ndarray:
+    """FASTA text wrapped at `line_width` bases per line."""
+    lib = _load()
+    raw = C.c_void_p()
+    raw_len = C.c_size_t()
+    rc = lib.frt_synth_fasta(n_contigs, total_bases, line_width, int(blank_lines), seed,
+                             threads or os.cpu_count() or 1, C.byref(raw), C.byref(raw_len))
+    if rc != 0:
+        raise ValueError("synthetic FASTA generation failed")
+    return _take(raw, raw_len.value)
+
+
+def fasta(n_contigs: int = 24, total_bases: int = 3_100_000_000, line_width: int = 60, blank_lines: bool = False,
+          seed: int = 1, levels=(6, 6)):
+    """(FASTA text, bgzipped FASTA)."""
+    raw = raw_fasta(n_contigs, total_bases, line_width, blank_lines, seed)
+    return raw, bgzf(raw, "full", levels)
 
 
 # The benchmark configurations.

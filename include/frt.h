@@ -236,6 +236,95 @@ int frt_record_batch_column_to_host(const frt_record_batch *rb, int column, void
 void *frt_record_batch_ready_event(const frt_record_batch *rb);
 void frt_record_batch_free(frt_record_batch *rb);
 
+/* ---- FASTQ, BCF and FASTA on the same container ---------------------------
+ * Each scanner takes a device-resident inflate batch (from the codec or the
+ * reader) and returns an frt_columns handle: device columns in the reference's
+ * order, the tail to carry into the next batch, and how the boundaries were
+ * established.  The handle keeps its inflate batch alive. */
+typedef struct frt_fastq_scanner frt_fastq_scanner;
+typedef struct frt_bcf_scanner frt_bcf_scanner;
+typedef struct frt_fasta_compactor frt_fasta_compactor;
+typedef struct frt_columns frt_columns;
+
+/* FASTQ DeviceColumns, crates/fritillaria-fastq/src/columnar/device.rs:44-72. */
+typedef enum {
+    FRT_FASTQ_COL_RECORD_OFFSETS = 0, /* u64, into the inflate batch */
+    FRT_FASTQ_COL_SEQUENCE_START = 1, /* u32, record-relative */
+    FRT_FASTQ_COL_PLUS_START = 2,     /* u32 */
+    FRT_FASTQ_COL_QUALITY_START = 3,  /* u32 */
+    FRT_FASTQ_COL_SEQUENCE_LEN = 4,   /* u32 */
+    FRT_FASTQ_COL_RECORD_END = 5,     /* u32 */
+    FRT_FASTQ_COL_COUNT = 6
+} frt_fastq_column;
+
+/* BCF DeviceColumns, crates/fritillaria-bcf/src/columnar/device.rs:68-110. */
+typedef enum {
+    FRT_BCF_COL_CHROMOSOME_ID = 0,   /* i32 */
+    FRT_BCF_COL_POSITION = 1,        /* i32, 0-based */
+    FRT_BCF_COL_REFERENCE_SPAN = 2,  /* i32 */
+    FRT_BCF_COL_QUALITY = 3,         /* u32, raw float bits */
+    FRT_BCF_COL_INFO_COUNT = 4,      /* u16 */
+    FRT_BCF_COL_ALLELE_COUNT = 5,    /* u16 */
+    FRT_BCF_COL_SAMPLE_COUNT = 6,    /* u32 */
+    FRT_BCF_COL_FORMAT_COUNT = 7,    /* u8 */
+    FRT_BCF_COL_RECORD_OFFSETS = 8,  /* u64 */
+    FRT_BCF_COL_ALLELES_START = 9,   /* u32, record-relative */
+    FRT_BCF_COL_FILTERS_START = 10,  /* u32 */
+    FRT_BCF_COL_INFO_START = 11,     /* u32 */
+    FRT_BCF_COL_GENOTYPES_START = 12, /* u32 */
+    FRT_BCF_COL_RECORD_END = 13,     /* u32 */
+    FRT_BCF_COL_COUNT = 14
+} frt_bcf_column;
+
+/* FASTA DeviceColumns, crates/fritillaria-fasta/src/columnar/device.rs. */
+typedef enum {
+    FRT_FASTA_COL_SEQUENCE = 0,         /* u8, every contig's bases, newlines removed */
+    FRT_FASTA_COL_SEQUENCE_OFFSETS = 1, /* u64, where each contig starts in SEQUENCE */
+    FRT_FASTA_COL_SEQUENCE_LENGTHS = 2, /* u64 */
+    FRT_FASTA_COL_RECORD_OFFSETS = 3,   /* u64, the '>' of each contig in the batch */
+    FRT_FASTA_COL_COUNT = 4
+} frt_fasta_column;
+
+/* FastqScanner::new / with_context, crates/fritillaria-cuda/src/fastq.rs:53-84. */
+int frt_fastq_scanner_create(int device, void *stream, frt_fastq_scanner **out, frt_error *err);
+void frt_fastq_scanner_destroy(frt_fastq_scanner *s);
+/* FastqScanner::decode(batch, start) (fastq.rs:117-140; scan, fastq.rs:94-110,
+ * is the same call with the scan info read from the handle). */
+int frt_fastq_decode(frt_fastq_scanner *s, const frt_inflate_batch *batch, uint64_t start, frt_columns **out,
+                     frt_error *err);
+
+/* parse_header, crates/fritillaria-bcf/src/columnar/header.rs:111-160: where
+ * records start, the sample count and the contig count the scan needs. */
+int frt_bcf_parse_header(const uint8_t *buf, size_t len, uint64_t *records_start, uint32_t *samples,
+                         uint32_t *contigs, frt_error *err);
+/* BcfScanner::new / with_context, crates/fritillaria-cuda/src/bcf.rs:46-80. */
+int frt_bcf_scanner_create(int device, void *stream, frt_bcf_scanner **out, frt_error *err);
+void frt_bcf_scanner_destroy(frt_bcf_scanner *s);
+/* BcfScanner::decode(batch, start, samples, contigs) (bcf.rs:125-150). */
+int frt_bcf_decode(frt_bcf_scanner *s, const frt_inflate_batch *batch, uint64_t start, uint32_t samples,
+                   uint32_t contigs, frt_columns **out, frt_error *err);
+
+/* FastaCompactor::new / with_context and compact(batch),
+ * crates/fritillaria-cuda/src/fasta.rs:40-80.  The batch holds a whole FASTA. */
+int frt_fasta_compactor_create(int device, void *stream, frt_fasta_compactor **out, frt_error *err);
+void frt_fasta_compactor_destroy(frt_fasta_compactor *s);
+int frt_fasta_compact(frt_fasta_compactor *s, const frt_inflate_batch *batch, frt_columns **out, frt_error *err);
+
+/* DeviceRecordBatch / DeviceReference accessors. */
+uint64_t frt_columns_len(const frt_columns *c);         /* records (contigs for FASTA) */
+uint64_t frt_columns_tail(const frt_columns *c);        /* FASTQ/BCF: carry point */
+uint64_t frt_columns_total_bases(const frt_columns *c); /* FASTA: bases in SEQUENCE */
+int frt_columns_count(const frt_columns *c);            /* columns of this format */
+int frt_columns_device_ordinal(const frt_columns *c);
+/* SpeculativeScan's proof (0 tiled, 1 walked), survivors and validated
+ * (crates/fritillaria-fastq/src/columnar/speculative.rs:62-90,
+ * crates/fritillaria-bcf/src/columnar/speculative.rs). */
+void frt_columns_scan_info(const frt_columns *c, uint64_t *proof, uint64_t *survivors, uint64_t *validated);
+int frt_columns_column(const frt_columns *c, int column, void **ptr, size_t *bytes, size_t *width);
+int frt_columns_column_to_host(const frt_columns *c, int column, void *dst, size_t cap, frt_error *err);
+void *frt_columns_ready_event(const frt_columns *c);
+void frt_columns_free(frt_columns *c);
+
 /* ---- batched, device-resident form ---------------------------------------
  * No reference counterpart: the batched launch model.  Members of a whole
  * BGZF file resident in device memory are discovered, inflated, verified,

@@ -29,10 +29,10 @@ def _run(cmd):
 
 
 def build_oracle() -> Path:
-    src = [HERE / "frt_oracle.c", HERE / "frt_oracle.h"]
-    if _newer(ORACLE_LIB, src):
-        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-o", str(ORACLE_LIB), str(HERE / "frt_oracle.c"),
-              "-lz", "-pthread"])
+    c_files = [HERE / "frt_oracle.c", HERE / "frt_oracle_formats.c"]
+    if _newer(ORACLE_LIB, c_files + [HERE / "frt_oracle.h"]):
+        _run(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-fPIC", "-shared", "-o", str(ORACLE_LIB),
+              *map(str, c_files), "-lz", "-pthread"])
     return ORACLE_LIB
 
 
@@ -42,7 +42,8 @@ def build_ref() -> Path | None:
         return None
     REF_DIR.mkdir(exist_ok=True)
     deps = [HERE / "ref_driver.cpp", HERE / "ref_shim.h"] + [REFERENCE_KERNELS / f for f in
-                                                            ("inflate.cu", "crc32.cu", "bam_decode.cu")]
+                                                            ("inflate.cu", "crc32.cu", "bam_decode.cu", "fastq_scan.cu", "bcf_scan.cu",
+                                                             "fasta_compact.cu")]
     if _newer(REF_LIB, deps):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-w", f"-I{HERE}", f"-I{REFERENCE_KERNELS}",
               "-o", str(REF_LIB), str(HERE / "ref_driver.cpp")])

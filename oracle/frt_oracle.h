@@ -125,6 +125,62 @@ typedef struct {
 int orc_baseline_bam(const uint8_t *file, size_t len, int threads, uint64_t max_members,
                      orc_baseline_result *res);
 
+/* ---- FASTQ, BCF, FASTA (frt_oracle_formats.c) ---------------------------- */
+
+enum { ORC_PROOF_TILED = 0, ORC_PROOF_WALKED = 1 };
+
+typedef struct {
+    uint32_t sequence_start, plus_start, quality_start, sequence_len, record_end;
+} orc_fastq_bounds;
+
+int orc_fastq_bounds_at(const uint8_t *buf, uint64_t len, uint64_t pos, orc_fastq_bounds *b);
+int orc_fastq_scan(const uint8_t *buf, uint64_t len, uint64_t start, uint64_t *offsets, size_t cap,
+                   size_t *n, uint64_t *tail, uint64_t *survivors, int *proof);
+int orc_fastq_decode(const uint8_t *buf, uint64_t len, const uint64_t *offsets, size_t n,
+                     uint32_t *sequence_start, uint32_t *plus_start, uint32_t *quality_start,
+                     uint32_t *sequence_len, uint32_t *record_end);
+
+typedef struct {
+    int32_t *chromosome_id;
+    int32_t *position;
+    int32_t *reference_span;
+    uint32_t *quality;
+    uint16_t *info_count;
+    uint16_t *allele_count;
+    uint32_t *sample_count;
+    uint8_t *format_count;
+    uint32_t *alleles_start;
+    uint32_t *filters_start;
+    uint32_t *info_start;
+    uint32_t *genotypes_start;
+    uint32_t *record_end;
+} orc_bcf_columns;
+
+int orc_bcf_header(const uint8_t *buf, uint64_t len, uint64_t *records_start, uint32_t *samples,
+                   uint32_t *contigs, orc_error *err);
+int orc_bcf_looks_like_a_record(const uint8_t *buf, uint64_t len, uint64_t pos, uint32_t samples,
+                                uint32_t contigs);
+int orc_bcf_validate(const uint8_t *buf, uint64_t len, uint64_t pos);
+int orc_bcf_scan(const uint8_t *buf, uint64_t len, uint64_t start, uint32_t samples, uint32_t contigs,
+                 uint64_t *offsets, size_t cap, size_t *n, uint64_t *tail, uint64_t *sieved,
+                 uint64_t *validated, int *proof);
+int orc_bcf_decode(const uint8_t *buf, uint64_t len, const uint64_t *offsets, size_t n,
+                   const orc_bcf_columns *cols);
+
+typedef struct {
+    uint32_t sequence_start;
+    uint32_t line_bases;
+    uint32_t line_width;
+    uint8_t uniform;
+    uint64_t sequence_len;
+    uint64_t record_end;
+} orc_fasta_bounds;
+
+int orc_fasta_bounds_at(const uint8_t *buf, uint64_t len, uint64_t pos, orc_fasta_bounds *b);
+int orc_fasta_compact(const uint8_t *buf, uint64_t len, uint8_t *seq, uint64_t seq_cap,
+                      uint64_t *seq_offsets, uint64_t *seq_lengths, uint64_t *record_offsets,
+                      orc_fasta_bounds *bounds, size_t cap, size_t *n, uint64_t *total);
+
 #ifdef __cplusplus
 }
 #endif

@@ -53,6 +53,13 @@ def lib():
         _lib.orc_bam_decode.argtypes = [_P, _P, C.c_size_t, _P]
         _lib.orc_bam_aux.argtypes = [_P, C.c_uint32, C.c_uint32, _P, C.c_uint32, _P]
         _lib.orc_baseline_bam.argtypes = [_P, C.c_size_t, C.c_int, C.c_uint64, _P]
+        _lib.orc_fastq_scan.argtypes = [_P, C.c_uint64, C.c_uint64, _P, C.c_size_t, _P, _P, _P, _P]
+        _lib.orc_fastq_decode.argtypes = [_P, C.c_uint64, _P, C.c_size_t, _P, _P, _P, _P, _P]
+        _lib.orc_bcf_header.argtypes = [_P, C.c_uint64, _P, _P, _P, _P]
+        _lib.orc_bcf_scan.argtypes = [_P, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, _P, C.c_size_t, _P, _P,
+                                      _P, _P, _P]
+        _lib.orc_bcf_decode.argtypes = [_P, C.c_uint64, _P, C.c_size_t, _P]
+        _lib.orc_fasta_compact.argtypes = [_P, C.c_uint64, _P, C.c_uint64, _P, _P, _P, _P, C.c_size_t, _P, _P]
     return _lib
 
 
@@ -240,3 +247,107 @@ def baseline_bam(bgzf, threads: int, max_members: int = 0):
     res = OrcBaseline()
     lib().orc_baseline_bam(_ptr(b), b.size, threads, max_members, C.byref(res))
     return res
+
+
+# ---- FASTQ, BCF, FASTA (frt_oracle_formats.c) ------------------------------
+
+TILED, WALKED = 0, 1
+
+FASTQ_COLUMNS = [("sequence_start", np.uint32), ("plus_start", np.uint32), ("quality_start", np.uint32),
+                 ("sequence_len", np.uint32), ("record_end", np.uint32)]
+
+
+def fastq_scan(buf, start: int = 0):
+    """FastqScanner::scan semantics: (offsets, tail, survivors, proof)."""
+    b = _buf(buf)
+    cap = b.size // 4 + 1
+    offs = np.zeros(cap, dtype=np.uint64)
+    n, tail, surv, proof = C.c_size_t(), C.c_uint64(), C.c_uint64(), C.c_int()
+    rc = lib().orc_fastq_scan(_ptr(b), b.size, start, _ptr(offs), cap, C.byref(n), C.byref(tail), C.byref(surv),
+                              C.byref(proof))
+    if rc:
+        raise RuntimeError(f"orc_fastq_scan: {rc}")
+    return offs[: n.value].copy(), tail.value, surv.value, proof.value
+
+
+def fastq_decode(buf, start: int = 0) -> dict:
+    """Offsets, tail and the five line-bound columns of FastqScanner::decode."""
+    b = _buf(buf)
+    offs, tail, surv, proof = fastq_scan(b, start)
+    cols = {name: np.zeros(len(offs), dtype=dt) for name, dt in FASTQ_COLUMNS}
+    errors = lib().orc_fastq_decode(_ptr(b), b.size, _ptr(offs), len(offs),
+                                    *[_ptr(cols[name]) for name, _ in FASTQ_COLUMNS])
+    if errors:
+        raise RuntimeError(f"{errors} FASTQ records failed to decode")
+    cols["record_offsets"] = offs
+    return {"columns": cols, "tail": tail, "survivors": surv, "proof": proof}
+
+
+BCF_COLUMNS = [("chromosome_id", np.int32), ("position", np.int32), ("reference_span", np.int32),
+               ("quality", np.uint32), ("info_count", np.uint16), ("allele_count", np.uint16),
+               ("sample_count", np.uint32), ("format_count", np.uint8), ("alleles_start", np.uint32),
+               ("filters_start", np.uint32), ("info_start", np.uint32), ("genotypes_start", np.uint32),
+               ("record_end", np.uint32)]
+
+
+def bcf_header(buf):
+    """(records_start, samples, contigs) of a BCF header (header.rs:111-160)."""
+    b = _buf(buf)
+    rs, ns, nc = C.c_uint64(), C.c_uint32(), C.c_uint32()
+    err = OrcError()
+    rc = lib().orc_bcf_header(_ptr(b), b.size, C.byref(rs), C.byref(ns), C.byref(nc), C.byref(err))
+    if rc:
+        raise OracleError(err)
+    return rs.value, ns.value, nc.value
+
+
+def bcf_scan(buf, start: int, samples: int, contigs: int):
+    """BcfScanner::scan semantics: (offsets, tail, sieved, validated, proof)."""
+    b = _buf(buf)
+    cap = b.size // 32 + 1
+    offs = np.zeros(cap, dtype=np.uint64)
+    n, tail, sv, va, proof = C.c_size_t(), C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_int()
+    rc = lib().orc_bcf_scan(_ptr(b), b.size, start, samples, contigs, _ptr(offs), cap, C.byref(n), C.byref(tail),
+                            C.byref(sv), C.byref(va), C.byref(proof))
+    if rc:
+        raise RuntimeError(f"orc_bcf_scan: {rc}")
+    return offs[: n.value].copy(), tail.value, sv.value, va.value, proof.value
+
+
+def bcf_decode(buf, start: int, samples: int, contigs: int) -> dict:
+    """Offsets, tail and the site-core columns of BcfScanner::decode."""
+    b = _buf(buf)
+    offs, tail, sv, va, proof = bcf_scan(b, start, samples, contigs)
+    cols = {name: np.zeros(len(offs), dtype=dt) for name, dt in BCF_COLUMNS}
+    ptrs = (C.c_void_p * len(BCF_COLUMNS))(*[_ptr(cols[name]) for name, _ in BCF_COLUMNS])
+    errors = lib().orc_bcf_decode(_ptr(b), b.size, _ptr(offs), len(offs), C.byref(ptrs))
+    if errors:
+        raise RuntimeError(f"{errors} BCF records failed to decode")
+    cols["record_offsets"] = offs
+    return {"columns": cols, "tail": tail, "sieved": sv, "validated": va, "proof": proof}
+
+
+FASTA_BOUNDS_DTYPE = np.dtype([("sequence_start", "<u4"), ("line_bases", "<u4"), ("line_width", "<u4"),
+                               ("uniform", "u1"), ("sequence_len", "<u8"), ("record_end", "<u8")], align=True)
+
+
+def fasta_compact(buf) -> dict:
+    """FastaCompactor::compact semantics: the bases of every contig without
+    newlines, plus per-contig offsets, lengths, record offsets and layout."""
+    b = _buf(buf)
+    cap = b.size // 2 + 1
+    so, sl, ro = (np.zeros(cap, dtype=np.uint64) for _ in range(3))
+    bounds = np.zeros(cap, dtype=FASTA_BOUNDS_DTYPE)
+    n, total = C.c_size_t(), C.c_uint64()
+    rc = lib().orc_fasta_compact(_ptr(b), b.size, None, 0, _ptr(so), _ptr(sl), _ptr(ro), _ptr(bounds), cap,
+                                 C.byref(n), C.byref(total))
+    if rc:
+        raise RuntimeError(f"orc_fasta_compact: {rc}")
+    seq = np.zeros(total.value + 1, dtype=np.uint8)
+    rc = lib().orc_fasta_compact(_ptr(b), b.size, _ptr(seq), seq.size, _ptr(so), _ptr(sl), _ptr(ro), _ptr(bounds),
+                                 cap, C.byref(n), C.byref(total))
+    if rc:
+        raise RuntimeError(f"orc_fasta_compact: {rc}")
+    k = n.value
+    return {"sequence": seq[: total.value], "sequence_offsets": so[:k].copy(), "sequence_lengths": sl[:k].copy(),
+            "record_offsets": ro[:k].copy(), "bounds": bounds[:k].copy()}

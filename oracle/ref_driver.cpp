@@ -7,7 +7,9 @@
  * present; never shipped.
  */
 #include <cstdint>
+#include <algorithm>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #include "ref_shim.h"
@@ -23,6 +25,30 @@ namespace ref_crc {
 namespace ref_bam {
 #include "bam_decode.cu"
 }
+namespace ref_fastq {
+#include "fastq_scan.cu"
+}
+namespace ref_bcf {
+#include "bcf_scan.cu"
+}
+namespace ref_fasta {
+#include "fasta_compact.cu"
+}
+
+namespace {
+
+/* One "thread" per index, as a grid of single-thread blocks. */
+template <class F> void for_threads(unsigned long long n, F &&f)
+{
+    blockDim.x = 1;
+    threadIdx.x = 0;
+    for (unsigned long long i = 0; i < n; ++i) {
+        blockIdx.x = (unsigned)i;
+        f();
+    }
+}
+
+} // namespace
 
 extern "C" {
 
@@ -87,6 +113,210 @@ int ref_bam_decode(const unsigned char *buf, unsigned long long len, const unsig
                                    tlen, cigar_start, seq_start, qual_start, aux_start, record_end);
     }
     return 0;
+}
+
+/* FastqScanner::run + decode (crates/fritillaria-cuda/src/fastq.rs:486-560)
+ * around the reference's fastq_sieve / fastq_decode / fastq_walk kernels,
+ * with the launcher's capacity rule (len / 64, at least 1024).  Returns 0, or
+ * 1 when decode reported failures, 2 when the walk overflowed. */
+int ref_fastq_run(const unsigned char *buf, unsigned long long len, unsigned long long start,
+                  unsigned long long *offsets, unsigned long long cap, unsigned long long *n_out,
+                  unsigned long long *tail_out, unsigned long long *survivors_out, int *proof_out,
+                  unsigned int *seq_start, unsigned int *plus_start, unsigned int *qual_start,
+                  unsigned int *seq_len, unsigned int *rec_end)
+{
+    *n_out = 0;
+    *survivors_out = 0;
+    *proof_out = 0;
+    if (start >= len) {
+        *tail_out = start < len ? start : len;
+        return 0;
+    }
+    unsigned long long capacity = len / 64 > 1024 ? len / 64 : 1024;
+    std::vector<unsigned long long> sieved(capacity);
+    unsigned int count = 0, overflow = 0;
+    unsigned long long anchor = 0;
+    unsigned long long span = len - start;
+    /* thread i covers byte start + i; blockIdx carries the high part */
+    blockDim.x = 256;
+    for (unsigned long long i = 0; i < span; ++i) {
+        blockIdx.x = (unsigned)(i / 256);
+        threadIdx.x = (unsigned)(i % 256);
+        ref_fastq::fastq_sieve(buf, len, start, sieved.data(), &count, (unsigned)capacity, &overflow, &anchor);
+    }
+    std::vector<unsigned long long> offs;
+    bool ok = overflow == 0;
+    if (ok) {
+        offs.assign(sieved.begin(), sieved.begin() + count);
+        std::sort(offs.begin(), offs.end());
+    }
+    *survivors_out = ok ? offs.size() : 0;
+    unsigned int errors = 0;
+    auto decode = [&](const std::vector<unsigned long long> &o) {
+        for_threads(o.size(), [&] {
+            ref_fastq::fastq_decode(buf, len, o.data(), (unsigned)o.size(), seq_start, plus_start, qual_start,
+                                    seq_len, rec_end, &errors);
+        });
+    };
+    if (ok && !offs.empty() && offs[0] == anchor && offs.size() <= cap) {
+        decode(offs);
+        if (errors) return 1; /* decode_offsets fails the call (fastq.rs:395-402) */
+        unsigned long long at = anchor;
+        bool tiled = true;
+        for (size_t k = 0; k < offs.size() && tiled; ++k) {
+            unsigned long long next = at + rec_end[k];
+            if (offs[k] != at || next <= at || next > len) tiled = false;
+            else at = next;
+        }
+        if (tiled) {
+            std::copy(offs.begin(), offs.end(), offsets);
+            *n_out = offs.size();
+            *tail_out = at;
+            return 0;
+        }
+    }
+    *proof_out = 1;
+    std::vector<unsigned long long> walked(capacity);
+    unsigned int wn = 0, wover = 0;
+    unsigned long long tail = 0;
+    blockIdx.x = 0;
+    threadIdx.x = 0;
+    blockDim.x = 1;
+    ref_fastq::fastq_walk(buf, len, start, walked.data(), &wn, (unsigned)capacity, &wover, &tail);
+    if (wover || wn > cap) return 2;
+    walked.resize(wn);
+    decode(walked);
+    std::copy(walked.begin(), walked.end(), offsets);
+    *n_out = wn;
+    *tail_out = tail;
+    return errors ? 1 : 0;
+}
+
+/* BcfScanner::scan (crates/fritillaria-cuda/src/bcf.rs:280-372) around
+ * bcf_sieve / bcf_validate / bcf_probe_tail / bcf_walk, with the launcher's
+ * capacity rule.  Returns 0, or 2 when the walk overflowed. */
+int ref_bcf_scan(const unsigned char *buf, unsigned long long len, unsigned long long start, unsigned int samples,
+                 unsigned int contigs, unsigned long long *offsets, unsigned long long cap,
+                 unsigned long long *n_out, unsigned long long *tail_out, unsigned long long *sieved_out,
+                 unsigned long long *validated_out, int *proof_out)
+{
+    *n_out = 0;
+    *sieved_out = *validated_out = 0;
+    *proof_out = 0;
+    if (start >= len) {
+        *tail_out = start < len ? start : len;
+        return 0;
+    }
+    unsigned long long capacity = len / 64 > 1024 ? len / 64 : 1024;
+    std::vector<unsigned long long> sv(capacity), se(capacity);
+    unsigned int ns = 0, overflow = 0;
+    unsigned long long span = len - start;
+    blockDim.x = 256;
+    for (unsigned long long i = 0; i < span; ++i) {
+        blockIdx.x = (unsigned)(i / 256);
+        threadIdx.x = (unsigned)(i % 256);
+        ref_bcf::bcf_sieve(buf, len, start, samples, contigs, sv.data(), se.data(), &ns, (unsigned)capacity,
+                           &overflow);
+    }
+    *sieved_out = ns;
+    bool walk = overflow != 0 || ns > capacity;
+    if (!walk) {
+        std::vector<unsigned long long> vv(capacity), ve(capacity);
+        unsigned int nv = 0;
+        for_threads(ns, [&] {
+            ref_bcf::bcf_validate(buf, len, sv.data(), se.data(), ns, vv.data(), ve.data(), &nv);
+        });
+        *validated_out = nv;
+        std::vector<std::pair<unsigned long long, unsigned long long>> pairs;
+        for (unsigned int k = 0; k < nv; ++k) pairs.emplace_back(vv[k], ve[k]);
+        std::sort(pairs.begin(), pairs.end());
+        unsigned long long at = start;
+        bool tiled = true;
+        for (auto &pe : pairs) {
+            if (pe.first != at || pe.second > len || pe.second <= pe.first) {
+                tiled = false;
+                break;
+            }
+            at = pe.second;
+        }
+        if (tiled) {
+            unsigned int whole = 0;
+            blockIdx.x = 0;
+            threadIdx.x = 0;
+            ref_bcf::bcf_probe_tail(buf, len, at, &whole);
+            if (!whole && pairs.size() <= cap) {
+                for (size_t k = 0; k < pairs.size(); ++k) offsets[k] = pairs[k].first;
+                *n_out = pairs.size();
+                *tail_out = at;
+                return 0;
+            }
+        }
+    }
+    *proof_out = 1;
+    unsigned long long wcap = (len - start) / 32 + 1;
+    if (wcap < 1024) wcap = 1024;
+    std::vector<unsigned long long> out(wcap);
+    unsigned int wn = 0, wover = 0;
+    unsigned long long tail = 0;
+    blockIdx.x = 0;
+    threadIdx.x = 0;
+    blockDim.x = 1;
+    ref_bcf::bcf_walk(buf, len, start, out.data(), &wn, (unsigned)wcap, &wover, &tail);
+    if (wover || wn > cap) return 2;
+    std::copy(out.begin(), out.begin() + wn, offsets);
+    *n_out = wn;
+    *tail_out = tail;
+    return 0;
+}
+
+/* bcf_decode over n records; returns its error count. */
+unsigned int ref_bcf_decode(const unsigned char *buf, unsigned long long len, const unsigned long long *offsets,
+                            unsigned int n, int *chrom, int *pos, int *rlen, unsigned int *qual,
+                            unsigned short *n_info, unsigned short *n_allele, unsigned int *n_sample,
+                            unsigned char *n_fmt, unsigned int *alleles, unsigned int *filters, unsigned int *info,
+                            unsigned int *genotypes, unsigned int *end)
+{
+    unsigned int errors = 0;
+    for_threads(n, [&] {
+        ref_bcf::bcf_decode(buf, len, offsets, n, chrom, pos, rlen, qual, n_info, n_allele, n_sample, n_fmt,
+                            alleles, filters, info, genotypes, end, &errors);
+    });
+    return errors;
+}
+
+/* fasta_find_contigs (sorted, as the launcher sorts), fasta_compact_uniform
+ * and fasta_compact_scan (crates/fritillaria-cuda/kernels/fasta_compact.cu). */
+unsigned int ref_fasta_find_contigs(const unsigned char *buf, unsigned long long len, unsigned long long *out,
+                                    unsigned int cap)
+{
+    unsigned int count = 0, overflow = 0;
+    blockDim.x = 256;
+    for (unsigned long long i = 0; i < len; ++i) {
+        blockIdx.x = (unsigned)(i / 256);
+        threadIdx.x = (unsigned)(i % 256);
+        ref_fasta::fasta_find_contigs(buf, len, 0, out, &count, cap, &overflow);
+    }
+    std::sort(out, out + (count < cap ? count : cap));
+    return overflow ? 0xFFFFFFFFu : count;
+}
+
+void ref_fasta_compact_uniform(const unsigned char *src, unsigned long long span, unsigned char *dst,
+                               unsigned int line_width)
+{
+    blockDim.x = 256;
+    for (unsigned long long i = 0; i < span; ++i) {
+        blockIdx.x = (unsigned)(i / 256);
+        threadIdx.x = (unsigned)(i % 256);
+        ref_fasta::fasta_compact_uniform(src, span, dst, line_width);
+    }
+}
+
+void ref_fasta_compact_scan(const unsigned char *src, unsigned long long span, unsigned char *dst)
+{
+    blockIdx.x = 0;
+    threadIdx.x = 0;
+    blockDim.x = 1;
+    ref_fasta::fasta_compact_scan(src, span, dst);
 }
 
 } // extern "C"

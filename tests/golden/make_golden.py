@@ -2,17 +2,20 @@
 
 Inputs are seeded synthetic BGZF files (made by this package's generator and
 by Python's zlib); outputs come from the reference's own kernels --
-crates/fritillaria-cuda/kernels/inflate.cu (inflate_blocks), crc32.cu and
+crates/fritillaria-cuda/kernels/inflate.cu (inflate_blocks), crc32.cu,
 bam_decode.cu (bam_scan_blocks, bam_reconcile, bam_emit_offsets,
-bam_decode_fields) -- compiled as host code from the reference tree by
+bam_decode_fields), fastq_scan.cu, bcf_scan.cu and fasta_compact.cu -- compiled as host code from the reference tree by
 oracle/build.py into oracle/_ref/ and driven in the reference's launch order.
 So the vectors pin the oracle and the GPU path to the reference's results on
 machines that have no reference tree.
 
 Each case is one .npz holding the input bytes, the member spans, the per-member
 inflate status/produced/CRC from the reference kernel, a SHA-256 of every
-member's output, and for BAM cases the record offsets, tail and the 13
-per-record columns of DeviceColumns.
+member's output, and per format: for BAM the record offsets, tail and the 13
+per-record columns of DeviceColumns; for FASTQ (fastq_scan.cu) and BCF
+(bcf_scan.cu) the offsets, tail, proof and columns of the launchers' decode;
+for FASTA (fasta_compact.cu) the contig offsets, lengths and a SHA-256 of the
+compacted bases.
 
 Run from the repository root with the reference tree present:
     python tests/golden/make_golden.py
@@ -20,7 +23,6 @@ Run from the repository root with the reference tree present:
 
 from __future__ import annotations
 
-import ctypes as C
 import hashlib
 import struct
 import sys
@@ -34,15 +36,8 @@ ROOT = HERE.parents[1]
 sys.path.insert(0, str(ROOT))
 
 from oracle import oracle  # noqa: E402
+from oracle import ref  # noqa: E402
 from fritillaria_gb300 import synth  # noqa: E402
-
-_P = C.c_void_p
-
-REF_COLUMNS = [("ref_id", np.int32), ("pos", np.int32), ("flags", np.uint16), ("mapq", np.uint8),
-               ("seq_len", np.uint32), ("mate_ref_id", np.int32), ("mate_pos", np.int32), ("tlen", np.int32),
-               ("cigar_start", np.uint32), ("sequence_start", np.uint32), ("quality_start", np.uint32),
-               ("aux_start", np.uint32), ("record_end", np.uint32)]
-
 
 def bgzf_member(payload: bytes, level: int = 6, strategy: int = zlib.Z_DEFAULT_STRATEGY) -> bytes:
     """One BGZF member (SAM spec 4.1): gzip header with the BC extra subfield,
@@ -78,47 +73,11 @@ def deflate_cases() -> bytes:
     return b"".join(members)
 
 
-def ref_inflate(bgzf: np.ndarray, spans):
-    ref = oracle.ref_lib()
-    n = len(spans)
-    in_off = np.ascontiguousarray(spans["payload_start"], dtype=np.uint64)
-    in_len = np.ascontiguousarray(spans["payload_len"], dtype=np.uint32)
-    caps = np.ascontiguousarray(spans["isize"], dtype=np.uint32)
-    out_off = np.zeros(n + 1, dtype=np.uint64)
-    out_off[1:] = np.cumsum(caps.astype(np.uint64))
-    out = np.zeros(int(out_off[-1]) + 1, dtype=np.uint8)
-    status = np.zeros(n, np.uint32)
-    produced = np.zeros(n, np.uint32)
-    crc = np.zeros(n, np.uint32)
-    ref.ref_inflate_blocks(bgzf.ctypes.data_as(_P), in_off.ctypes.data_as(_P), in_len.ctypes.data_as(_P),
-                           out.ctypes.data_as(_P), out_off.ctypes.data_as(_P), caps.ctypes.data_as(_P),
-                           status.ctypes.data_as(_P), produced.ctypes.data_as(_P), crc.ctypes.data_as(_P), n)
-    return out[: int(out_off[-1])], out_off, status, produced, crc
-
-
-def ref_bam(data: np.ndarray, member_starts: np.ndarray, start: int):
-    ref = oracle.ref_lib()
-    cap = data.size // 36 + 1
-    offs = np.zeros(cap, np.uint64)
-    cols = {name: np.zeros(cap, dt) for name, dt in REF_COLUMNS}
-    n = C.c_ulonglong()
-    tail = C.c_ulonglong()
-    bs = np.ascontiguousarray(member_starts, dtype=np.uint64)
-    args = [data.ctypes.data_as(_P), C.c_ulonglong(data.size), bs.ctypes.data_as(_P), C.c_int(len(bs) - 1),
-            C.c_ulonglong(start), offs.ctypes.data_as(_P), C.c_ulonglong(cap), C.byref(n), C.byref(tail)]
-    args += [cols[name].ctypes.data_as(_P) for name, _ in REF_COLUMNS]
-    rc = ref.ref_bam_decode(*args)
-    if rc != 0:
-        raise RuntimeError(f"reference scan returned {rc}")
-    k = n.value
-    return offs[:k].copy(), tail.value, {name: c[:k].copy() for name, c in cols.items()}
-
-
-def make_case(name: str, bgzf: bytes, bam: bool) -> Path:
+def make_case(name: str, bgzf: bytes, kind: str) -> Path:
     b = np.frombuffer(bgzf, dtype=np.uint8).copy()
     spans, used = oracle.discover(b)
     assert used == b.size, "golden inputs hold whole members only"
-    data, out_off, status, produced, crc = ref_inflate(b, spans)
+    data, out_off, status, produced, crc = ref.inflate(b, spans)
     assert not status.any(), f"{name}: reference kernel status {status}"
     assert np.array_equal(produced, spans["isize"]), f"{name}: produced != ISIZE"
     assert np.array_equal(crc, spans["crc32"]), f"{name}: CRC mismatch"
@@ -128,31 +87,50 @@ def make_case(name: str, bgzf: bytes, bam: bool) -> Path:
            "span_payload_len": spans["payload_len"], "span_isize": spans["isize"], "span_crc32": spans["crc32"],
            "ref_status": status, "ref_produced": produced, "ref_crc": crc, "member_sha256": sha,
            "inflated_len": np.uint64(data.size)}
-    if bam:
+    if kind == "bam":
         start, n_ref = oracle.bam_header(data)
-        offs, tail, cols = ref_bam(data, out_off, start)
+        offs, tail, cols = ref.bam(data, out_off, start)
         rec.update({"records_start": np.uint64(start), "n_ref": np.int32(n_ref), "record_offsets": offs,
                     "tail": np.uint64(tail)})
         rec.update({f"col_{k}": v for k, v in cols.items()})
+    elif kind == "fastq":
+        r = ref.fastq(data, 0)
+        rec.update({"tail": np.uint64(r["tail"]), "survivors": np.uint64(r["survivors"]), "proof": np.int32(r["proof"])})
+        rec.update({f"col_{k}": v for k, v in r["columns"].items()})
+    elif kind == "bcf":
+        start, samples, contigs = oracle.bcf_header(data)
+        r = ref.bcf(data, start, samples, contigs)
+        rec.update({"records_start": np.uint64(start), "samples": np.uint32(samples), "contigs": np.uint32(contigs),
+                    "tail": np.uint64(r["tail"]), "proof": np.int32(r["proof"])})
+        rec.update({f"col_{k}": v for k, v in r["columns"].items()})
+    elif kind == "fasta":
+        r = ref.fasta_compact(data)
+        rec.update({"sequence_sha256": np.frombuffer(hashlib.sha256(r["sequence"].tobytes()).digest(), np.uint8),
+                    "total_bases": np.uint64(r["sequence"].size)})
+        rec.update({f"col_{k}": r[k] for k in ("sequence_offsets", "sequence_lengths", "record_offsets")})
     path = HERE / f"{name}.npz"
     np.savez_compressed(path, **rec)
     return path
 
 
 def main():
-    if oracle.ref_lib() is None:
+    if ref.lib() is None:
         sys.exit("the reference kernels (oracle/_ref) are not built; they need the reference tree")
     cases = [
-        ("deflate_strategies", deflate_cases(), False),
+        ("deflate_strategies", deflate_cases(), "inflate"),
         ("bam_short_full", synth.short_read_bam(1200, n_contigs=3, genome_len=2_000_000, seed=101, levels=(1, 6),
-                                                member_payload=16000)[1].tobytes(), True),
+                                                member_payload=16000)[1].tobytes(), "bam"),
         ("bam_short_record_stored", synth.short_read_bam(400, n_contigs=2, genome_len=1_000_000, seed=102,
-                                                         levels=(0, 9), packing="record")[1].tobytes(), True),
+                                                         levels=(0, 9), packing="record")[1].tobytes(), "bam"),
         ("bam_ultra_long", synth.ultra_long_bam(3, 0, seed=103, levels=(6, 6),
-                                                member_payload=8000)[1].tobytes(), True),
+                                                member_payload=8000)[1].tobytes(), "bam"),
+        ("fastq_illumina", synth.fastq(500, seed=104, levels=(1, 6), member_payload=20000)[1].tobytes(), "fastq"),
+        ("fastq_ultra_long", synth.fastq(2, kind="ont", seed=105, member_payload=9000)[1].tobytes(), "fastq"),
+        ("bcf_sites", synth.bcf(500, n_samples=16, seed=106, member_payload=12000)[1].tobytes(), "bcf"),
+        ("fasta_wrapped", synth.fasta(3, 120_000, 60, True, seed=107)[1].tobytes(), "fasta"),
     ]
-    for name, data, bam in cases:
-        p = make_case(name, data, bam)
+    for name, data, kind in cases:
+        p = make_case(name, data, kind)
         print(f"{p.name}: {p.stat().st_size} bytes")
 
 

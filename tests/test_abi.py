@@ -94,3 +94,26 @@ def test_host_header_parse_matches_oracle(frt, case):
         frt.parse_header(data[: int(g["records_start"]) - 1])
     with pytest.raises(frt.Malformed):
         frt.parse_header(b"BAM\x02")
+
+
+@pytest.mark.parametrize("case", ["bcf_sites"])
+def test_host_bcf_header_parse_matches_oracle(frt, case):
+    g = np.load(GOLDEN / f"{case}.npz")
+    data, _ = oracle.inflate_batch(g["bgzf"], oracle.discover(g["bgzf"])[0])
+    want = oracle.bcf_header(data)
+    assert frt.parse_bcf_header(data) == want == (int(g["records_start"]), int(g["samples"]), int(g["contigs"]))
+    for cut in (4, 8, int(g["records_start"]) - 1):
+        with pytest.raises(frt.Malformed):
+            frt.parse_bcf_header(data[:cut])
+    bad = data.copy()
+    bad[3] = 3
+    with pytest.raises(frt.Malformed):
+        frt.parse_bcf_header(bad)
+
+
+def test_format_scanners_refuse_without_a_gpu(frt):
+    if frt.cuda_is_usable():
+        pytest.skip("a GPU is present")
+    for cls in (frt.FastqScanner, frt.BcfScanner, frt.FastaCompactor):
+        with pytest.raises(frt.CudaUnavailable):
+            cls(0)
