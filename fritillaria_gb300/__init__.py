@@ -230,6 +230,11 @@ def lib():
         "frt_engine_stream": (_P, [_P]),
         "frt_engine_time_stages": (C.c_int, [_P, _P, C.c_int, _P]),
         "frt_engine_launches": (C.c_uint64, [_P]),
+        "frt_engine_bind_files": (C.c_int, [_P, _P, C.c_size_t, _P, C.c_size_t, _P]),
+        "frt_engine_file_count": (C.c_size_t, [_P]),
+        "frt_engine_get_file_info": (C.c_int, [_P, C.c_size_t, _P]),
+        "frt_engine_file_bam": (_P, [_P, C.c_size_t]),
+        "frt_engine_file_columns": (_P, [_P, C.c_size_t]),
         "frt_fastq_scanner_create": (C.c_int, [C.c_int, _P, _P, _P]),
         "frt_fastq_scanner_destroy": (None, [_P]),
         "frt_fastq_decode": (C.c_int, [_P, _P, C.c_uint64, _P, _P]),
@@ -557,8 +562,9 @@ def bam_scan_noalloc(data_ptr: int, length: int, member_offsets_ptr: int, n_memb
 class DeviceRecordBatch:
     """DeviceRecordBatch: device columns; keeps its inflate batch alive."""
 
-    def __init__(self, handle):
+    def __init__(self, handle, owned: bool = True):
         self._h = handle
+        self._owned = owned
 
     def __len__(self):
         return lib().frt_record_batch_len(self._h)
@@ -595,7 +601,7 @@ class DeviceRecordBatch:
         return {name: self.column(name) for name in BAM_COLUMNS}
 
     def free(self):
-        if self._h and _lib is not None:
+        if self._h and self._owned and _lib is not None:
             _lib.frt_record_batch_free(self._h)
         self._h = None
 
@@ -639,9 +645,10 @@ class ColumnBatch:
     """Device columns of a FASTQ or BCF batch, or a compacted FASTA reference
     (DeviceRecordBatch / DeviceReference); keeps its inflate batch alive."""
 
-    def __init__(self, handle, columns: dict):
+    def __init__(self, handle, columns: dict, owned: bool = True):
         self._h = handle
         self._cols = columns
+        self._owned = owned
 
     def __len__(self):
         return lib().frt_columns_len(self._h)
@@ -681,7 +688,7 @@ class ColumnBatch:
         return {name: self.column(name) for name in self._cols}
 
     def free(self):
-        if self._h and _lib is not None:
+        if self._h and self._owned and _lib is not None:
             _lib.frt_columns_free(self._h)
         self._h = None
 
@@ -762,10 +769,30 @@ class FastaCompactor(_Scanner):
         return ColumnBatch(out, FASTA_COLUMNS)
 
 
+class Format(enum.IntEnum):
+    """File formats of a multi-file engine bind (frt_format)."""
+    BAM = 0
+    BCF = 1
+    FASTQ = 2
+    FASTA = 3
+
+
+class EngineFile(C.Structure):
+    _fields_ = [("offset", C.c_uint64), ("length", C.c_uint64), ("format", C.c_int32)]
+
+
+class EngineFileInfo(C.Structure):
+    _fields_ = [("format", C.c_int32), ("members", C.c_uint64), ("compressed_bytes", C.c_uint64),
+                ("inflated_offset", C.c_uint64), ("inflated_bytes", C.c_uint64), ("records", C.c_uint64),
+                ("tail", C.c_uint64), ("proof", C.c_uint64)]
+
+
 class BatchEngine:
     """The batched form: a whole BGZF BAM resident on the device, inflated,
     verified, scanned and decoded by persistent kernels fed from a device work
-    queue, the steady state replayed as a CUDA graph."""
+    queue, the steady state replayed as a CUDA graph.  bind_files() takes
+    several BGZF files of different formats laid out back to back: one inflate
+    over all their members, then each file's decoder."""
 
     def __init__(self, device: int = 0, stream: int | None = None, warps_per_cta: int = 0, queue_chunk: int = 0,
                  use_graph: bool = True, sort_queue: bool = True):
@@ -778,6 +805,30 @@ class BatchEngine:
     def bind_bam(self, dev_ptr: int, length: int) -> None:
         err = _Err()
         _raise(lib().frt_engine_bind_bam(self._h, dev_ptr, length, C.byref(err)), err)
+
+    def bind_files(self, dev_ptr: int, length: int, files) -> None:
+        """files: (offset, length, Format) for each file, back to back."""
+        arr = (EngineFile * len(files))(*[EngineFile(int(o), int(n), int(f)) for o, n, f in files])
+        err = _Err()
+        _raise(lib().frt_engine_bind_files(self._h, dev_ptr, length, arr, len(files), C.byref(err)), err)
+
+    def file_count(self) -> int:
+        return int(lib().frt_engine_file_count(self._h))
+
+    def file_info(self, i: int) -> EngineFileInfo:
+        info = EngineFileInfo()
+        if lib().frt_engine_get_file_info(self._h, i, C.byref(info)):
+            raise InvalidArgument(message=f"no file {i}")
+        return info
+
+    def file_result(self, i: int):
+        """The last run's result for file i: a DeviceRecordBatch (BAM) or a
+        ColumnBatch (BCF, FASTQ, FASTA), owned by the engine."""
+        fmt = Format(self.file_info(i).format)
+        if fmt == Format.BAM:
+            return DeviceRecordBatch(lib().frt_engine_file_bam(self._h, i), owned=False)
+        cols = {Format.BCF: BCF_COLUMNS, Format.FASTQ: FASTQ_COLUMNS, Format.FASTA: FASTA_COLUMNS}[fmt]
+        return ColumnBatch(lib().frt_engine_file_columns(self._h, i), cols, owned=False)
 
     def run(self) -> None:
         err = _Err()

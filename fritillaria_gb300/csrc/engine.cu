@@ -414,6 +414,26 @@ struct frt_engine {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     EngineDevState host_state{};
+    // several files: one inflate over all members, then each file's decoder
+    struct File {
+        frt_engine_file desc{};
+        u64 m0 = 0, m1 = 0;     // member range
+        u64 out0 = 0, out1 = 0; // inflated range
+        u64 records_start = 0;
+        int32_t n_ref = -1;
+        uint32_t samples = 0, contigs = 0;
+        frt_inflate_batch *view = nullptr;
+        frt_record_batch *bam = nullptr;
+        frt_columns *cols = nullptr;
+    };
+    bool multi = false;
+    std::vector<File> files;
+    frt_bam_decoder *bam_dec = nullptr;
+    frt_fastq_scanner *fastq = nullptr;
+    frt_bcf_scanner *bcf = nullptr;
+    frt_fasta_compactor *fasta = nullptr;
+    int decode_rc = FRT_OK;
+    frt_error decode_err{};
 };
 
 namespace {
@@ -428,8 +448,23 @@ template <typename T> int ealloc(frt_engine *e, T **p, size_t n, frt_error *err)
     return FRT_OK;
 }
 
+void release_results(frt_engine *e)
+{
+    for (auto &f : e->files) {
+        if (f.bam) frt_record_batch_free(f.bam);
+        if (f.cols) frt_columns_free(f.cols);
+        f.bam = nullptr;
+        f.cols = nullptr;
+    }
+}
+
 void free_all(frt_engine *e)
 {
+    release_results(e);
+    for (auto &f : e->files)
+        if (f.view) batch_release(f.view);
+    e->files.clear();
+    e->multi = false;
     if (e->exec) cudaGraphExecDestroy(e->exec);
     if (e->graph) cudaGraphDestroy(e->graph);
     e->exec = nullptr;
@@ -639,13 +674,18 @@ extern "C" void frt_engine_destroy(frt_engine *e)
     if (!e) return;
     DeviceGuardLite g(e->device);
     free_all(e);
+    frt_bam_decoder_destroy(e->bam_dec);
+    frt_fastq_scanner_destroy(e->fastq);
+    frt_bcf_scanner_destroy(e->bcf);
+    frt_fasta_compactor_destroy(e->fasta);
     stream_release(e->shared);
     delete e;
 }
 
-extern "C" int frt_engine_bind_bam(frt_engine *e, const uint8_t *dev_bgzf, size_t len, frt_error *err)
+// Discovery, plan, queue and one eager inflate of a bound buffer; sizes every
+// member-indexed buffer and the output.
+static int bind_front(frt_engine *e, const uint8_t *dev_bgzf, size_t len, frt_error *err)
 {
-    DeviceGuardLite g(e->device);
     free_all(e);
     e->in = dev_bgzf;
     e->len = len;
@@ -701,6 +741,18 @@ extern "C" int frt_engine_bind_bam(frt_engine *e, const uint8_t *dev_bgzf, size_
     e->out_cap = h.inflated_total;
     if ((rc = ealloc(e, &e->out, e->out_cap + 64, err))) return rc;
     if ((ce = enqueue_inflate(e)) != cudaSuccess) return cuda_fail(err, ce, "inflate");
+    return FRT_OK;
+}
+
+extern "C" int frt_engine_bind_bam(frt_engine *e, const uint8_t *dev_bgzf, size_t len, frt_error *err)
+{
+    DeviceGuardLite g(e->device);
+    int rc = bind_front(e, dev_bgzf, len, err);
+    if (rc) return rc;
+    cudaStream_t s = e->stream;
+    cudaError_t ce;
+    u64 n = e->n_cap;
+    EngineDevState h{};
     // Record scan once to learn the record count.
     if ((rc = ealloc(e, &e->entry, n, err)) || (rc = ealloc(e, &e->land, n, err)) ||
         (rc = ealloc(e, &e->count, n, err)) || (rc = ealloc(e, &e->first, n, err)) ||
@@ -739,12 +791,237 @@ extern "C" int frt_engine_bind_bam(frt_engine *e, const uint8_t *dev_bgzf, size_
     return FRT_OK;
 }
 
+
+// ---- several files ---------------------------------------------------------
+
+namespace {
+
+// Parses a header from the start of a file's inflated range, growing the
+// host copy until the parse succeeds or the range is exhausted.
+template <typename Parse> int parse_prefix(frt_engine *e, const frt_engine::File &f, Parse parse, frt_error *err)
+{
+    u64 len = f.out1 - f.out0;
+    std::vector<uint8_t> host;
+    for (u64 take = 1u << 16;; take *= 4) {
+        u64 n = take < len ? take : len;
+        host.resize(n);
+        cudaError_t ce = cudaMemcpyAsync(host.data(), e->out + f.out0, n, cudaMemcpyDeviceToHost, e->stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+        if (ce != cudaSuccess) return cuda_fail(err, ce, "reading a header");
+        int rc = parse(host.data(), n, err);
+        if (rc == FRT_OK || rc != FRT_ERR_MALFORMED || n == len) return rc;
+    }
+}
+
+// Each file's decoder over its inflated range (the views' events order them
+// after the inflate).
+int decode_files(frt_engine *e, frt_error *err)
+{
+    release_results(e);
+    for (auto &f : e->files) {
+        cudaEventRecord(f.view->ready, e->stream);
+        int rc = FRT_OK;
+        switch (f.desc.format) {
+        case FRT_FORMAT_BAM:
+            frt_bam_decoder_set_reference_count(e->bam_dec, f.n_ref);
+            rc = frt_bam_decode(e->bam_dec, f.view, f.records_start, &f.bam, err);
+            break;
+        case FRT_FORMAT_BCF:
+            rc = frt_bcf_decode(e->bcf, f.view, f.records_start, f.samples, f.contigs, &f.cols, err);
+            break;
+        case FRT_FORMAT_FASTQ:
+            rc = frt_fastq_decode(e->fastq, f.view, 0, &f.cols, err);
+            break;
+        default:
+            rc = frt_fasta_compact(e->fasta, f.view, &f.cols, err);
+            break;
+        }
+        if (rc) return rc;
+    }
+    return FRT_OK;
+}
+
+// Inflate errors first: decoding garbage would only hide them.
+int inflate_status(frt_engine *e, frt_error *err)
+{
+    cudaMemcpyAsync(&e->host_state, e->st, sizeof(EngineDevState), cudaMemcpyDeviceToHost, e->stream);
+    cudaError_t ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "engine run");
+    EngineDevState &h = e->host_state;
+    if (h.walk_err || h.block_err != ~0ull || (h.tiling_failed && h.n_members == 0 && e->len))
+        return stats_from_state(e, nullptr, err);
+    return FRT_OK;
+}
+
+int run_multi(frt_engine *e, frt_error *err)
+{
+    cudaError_t ce;
+    if (e->exec) {
+        ce = cudaGraphLaunch(e->exec, e->stream);
+    } else {
+        enqueue_front(e);
+        ce = enqueue_inflate(e);
+    }
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "launching the engine");
+    int rc = inflate_status(e, err);
+    if (rc) return rc;
+    return decode_files(e, err);
+}
+
+} // namespace
+
+extern "C" int frt_engine_bind_files(frt_engine *e, const uint8_t *dev, size_t len, const frt_engine_file *files,
+                                     size_t n_files, frt_error *err)
+{
+    if (!e || (!files && n_files)) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    DeviceGuardLite g(e->device);
+    // the files must tile the buffer, in order
+    uint64_t at = 0;
+    for (size_t i = 0; i < n_files; ++i) {
+        if (files[i].offset != at || files[i].format < FRT_FORMAT_BAM || files[i].format > FRT_FORMAT_FASTA) {
+            set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr,
+                      "file %zu: files must lie back to back from offset 0 with a known format", i);
+            return FRT_ERR_INVALID_ARGUMENT;
+        }
+        at += files[i].length;
+    }
+    if (at != len) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "the files cover %llu of %zu bytes",
+                  (unsigned long long)at, len);
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    int rc = bind_front(e, dev, len, err);
+    if (rc) return rc;
+    cudaStream_t s = e->stream;
+    EngineDevState h{};
+    cudaMemcpyAsync(&h, e->st, sizeof h, cudaMemcpyDeviceToHost, s);
+    cudaError_t ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "inflate");
+    e->host_state = h;
+    if ((rc = stats_from_state(e, nullptr, err))) return rc;
+    const u64 n = h.n_members;
+    std::vector<uint64_t> coff(n + 1), out_off(n + 1);
+    if (n) {
+        cudaMemcpyAsync(coff.data(), e->coffset, 8 * n, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(out_off.data(), e->out_off, 8 * (n + 1), cudaMemcpyDeviceToHost, s);
+        if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(err, ce, "reading the plan");
+    }
+    coff[n] = len;
+    e->multi = true;
+    // decoders on the engine's stream
+    if (!e->bam_dec && (rc = frt_bam_decoder_create(e->device, s, &e->bam_dec, err))) return rc;
+    if (!e->fastq && (rc = frt_fastq_scanner_create(e->device, s, &e->fastq, err))) return rc;
+    if (!e->bcf && (rc = frt_bcf_scanner_create(e->device, s, &e->bcf, err))) return rc;
+    if (!e->fasta && (rc = frt_fasta_compactor_create(e->device, s, &e->fasta, err))) return rc;
+    e->files.resize(n_files);
+    for (size_t i = 0; i < n_files; ++i) {
+        auto &f = e->files[i];
+        f.desc = files[i];
+        f.m0 = (u64)(std::lower_bound(coff.begin(), coff.begin() + n, files[i].offset) - coff.begin());
+        f.m1 = (u64)(std::lower_bound(coff.begin(), coff.begin() + n, files[i].offset + files[i].length) - coff.begin());
+        if (f.m0 < n && coff[f.m0] != files[i].offset) {
+            set_error(err, FRT_ERR_INVALID_ARGUMENT, files[i].offset, 0, 0, 0, nullptr,
+                      "file %zu does not start on a BGZF member", i);
+            return FRT_ERR_INVALID_ARGUMENT;
+        }
+        f.out0 = out_off[f.m0];
+        f.out1 = out_off[f.m1];
+        // a non-owning batch over the file's inflated bytes
+        frt_inflate_batch *v = new frt_inflate_batch;
+        v->device = e->device;
+        v->stream = s;
+        v->shared = stream_retain(e->shared);
+        v->owns_data = false;
+        v->data = e->out + f.out0;
+        v->len = f.out1 - f.out0;
+        u64 k = f.m1 - f.m0;
+        v->offsets.resize(k + 1);
+        v->coffsets.resize(k);
+        for (u64 j = 0; j <= k; ++j) v->offsets[j] = out_off[f.m0 + j] - f.out0;
+        for (u64 j = 0; j < k; ++j) v->coffsets[j] = coff[f.m0 + j] - files[i].offset;
+        std::vector<uint64_t> dev_off(2 * k + 1);
+        std::copy(v->offsets.begin(), v->offsets.end(), dev_off.begin());
+        std::copy(v->coffsets.begin(), v->coffsets.end(), dev_off.begin() + k + 1);
+        cudaEventCreateWithFlags(&v->ready, cudaEventDisableTiming);
+        f.view = v;
+        if ((rc = dev_alloc((void **)&v->d_offsets, 8 * dev_off.size(), s, err))) return rc;
+        if ((ce = cudaMemcpyAsync(v->d_offsets, dev_off.data(), 8 * dev_off.size(), cudaMemcpyHostToDevice, s)) !=
+            cudaSuccess)
+            return cuda_fail(err, ce, "uploading a file's member offsets");
+        if (f.desc.format == FRT_FORMAT_BAM && v->len) {
+            rc = parse_prefix(e, f, [&](const uint8_t *b, u64 m, frt_error *er) {
+                return frt_bam_parse_header(b, m, &f.records_start, &f.n_ref, er);
+            }, err);
+        } else if (f.desc.format == FRT_FORMAT_BCF && v->len) {
+            rc = parse_prefix(e, f, [&](const uint8_t *b, u64 m, frt_error *er) {
+                return frt_bcf_parse_header(b, m, &f.records_start, &f.samples, &f.contigs, er);
+            }, err);
+        }
+        if (rc) return rc;
+    }
+    cudaStreamSynchronize(s); // the offsets uploads read from host vectors
+    if ((rc = decode_files(e, err))) return rc;
+    if (e->cfg.use_graph) {
+        ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (ce == cudaSuccess) {
+            enqueue_front(e);
+            enqueue_inflate(e);
+            ce = cudaStreamEndCapture(s, &e->graph);
+        }
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&e->exec, e->graph, 0);
+        if (ce != cudaSuccess) return cuda_fail(err, ce, "capturing the engine graph");
+    }
+    return FRT_OK;
+}
+
+extern "C" size_t frt_engine_file_count(const frt_engine *e) { return e ? e->files.size() : 0; }
+
+extern "C" int frt_engine_get_file_info(const frt_engine *e, size_t i, frt_engine_file_info *info)
+{
+    if (!e || i >= e->files.size() || !info) return FRT_ERR_INVALID_ARGUMENT;
+    const auto &f = e->files[i];
+    frt_engine_file_info o{};
+    o.format = f.desc.format;
+    o.members = f.m1 - f.m0;
+    o.compressed_bytes = f.desc.length;
+    o.inflated_offset = f.out0;
+    o.inflated_bytes = f.out1 - f.out0;
+    if (f.bam) {
+        o.records = frt_record_batch_len(f.bam);
+        o.tail = frt_record_batch_tail(f.bam);
+    } else if (f.cols) {
+        o.records = frt_columns_len(f.cols);
+        o.tail = f.desc.format == FRT_FORMAT_FASTA ? frt_columns_total_bases(f.cols) : frt_columns_tail(f.cols);
+        frt_columns_scan_info(f.cols, &o.proof, nullptr, nullptr);
+    }
+    *info = o;
+    return FRT_OK;
+}
+
+extern "C" const frt_record_batch *frt_engine_file_bam(const frt_engine *e, size_t i)
+{
+    return e && i < e->files.size() ? e->files[i].bam : nullptr;
+}
+
+extern "C" const frt_columns *frt_engine_file_columns(const frt_engine *e, size_t i)
+{
+    return e && i < e->files.size() ? e->files[i].cols : nullptr;
+}
+
 extern "C" int frt_engine_run(frt_engine *e, frt_error *err)
 {
     DeviceGuardLite g(e->device);
     if (!e->in && e->len) {
         set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "no file bound");
         return FRT_ERR_INVALID_ARGUMENT;
+    }
+    if (e->multi) {
+        e->decode_rc = run_multi(e, &e->decode_err);
+        if (e->decode_rc && err) *err = e->decode_err;
+        return e->decode_rc;
     }
     cudaError_t ce;
     if (e->exec) {
@@ -764,7 +1041,26 @@ extern "C" int frt_engine_finish(frt_engine *e, frt_engine_stats *stats, frt_err
     cudaMemcpyAsync(&e->host_state, e->st, sizeof(EngineDevState), cudaMemcpyDeviceToHost, e->stream);
     cudaError_t ce = cudaStreamSynchronize(e->stream);
     if (ce != cudaSuccess) return cuda_fail(err, ce, "engine run");
-    return stats_from_state(e, stats, err);
+    if (!e->multi) return stats_from_state(e, stats, err);
+    // several files: the inflate's own errors, then the decoders'
+    frt_engine_stats out{};
+    int rc = stats_from_state(e, &out, err);
+    out.records = out.tail = out.aux_fields = out.fallbacks = 0;
+    for (auto &f : e->files) {
+        if (f.bam) {
+            out.records += frt_record_batch_len(f.bam);
+            out.aux_fields += frt_record_batch_aux_fields(f.bam);
+        } else if (f.cols) {
+            out.records += frt_columns_len(f.cols);
+        }
+    }
+    if (!rc && e->decode_rc) {
+        rc = e->decode_rc;
+        if (err) *err = e->decode_err;
+    }
+    out.status = rc;
+    if (stats) *stats = out;
+    return rc;
 }
 
 extern "C" int frt_engine_run_host(frt_engine *e, const uint8_t *host, size_t len, frt_engine_stats *stats,
@@ -840,7 +1136,15 @@ extern "C" int frt_engine_time_stages(frt_engine *e, float *ms, int repeats, frt
         cudaEventRecord(ev[1], e->stream);
         enqueue_inflate(e);
         cudaEventRecord(ev[2], e->stream);
-        enqueue_records(e, true);
+        if (e->multi) {
+            int drc = decode_files(e, err);
+            if (drc) {
+                for (auto &x : ev) cudaEventDestroy(x);
+                return drc;
+            }
+        } else {
+            enqueue_records(e, true);
+        }
         cudaEventRecord(ev[3], e->stream);
         ce = cudaStreamSynchronize(e->stream);
         for (int k = 0; k < 3 && ce == cudaSuccess; ++k) {

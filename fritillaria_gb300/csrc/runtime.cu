@@ -206,7 +206,7 @@ void frt::batch_release(const frt_inflate_batch *cb)
     if (b->refs.fetch_sub(1) != 1) return;
     {
         DeviceGuard g(b->device);
-        dev_free(b->data, b->stream);
+        if (b->owns_data) dev_free(b->data, b->stream);
         dev_free(b->d_offsets, b->stream);
         if (b->ready) cudaEventDestroy(b->ready);
     }

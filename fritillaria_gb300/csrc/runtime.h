@@ -86,6 +86,7 @@ struct frt_inflate_batch {
     uint64_t *d_offsets = nullptr; // n + 1 member starts, then n compressed offsets
     cudaEvent_t ready = nullptr;
     frt::SharedStream *shared = nullptr;
+    bool owns_data = true; // false for a view into memory owned elsewhere (an engine's output)
 };
 
 namespace frt {

@@ -366,6 +366,42 @@ int frt_engine_column(const frt_engine *e, int column, void **ptr, size_t *bytes
 int frt_engine_column_to_host(const frt_engine *e, int column, void *dst, size_t cap, frt_error *err);
 const uint8_t *frt_engine_inflated(const frt_engine *e, size_t *len);
 void *frt_engine_stream(const frt_engine *e);
+/* Several files, several formats, one inflate.  No reference counterpart:
+ * BGZF files laid out back to back in one device buffer (each a whole BGZF
+ * stream, together covering the buffer) are discovered, queued and inflated
+ * as one population of members by the persistent kernel; each file's inflated
+ * range then goes through its format's decoder (BamDecoder, BcfScanner,
+ * FastqScanner, FastaCompactor).  BAM and BCF headers are parsed at bind.
+ * frt_engine_run runs the inflate and the decoders; the per-file results stay
+ * valid until the next run. */
+typedef enum { FRT_FORMAT_BAM = 0, FRT_FORMAT_BCF = 1, FRT_FORMAT_FASTQ = 2, FRT_FORMAT_FASTA = 3 } frt_format;
+
+typedef struct {
+    uint64_t offset; /* in the bound buffer */
+    uint64_t length;
+    int32_t format;  /* frt_format */
+} frt_engine_file;
+
+typedef struct {
+    int32_t format;
+    uint64_t members;
+    uint64_t compressed_bytes;
+    uint64_t inflated_offset; /* where the file's bytes start in frt_engine_inflated */
+    uint64_t inflated_bytes;
+    uint64_t records;         /* contigs for FASTA */
+    uint64_t tail;            /* BAM/BCF/FASTQ: carry point; FASTA: total bases */
+    uint64_t proof;           /* BCF/FASTQ: 0 tiled, 1 walked */
+} frt_engine_file_info;
+
+int frt_engine_bind_files(frt_engine *e, const uint8_t *dev, size_t len, const frt_engine_file *files, size_t n_files,
+                          frt_error *err);
+size_t frt_engine_file_count(const frt_engine *e);
+int frt_engine_get_file_info(const frt_engine *e, size_t file, frt_engine_file_info *info);
+/* The last run's result for a file: a BAM file's record batch, or the column
+ * batch of a BCF/FASTQ/FASTA file; owned by the engine (do not free). */
+const frt_record_batch *frt_engine_file_bam(const frt_engine *e, size_t file);
+const frt_columns *frt_engine_file_columns(const frt_engine *e, size_t file);
+
 /* Per-stage milliseconds (front, inflate, records) of eager runs. */
 int frt_engine_time_stages(frt_engine *e, float *ms, int repeats, frt_error *err);
 /* Kernel launches per run (kernel nodes of the captured graph). */
