@@ -54,6 +54,17 @@ WORKLOADS = {
                                 "MM/ML/qs/ch tags, BGZF level 6 packed full"),
 }
 
+# Several formats in one persistent inflate: (a) BCF, (b) bgzipped FASTQ,
+# (c) bgzipped FASTA, decoded by their scanners after one inflate of all members.
+MIXED = {
+    "mixed_formats": dict(bcf_sites=2_000_000, bcf_samples=500, fastq_reads=10_000_000, fasta_bases=3_100_000_000,
+                          desc="one persistent inflate over (a) BCF 2M sites x 500 samples over 24 contigs, "
+                               "(b) bgzipped FASTQ 10M x 150 bp, (c) bgzipped FASTA 3.1 Gb (60-column lines, "
+                               "soft-masked runs, N runs); each then decoded by its scanner"),
+    "mixed_formats_small": dict(bcf_sites=200_000, bcf_samples=500, fastq_reads=1_000_000, fasta_bases=310_000_000,
+                                desc="the mixed-format workload at one tenth size (profiling size)"),
+}
+
 METRIC = "BAM->device-column decompressed GB/s, batched vs plain, 1 GB300, bit-exact"
 
 
@@ -63,7 +74,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=sorted(WORKLOADS), default="short_reads_20m")
+    p.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(MIXED), default="short_reads_20m")
     p.add_argument("--no-plain", action="store_true", help="skip the per-batch comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     return p.parse_args()
@@ -190,10 +201,33 @@ def cpu_baseline(bgzf, inflated_bytes: int):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    bgzf = generate(args.workload)
     from oracle import oracle
 
     threads = os.cpu_count() or 1
+    if args.workload in MIXED:
+        files = generate_mixed(args.workload)
+        fmt = {"bcf": 1, "fastq": 2, "fasta": 3}
+        times, total = [], 0
+        for i in range(args.warmup + args.steps):
+            secs, total, records = 0.0, 0, 0
+            for name, _, bgzf in files:
+                r = oracle.baseline_file(bgzf, fmt[name], threads)
+                secs, total, records = secs + r.seconds, total + r.inflated_bytes, records + r.records
+            if i >= args.warmup:
+                times.append(secs)
+        gbs = total * len(times) / sum(times) / 1e9
+        line = {"impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * sum(times) / len(times), 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+                "config": {"workload": args.workload, "description": MIXED[args.workload]["desc"],
+                           "inflated_bytes": total, "records": records},
+                "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                                 "sample": "the three whole files per step; C restatement of the noodles CPU path "
+                                           "(multithreaded BGZF inflate + serial scan/decode per format)"},
+                "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    bgzf = generate(args.workload)
     times = []
     res = None
     for i in range(args.warmup + args.steps):
@@ -380,11 +414,166 @@ def run_ours(args, rank, world, local):
         dist.destroy_process_group()
 
 
+def generate_mixed(name: str):
+    """[(format name, raw bytes, bgzf bytes)] for the mixed-format workload."""
+    from fritillaria_gb300 import synth
+
+    w = MIXED[name]
+    files = []
+    raw, bgzf = synth.bcf(w["bcf_sites"], n_samples=w["bcf_samples"], n_contigs=24, seed=61, levels=(6, 6))
+    files.append(("bcf", raw.size, bgzf))
+    del raw
+    raw, bgzf = synth.fastq(w["fastq_reads"], seed=62, levels=(6, 6))
+    files.append(("fastq", raw.size, bgzf))
+    del raw
+    raw, bgzf = synth.fasta(24, w["fasta_bases"], 60, False, seed=63, levels=(6, 6))
+    files.append(("fasta", raw.size, bgzf))
+    del raw
+    return files
+
+
+def run_mixed(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    import fritillaria_gb300 as frt
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    files = generate_mixed(args.workload)
+    blob = np.concatenate([f[2] for f in files])
+    host = torch.from_numpy(blob).pin_memory()
+    dev = host.to("cuda")
+    fmt = {"bam": frt.Format.BAM, "bcf": frt.Format.BCF, "fastq": frt.Format.FASTQ, "fasta": frt.Format.FASTA}
+    layout, at = [], 0
+    for name, _, bgzf in files:
+        layout.append((at, bgzf.size, fmt[name]))
+        at += bgzf.size
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    eng = frt.BatchEngine(0, stream=stream.cuda_stream)
+    eng.bind_files(dev.data_ptr(), dev.numel(), layout)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            eng.run()
+            st = eng.finish()
+        assert st.status == 0
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        with Clocks(local) as clocks:
+            t0 = time.perf_counter()
+            ev0.record(stream)
+            for _ in range(args.steps):
+                eng.run()
+                st = eng.finish()
+                if st.status != 0:
+                    raise RuntimeError(f"engine status {st.status}")
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(ms, dist, "cuda")
+    if dist:
+        dist.barrier()
+    ms_step = ms / args.steps
+    inflated = st.inflated_bytes
+    value = whole_job_gbs(inflated, world, args.steps, ms)
+
+    front_ms, inflate_ms, decode_ms = eng.time_stages(3)
+    per = {}
+    col_bytes = 0
+    launches = 0
+    for i, (name, raw_size, bgzf) in enumerate(files):
+        info = eng.file_info(i)
+        res = eng.file_result(i)
+        cb = sum(res.column_ptr(k)[1] for k in res._cols)
+        col_bytes += cb
+        launches += info.launches
+        algo = info.inflated_bytes + cb  # read the inflated file, write its columns
+        per[name] = {"compressed_bytes": int(info.compressed_bytes), "inflated_bytes": int(info.inflated_bytes),
+                     "records": int(info.records), "decode_ms": round(info.decode_ms, 3),
+                     "decode_gbs": round(info.inflated_bytes / (info.decode_ms / 1e3) / 1e9, 2) if info.decode_ms else None,
+                     "column_bytes": int(cb), "proof": int(info.proof),
+                     "decode_hbm_frac": round(algo / (info.decode_ms / 1e3) / 1e9 / peaks()[0], 4) if info.decode_ms else None}
+    peak, peak_kind = peaks()
+    payload = sum(int(frt.discover_blocks(f[2])[0]["payload_len"].astype(np.uint64).sum()) for f in files)
+    inflate_bytes = payload + inflated
+    achieved = inflate_bytes / (inflate_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 5), "traffic": None,
+                "kernel": "k_inflate_persistent (one persistent inflate over the members of all three files)",
+                "algorithmic_bytes_per_launch": inflate_bytes, "kernel_ms": round(inflate_ms, 3),
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "pipeline": {"bytes": blob.size + inflated + col_bytes, "ms": round(ms_step, 3),
+                             "frac": round((blob.size + inflated + col_bytes) / (ms_step / 1e3) / 1e9 / peak, 5)},
+                "stages_ms": {"discover_plan_queue": round(front_ms, 3), "inflate_verify": round(inflate_ms, 3),
+                              "decoders": round(decode_ms, 3)}}
+
+    e2e_steps = max(3, min(args.steps, 5))
+    hbuf = host.numpy()
+    eng.run_host(hbuf)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        st2 = eng.run_host(hbuf)
+        assert st2.status == 0
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, dist, "cuda")
+    e2e = {"value": round(whole_job_gbs(inflated, world, 1, 1e3 * e2e_s), 3), "unit": "GB/s",
+           "h2d_bytes_per_step": int(blob.size), "d2h_bytes_per_step": 128, "ms_per_step": round(1e3 * e2e_s, 3)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle
+
+        threads = os.cpu_count() or 1
+        secs, nbytes, parts = 0.0, 0, {}
+        for name, _, bgzf in files:
+            r = oracle.baseline_file(bgzf, int(fmt[name]), threads)
+            secs += r.seconds
+            nbytes += r.inflated_bytes
+            parts[name] = {"seconds": round(r.seconds, 3), "records": int(r.records)}
+        cpu = {"value": round(nbytes / secs / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+               "sample": f"whole files: {parts}; C restatement of the noodles multithreaded BGZF reader (zlib 1.3 "
+                         f"inflate + CRC32 on all cores) then the reference's serial CPU scan/decode per format"}
+
+    if rank == 0:
+        w = MIXED[args.workload]
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": args.workload, "description": w["desc"], "members": st.members,
+                       "compressed_bytes": int(blob.size), "inflated_bytes": int(inflated), "records": int(st.records),
+                       "column_bytes": int(col_bytes), "files": per, "l2": "inputs larger than L2 (no flush)",
+                       "queue": "sorted by compressed size", "graph": "discovery + plan + inflate",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": eng.launches_per_run() * args.steps,
+            "clocks": clocks.summary(),
+            "wall_s": round(wall, 3),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload in MIXED:
+        run_mixed(args, rank, world, local)
         return
     run_ours(args, rank, world, local)
 

@@ -784,7 +784,7 @@ class EngineFile(C.Structure):
 class EngineFileInfo(C.Structure):
     _fields_ = [("format", C.c_int32), ("members", C.c_uint64), ("compressed_bytes", C.c_uint64),
                 ("inflated_offset", C.c_uint64), ("inflated_bytes", C.c_uint64), ("records", C.c_uint64),
-                ("tail", C.c_uint64), ("proof", C.c_uint64)]
+                ("tail", C.c_uint64), ("proof", C.c_uint64), ("decode_ms", C.c_double), ("launches", C.c_uint64)]
 
 
 class BatchEngine:

@@ -425,6 +425,7 @@ struct frt_engine {
         frt_inflate_batch *view = nullptr;
         frt_record_batch *bam = nullptr;
         frt_columns *cols = nullptr;
+        cudaEvent_t t0 = nullptr, t1 = nullptr; // around the file's decode
     };
     bool multi = false;
     std::vector<File> files;
@@ -461,8 +462,11 @@ void release_results(frt_engine *e)
 void free_all(frt_engine *e)
 {
     release_results(e);
-    for (auto &f : e->files)
+    for (auto &f : e->files) {
         if (f.view) batch_release(f.view);
+        if (f.t0) cudaEventDestroy(f.t0);
+        if (f.t1) cudaEventDestroy(f.t1);
+    }
     e->files.clear();
     e->multi = false;
     if (e->exec) cudaGraphExecDestroy(e->exec);
@@ -820,6 +824,7 @@ int decode_files(frt_engine *e, frt_error *err)
     release_results(e);
     for (auto &f : e->files) {
         cudaEventRecord(f.view->ready, e->stream);
+        cudaEventRecord(f.t0, e->stream);
         int rc = FRT_OK;
         switch (f.desc.format) {
         case FRT_FORMAT_BAM:
@@ -836,9 +841,22 @@ int decode_files(frt_engine *e, frt_error *err)
             rc = frt_fasta_compact(e->fasta, f.view, &f.cols, err);
             break;
         }
+        cudaEventRecord(f.t1, e->stream);
         if (rc) return rc;
     }
     return FRT_OK;
+}
+
+// Kernels each decoder launches (counted from their launch sequences in
+// decoder.cu and formats.cu; the BCF walk adds two when it runs).
+uint64_t decode_launches(const frt_engine::File &f)
+{
+    switch (f.desc.format) {
+    case FRT_FORMAT_BAM: return 7;   // spec, reconcile, decode, 3-kernel scan, aux directory
+    case FRT_FORMAT_BCF: return 8;   // sieve x2, 3-kernel scan, check, finalize, decode
+    case FRT_FORMAT_FASTQ: return 13; // newline count/emit, 2 scans, lines, compact, check, finalize, decode
+    default: return 6;                // three passes, tile scan, scan64, lengths
+    }
 }
 
 // Inflate errors first: decoding garbage would only hide them.
@@ -946,6 +964,8 @@ extern "C" int frt_engine_bind_files(frt_engine *e, const uint8_t *dev, size_t l
         std::copy(v->offsets.begin(), v->offsets.end(), dev_off.begin());
         std::copy(v->coffsets.begin(), v->coffsets.end(), dev_off.begin() + k + 1);
         cudaEventCreateWithFlags(&v->ready, cudaEventDisableTiming);
+        cudaEventCreate(&f.t0);
+        cudaEventCreate(&f.t1);
         f.view = v;
         if ((rc = dev_alloc((void **)&v->d_offsets, 8 * dev_off.size(), s, err))) return rc;
         if ((ce = cudaMemcpyAsync(v->d_offsets, dev_off.data(), 8 * dev_off.size(), cudaMemcpyHostToDevice, s)) !=
@@ -997,6 +1017,10 @@ extern "C" int frt_engine_get_file_info(const frt_engine *e, size_t i, frt_engin
         o.tail = f.desc.format == FRT_FORMAT_FASTA ? frt_columns_total_bases(f.cols) : frt_columns_tail(f.cols);
         frt_columns_scan_info(f.cols, &o.proof, nullptr, nullptr);
     }
+    float ms = 0;
+    if (f.t1 && cudaEventSynchronize(f.t1) == cudaSuccess && cudaEventElapsedTime(&ms, f.t0, f.t1) == cudaSuccess)
+        o.decode_ms = ms;
+    o.launches = decode_launches(f);
     *info = o;
     return FRT_OK;
 }
@@ -1162,7 +1186,10 @@ extern "C" int frt_engine_time_stages(frt_engine *e, float *ms, int repeats, frt
 // Kernels this library launches per engine run (the graph's kernel nodes).
 extern "C" uint64_t frt_engine_launches(const frt_engine *e)
 {
-    if (!e || !e->graph) return 0;
+    if (!e) return 0;
+    uint64_t dec = 0;
+    for (auto &f : e->files) dec += decode_launches(f);
+    if (!e->graph) return dec;
     size_t n = 0;
     cudaGraphGetNodes(e->graph, nullptr, &n);
     std::vector<cudaGraphNode_t> nodes(n);
@@ -1173,5 +1200,5 @@ extern "C" uint64_t frt_engine_launches(const frt_engine *e)
         cudaGraphNodeGetType(nd, &t);
         if (t == cudaGraphNodeTypeKernel) ++k;
     }
-    return k;
+    return k + dec;
 }

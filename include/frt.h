@@ -391,6 +391,8 @@ typedef struct {
     uint64_t records;         /* contigs for FASTA */
     uint64_t tail;            /* BAM/BCF/FASTQ: carry point; FASTA: total bases */
     uint64_t proof;           /* BCF/FASTQ: 0 tiled, 1 walked */
+    double decode_ms;         /* the last run's decode of this file (CUDA events on the engine stream) */
+    uint64_t launches;        /* kernels that decode launched */
 } frt_engine_file_info;
 
 int frt_engine_bind_files(frt_engine *e, const uint8_t *dev, size_t len, const frt_engine_file *files, size_t n_files,

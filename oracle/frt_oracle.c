@@ -601,3 +601,93 @@ int orc_baseline_bam(const uint8_t *file, size_t len, int threads, uint64_t max_
     free(spans);
     return status;
 }
+
+
+/* CPU baseline for the other formats on the container: the same
+ * multithreaded inflate (every member inflated and CRC-checked by the worker
+ * pool), then the reference's serial CPU scan and decode of the whole file:
+ *   FASTQ  scan_records + bounds (fastq record.rs:158-200, batch.rs);
+ *   BCF    the length-prefix chain + Record::bounds (bcf batch.rs:222-241);
+ *   FASTA  scan_records(at_eof) + compact_into (fasta record.rs:180-330).
+ * format: 1 BCF, 2 FASTQ, 3 FASTA (frt_format numbering). */
+int orc_baseline_file(const uint8_t *file, size_t len, int format, int threads, orc_baseline_result *res)
+{
+    memset(res, 0, sizeof *res);
+    double t0 = now_s();
+    size_t cap = len / 28 + 1;
+    orc_span *spans = (orc_span *)malloc(cap * sizeof *spans);
+    size_t n = 0, consumed = 0;
+    orc_error err;
+    if (orc_bgzf_discover(file, len, 0, spans, cap, &n, &consumed, &err)) { free(spans); res->status = err.code; return err.code; }
+    uint64_t *out_off = (uint64_t *)malloc((n + 1) * sizeof *out_off);
+    uint64_t total = 0;
+    for (size_t i = 0; i < n; ++i) { out_off[i] = total; total += spans[i].isize; }
+    out_off[n] = total;
+    uint8_t *out = (uint8_t *)malloc(total + 1);
+    bl_ctx ctx;
+    ctx.file = file; ctx.spans = spans; ctx.out_off = out_off; ctx.out = out; ctx.n = n;
+    atomic_init(&ctx.next, 0);
+    atomic_init(&ctx.failed, 0);
+    ctx.done = (atomic_uchar *)calloc(n + 1, 1);
+    if (threads < 1) threads = 1;
+    pthread_t *tids = (pthread_t *)malloc(sizeof(pthread_t) * threads);
+    for (int t = 0; t < threads; ++t) pthread_create(&tids[t], NULL, bl_worker, &ctx);
+    for (int t = 0; t < threads; ++t) pthread_join(tids[t], NULL);
+    int status = atomic_load(&ctx.failed) ? ORC_ERR_CHECKSUM : ORC_OK;
+    uint64_t records = 0, checksum = 0;
+    if (!status && format == 2) {
+        uint64_t pos = 0;
+        orc_fastq_bounds b;
+        while (pos < total) {
+            if (out[pos] == '\n') { ++pos; continue; }
+            if (!orc_fastq_bounds_at(out, total, pos, &b)) break;
+            checksum += b.sequence_len * 7u + b.quality_start;
+            ++records;
+            pos += b.record_end;
+        }
+    } else if (!status && format == 1) {
+        uint64_t start;
+        uint32_t samples, contigs;
+        if (orc_bcf_header(out, total, &start, &samples, &contigs, &err)) {
+            status = err.code;
+        } else {
+            uint64_t pos = start;
+            int32_t chrom, posv, rlen;
+            uint32_t qual, ns, a, f, inf, g, e;
+            uint16_t ni, na;
+            uint8_t nf;
+            orc_bcf_columns c = {&chrom, &posv, &rlen, &qual, &ni, &na, &ns, &nf, &a, &f, &inf, &g, &e};
+            while (pos + 8 <= total) {
+                uint64_t ls = rd32(out + pos), li = rd32(out + pos + 4);
+                if (ls < 24 || pos + 8 + ls + li > total) break;
+                if (orc_bcf_decode(out, total, &pos, 1, &c)) { status = ORC_ERR_MALFORMED; break; }
+                checksum += (uint64_t)(uint32_t)posv * 3u + a + f + inf;
+                ++records;
+                pos += 8 + ls + li;
+            }
+        }
+    } else if (!status && format == 3) {
+        size_t cap2 = total / 2 + 1, nc = 0;
+        uint64_t *so = (uint64_t *)malloc(3 * cap2 * sizeof(uint64_t));
+        uint64_t bases = 0;
+        uint8_t *seq = (uint8_t *)malloc(total + 1);
+        if (orc_fasta_compact(out, total, seq, total + 1, so, so + cap2, so + 2 * cap2, NULL, cap2, &nc, &bases))
+            status = ORC_ERR_MALFORMED;
+        records = nc;
+        checksum = bases;
+        free(seq);
+        free(so);
+    }
+    res->seconds = now_s() - t0;
+    res->members = n;
+    res->inflated_bytes = total;
+    res->records = records;
+    res->checksum = checksum;
+    res->status = status;
+    free(tids);
+    free((void *)ctx.done);
+    free(out);
+    free(out_off);
+    free(spans);
+    return status;
+}

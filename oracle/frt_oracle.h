@@ -124,6 +124,8 @@ typedef struct {
 
 int orc_baseline_bam(const uint8_t *file, size_t len, int threads, uint64_t max_members,
                      orc_baseline_result *res);
+/* The same for a bgzipped BCF (1), FASTQ (2) or FASTA (3) file. */
+int orc_baseline_file(const uint8_t *file, size_t len, int format, int threads, orc_baseline_result *res);
 
 /* ---- FASTQ, BCF, FASTA (frt_oracle_formats.c) ---------------------------- */
 

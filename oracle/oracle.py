@@ -53,6 +53,7 @@ def lib():
         _lib.orc_bam_decode.argtypes = [_P, _P, C.c_size_t, _P]
         _lib.orc_bam_aux.argtypes = [_P, C.c_uint32, C.c_uint32, _P, C.c_uint32, _P]
         _lib.orc_baseline_bam.argtypes = [_P, C.c_size_t, C.c_int, C.c_uint64, _P]
+        _lib.orc_baseline_file.argtypes = [_P, C.c_size_t, C.c_int, C.c_int, _P]
         _lib.orc_fastq_scan.argtypes = [_P, C.c_uint64, C.c_uint64, _P, C.c_size_t, _P, _P, _P, _P]
         _lib.orc_fastq_decode.argtypes = [_P, C.c_uint64, _P, C.c_size_t, _P, _P, _P, _P, _P]
         _lib.orc_bcf_header.argtypes = [_P, C.c_uint64, _P, _P, _P, _P]
@@ -240,6 +241,14 @@ def virtual_offsets(spans, member_offsets, record_offsets):
     m = np.searchsorted(mo, ro, side="right") - 1
     co = np.asarray(spans["compressed_offset"], dtype=np.uint64)[m]
     return (co << np.uint64(16)) | (ro - mo[m])
+
+
+def baseline_file(bgzf, fmt: int, threads: int):
+    """CPU baseline for a bgzipped BCF (1), FASTQ (2) or FASTA (3) file."""
+    b = _buf(bgzf)
+    res = OrcBaseline()
+    lib().orc_baseline_file(_ptr(b), b.size, fmt, threads, C.byref(res))
+    return res
 
 
 def baseline_bam(bgzf, threads: int, max_members: int = 0):
