@@ -235,6 +235,24 @@ def lib():
         "frt_engine_get_file_info": (C.c_int, [_P, C.c_size_t, _P]),
         "frt_engine_file_bam": (_P, [_P, C.c_size_t]),
         "frt_engine_file_columns": (_P, [_P, C.c_size_t]),
+        "frt_bai_parse": (C.c_int, [_P, C.c_size_t, _P, _P]),
+        "frt_bai_free": (None, [_P]),
+        "frt_bai_reference_count": (C.c_int32, [_P]),
+        "frt_bai_query": (C.c_int, [_P, C.c_int32, C.c_uint64, C.c_uint64, _P, C.c_size_t, _P, _P]),
+        "frt_server_create": (C.c_int, [C.c_int, _P, C.c_uint64, _P, _P]),
+        "frt_server_destroy": (None, [_P]),
+        "frt_server_set_limits": (None, [_P, C.c_uint32, C.c_uint32]),
+        "frt_server_clock_ms": (C.c_double, [_P]),
+        "frt_server_add_bam": (C.c_int, [_P, _P, C.c_size_t, _P, C.c_size_t, _P, _P]),
+        "frt_server_submit": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, C.c_double, _P, _P]),
+        "frt_server_progress": (C.c_int, [_P, _P, _P]),
+        "frt_server_drain": (C.c_int, [_P, _P]),
+        "frt_server_request_info": (C.c_int, [_P, C.c_uint64, _P]),
+        "frt_server_request_error": (C.c_int, [_P, C.c_uint64, _P]),
+        "frt_server_request_column": (C.c_int, [_P, C.c_uint64, C.c_int, _P, _P, _P]),
+        "frt_server_request_column_to_host": (C.c_int, [_P, C.c_uint64, C.c_int, _P, C.c_size_t, _P]),
+        "frt_server_request_inflated": (_P, [_P, C.c_uint64, _P]),
+        "frt_server_release": (None, [_P, C.c_uint64]),
         "frt_fastq_scanner_create": (C.c_int, [C.c_int, _P, _P, _P]),
         "frt_fastq_scanner_destroy": (None, [_P]),
         "frt_fastq_decode": (C.c_int, [_P, _P, C.c_uint64, _P, _P]),
@@ -785,6 +803,124 @@ class EngineFileInfo(C.Structure):
     _fields_ = [("format", C.c_int32), ("members", C.c_uint64), ("compressed_bytes", C.c_uint64),
                 ("inflated_offset", C.c_uint64), ("inflated_bytes", C.c_uint64), ("records", C.c_uint64),
                 ("tail", C.c_uint64), ("proof", C.c_uint64), ("decode_ms", C.c_double), ("launches", C.c_uint64)]
+
+
+class Bai:
+    """A BAI index (crates/fritillaria-bam/src/bai.rs) with the region query of
+    the csi BinningIndex (binning_index/index.rs:93-119)."""
+
+    def __init__(self, data):
+        self._buf = _u8(data)
+        h = _P()
+        err = _Err()
+        _raise(lib().frt_bai_parse(self._buf.ctypes.data, self._buf.size, C.byref(h), C.byref(err)), err)
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def reference_count(self) -> int:
+        return int(lib().frt_bai_reference_count(self._h))
+
+    def query(self, ref: int, start: int = 0, end: int = 0):
+        """Chunks (start, end virtual offsets) for [start, end], 1-based inclusive."""
+        n = C.c_size_t()
+        err = _Err()
+        rc = lib().frt_bai_query(self._h, ref, start, end, None, 0, C.byref(n), C.byref(err))
+        if rc and n.value == 0:
+            _raise(rc, err)
+        out = np.zeros(max(n.value, 1), dtype=[("start", "<u8"), ("end", "<u8")])
+        _raise(lib().frt_bai_query(self._h, ref, start, end, out.ctypes.data, len(out), C.byref(n), C.byref(err)), err)
+        return [(int(a), int(b)) for a, b in out[: n.value]]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.frt_bai_free(h)
+            self._h = None
+
+
+REGION_COLUMNS = {"virtual_offset": (0, np.uint64), "record_offset": (1, np.uint64), "ref_id": (2, np.int32),
+                  "pos": (3, np.int32), "flags": (4, np.uint16), "mapq": (5, np.uint8), "seq_len": (6, np.uint32)}
+
+
+class RegionInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("records", C.c_uint64), ("arrival_ms", C.c_double),
+                ("done_ms", C.c_double), ("inflated_bytes", C.c_uint64), ("chunks", C.c_uint32),
+                ("members", C.c_uint64), ("retries", C.c_uint32)]
+
+
+class RegionServer:
+    """Region queries over resident BAMs with their BAIs, batched continuously
+    into one persistent inflate per tick (frt_server_*)."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 150 << 30, stream: int | None = None):
+        h = _P()
+        err = _Err()
+        _raise(lib().frt_server_create(device, stream, int(budget_bytes), C.byref(h), C.byref(err)), err)
+        self._h = h
+
+    def set_limits(self, max_requests_per_tick: int = 0, max_ticks_in_flight: int = 2) -> None:
+        lib().frt_server_set_limits(self._h, max_requests_per_tick, max_ticks_in_flight)
+
+    def clock_ms(self) -> float:
+        return lib().frt_server_clock_ms(self._h)
+
+    def add_bam(self, bgzf, bai) -> int:
+        b, x = _u8(bgzf), _u8(bai)
+        fid = C.c_int32()
+        err = _Err()
+        _raise(lib().frt_server_add_bam(self._h, b.ctypes.data, b.size, x.ctypes.data, x.size, C.byref(fid),
+                                        C.byref(err)), err)
+        return fid.value
+
+    def submit(self, file: int, ref: int, start: int, end: int, arrival_ms: float = -1.0) -> int:
+        rid = C.c_uint64()
+        err = _Err()
+        _raise(lib().frt_server_submit(self._h, file, ref, start, end, arrival_ms, C.byref(rid), C.byref(err)), err)
+        return rid.value
+
+    def progress(self) -> int:
+        n = C.c_uint32()
+        err = _Err()
+        _raise(lib().frt_server_progress(self._h, C.byref(n), C.byref(err)), err)
+        return n.value
+
+    def drain(self) -> None:
+        err = _Err()
+        _raise(lib().frt_server_drain(self._h, C.byref(err)), err)
+
+    def info(self, request: int) -> RegionInfo:
+        out = RegionInfo()
+        if lib().frt_server_request_info(self._h, request, C.byref(out)):
+            raise InvalidArgument(message=f"no request {request}")
+        return out
+
+    def check(self, request: int) -> None:
+        """Raises the request's error, if it failed."""
+        err = _Err()
+        _raise(lib().frt_server_request_error(self._h, request, C.byref(err)), err)
+
+    def column(self, request: int, name: str) -> np.ndarray:
+        cid, dt = REGION_COLUMNS[name]
+        p, nb, w = _P(), C.c_size_t(), C.c_size_t()
+        if lib().frt_server_request_column(self._h, request, cid, C.byref(p), C.byref(nb), C.byref(w)):
+            raise InvalidArgument(message=f"request {request} has no results")
+        out = np.empty(nb.value // np.dtype(dt).itemsize, dtype=dt)
+        err = _Err()
+        _raise(lib().frt_server_request_column_to_host(self._h, request, cid, out.ctypes.data, out.nbytes,
+                                                       C.byref(err)), err)
+        return out
+
+    def release(self, request: int) -> None:
+        lib().frt_server_release(self._h, request)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.frt_server_destroy(h)
+            self._h = None
 
 
 class BatchEngine:

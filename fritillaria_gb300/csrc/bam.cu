@@ -121,15 +121,11 @@ __device__ Seg walk_record(const u8 *buf, u64 len, u64 from, u64 until, u64 msta
 
 } // namespace
 
-// Phase 1.  One warp per member.
-__global__ void k_bam_spec(const u8 *buf, u64 len, const u64 *starts, u32 n_members, u64 start,
-                                        int n_ref, u64 *entry, u32 *count, u64 *land, u8 *flags, u16 *scratch,
-                                        const u64 *start_dev, const int *nref_dev)
+// Phase 1 for member m: the first plausible record start, then the walk to
+// the member end.  Called by one whole warp.
+__device__ void spec_member(const u8 *buf, u64 len, const u64 *starts, u32 m, u64 start, int n_ref, u64 *entry,
+                            u32 *count, u64 *land, u8 *flags, u16 *scratch)
 {
-    u32 m = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    if (m >= n_members) return;
-    if (start_dev) start = *start_dev;
-    if (nref_dev) n_ref = *nref_dev < 0 ? (1 << 24) : *nref_dev;
     const u32 lane = lane_id();
     u64 ms = starts[m], me = starts[m + 1];
     u64 e = INF64;
@@ -167,13 +163,38 @@ __global__ void k_bam_spec(const u8 *buf, u64 len, const u64 *starts, u32 n_memb
     }
 }
 
-// Phase 2.  One CTA of 1024 threads.  totals = {n_records, tail, status,
-// fallbacks}.
-__global__ void __launch_bounds__(1024)
-k_bam_reconcile(const u8 *buf, u64 len, const u64 *starts, u32 n_members, u64 start, u64 *entry, u32 *count,
-                  u64 *land, u8 *flags, u16 *scratch, u32 *first_index, u64 *totals, const u64 *start_dev)
+// Phase 1.  One warp per member.
+__global__ void k_bam_spec(const u8 *buf, u64 len, const u64 *starts, u32 n_members, u64 start,
+                                        int n_ref, u64 *entry, u32 *count, u64 *land, u8 *flags, u16 *scratch,
+                                        const u64 *start_dev, const int *nref_dev)
 {
+    u32 m = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (m >= n_members) return;
     if (start_dev) start = *start_dev;
+    if (nref_dev) n_ref = *nref_dev < 0 ? (1 << 24) : *nref_dev;
+    spec_member(buf, len, starts, m, start, n_ref, entry, count, land, flags, scratch);
+}
+
+// Phase 1 over many segments (independent record chains, each over its own
+// members): segment s owns members [seg[s].m0, seg[s].m0 + seg[s].n) of the
+// per-member arrays and the n + 1 starts at starts + seg[s].m0 + s.
+__global__ void k_bam_spec_seg(const u8 *buf, const FrtScanSeg *seg, const u32 *seg_of, u32 n_total, int n_ref,
+                               const u64 *starts, u64 *entry, u32 *count, u64 *land, u8 *flags, u16 *scratch)
+{
+    u32 g = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (g >= n_total) return;
+    u32 si = seg_of[g];
+    FrtScanSeg sg = seg[si];
+    u32 j = g - sg.m0;
+    spec_member(buf, sg.len, starts + sg.m0 + si, j, sg.start, n_ref, entry + sg.m0, count + sg.m0, land + sg.m0,
+                flags + sg.m0, scratch + (size_t)sg.m0 * FRT_SCAN_CAP);
+}
+
+// Phase 2 for one record chain, by one CTA of 1024 threads.  totals =
+// {n_records, tail, status, fallbacks}.
+__device__ void reconcile_chain(const u8 *buf, u64 len, const u64 *starts, u32 n_members, u64 start, u64 *entry,
+                                u32 *count, u64 *land, u8 *flags, u16 *scratch, u32 *first_index, u64 *totals)
+{
     __shared__ u64 s_warp[32];
     __shared__ u64 s_carry;
     __shared__ u32 s_bad;
@@ -337,6 +358,104 @@ k_bam_reconcile(const u8 *buf, u64 len, const u64 *starts, u32 n_members, u64 st
         totals[1] = s_stop ? s_tail : s_carry;
         totals[2] = s_stop == 2 ? 1ull : 0ull;
         totals[3] = s_fallbacks;
+    }
+}
+
+// Phase 2.  One CTA of 1024 threads.
+__global__ void __launch_bounds__(1024)
+k_bam_reconcile(const u8 *buf, u64 len, const u64 *starts, u32 n_members, u64 start, u64 *entry, u32 *count,
+                  u64 *land, u8 *flags, u16 *scratch, u32 *first_index, u64 *totals, const u64 *start_dev)
+{
+    if (start_dev) start = *start_dev;
+    reconcile_chain(buf, len, starts, n_members, start, entry, count, land, flags, scratch, first_index, totals);
+}
+
+// Phase 2 over many segments: one CTA per segment, totals at totals + 4 * s.
+__global__ void __launch_bounds__(1024)
+k_bam_reconcile_seg(const u8 *buf, const FrtScanSeg *seg, const u64 *starts, u64 *entry, u32 *count, u64 *land,
+                    u8 *flags, u16 *scratch, u32 *first_index, u64 *totals)
+{
+    u32 si = blockIdx.x;
+    FrtScanSeg sg = seg[si];
+    reconcile_chain(buf, sg.len, starts + sg.m0 + si, sg.n, sg.start, entry + sg.m0, count + sg.m0, land + sg.m0,
+                    flags + sg.m0, scratch + (size_t)sg.m0 * FRT_SCAN_CAP, first_index + sg.m0, totals + 4ull * si);
+}
+
+// Region filter (crates/fritillaria-bam/src/io/reader/query.rs:97-122 with the
+// chunk bound of the csi query reader): a record is kept when its start
+// virtual offset is below its segment's chunk end, its reference is `ref`
+// and [pos + 1, pos + span] meets [beg, end] (span from the CIGAR's
+// M/D/N/=/X, at least 1).  One warp per member, lanes over its records.
+__device__ __forceinline__ bool region_keep(const u8 *buf, u64 rec, u64 voff, const FrtScanSeg &sg)
+{
+    if (voff >= sg.chunk_end) return false;
+    int ref = (int)ld_u32le(buf + rec + 4), pos = (int)ld_u32le(buf + rec + 8);
+    if (ref != sg.ref || pos < 0) return false;
+    u32 name_len = buf[rec + 12], n_cigar = ld_u16le(buf + rec + 16);
+    u64 span = 0;
+    for (u32 k = 0; k < n_cigar; ++k) {
+        u32 op = ld_u32le(buf + rec + 36 + name_len + 4 * k), kind = op & 15u;
+        if (kind == 0 || kind == 2 || kind == 3 || kind == 7 || kind == 8) span += op >> 4;
+    }
+    if (span == 0) span = 1;
+    u64 a0 = (u64)pos + 1, a1 = a0 + span - 1;
+    return a0 <= sg.end && sg.beg <= a1;
+}
+
+__device__ __forceinline__ u64 member_voff(const u64 *coff, u32 m, u64 in_member) { return (coff[m] << 16) | in_member; }
+
+__global__ void k_region_count(const u8 *buf, const FrtScanSeg *seg, const u32 *seg_of, u32 n_total, const u64 *starts,
+                               const u64 *coff, const u32 *count, const u16 *scratch, u32 *kept)
+{
+    u32 g = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (g >= n_total) return;
+    u32 si = seg_of[g];
+    FrtScanSeg sg = seg[si];
+    const u64 ms = starts[g + si];
+    u32 n = count[g], c = 0;
+    const u16 *r = scratch + (size_t)g * FRT_SCAN_CAP;
+    for (u32 k = lane_id(); k < n; k += 32) {
+        u64 rec = ms + r[k];
+        c += region_keep(buf, rec, member_voff(coff, g, r[k]), sg);
+    }
+    for (int o = 16; o; o >>= 1) c += __shfl_down_sync(FRT_FULL_MASK, c, o);
+    if (lane_id() == 0) kept[g] = c;
+}
+
+__global__ void k_region_emit(const u8 *buf, const FrtScanSeg *seg, const u32 *seg_of, u32 n_total,
+                              const u64 *starts, const u64 *coff, const u32 *count, const u16 *scratch,
+                              const u32 *kept_first, FrtRegionColumns out)
+{
+    u32 g = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (g >= n_total) return;
+    u32 si = seg_of[g];
+    FrtScanSeg sg = seg[si];
+    const u64 ms = starts[g + si];
+    u32 n = count[g], at = kept_first[g];
+    const u16 *r = scratch + (size_t)g * FRT_SCAN_CAP;
+    const u32 lane = lane_id();
+    for (u32 b = 0; b < n; b += 32) {
+        u32 k = b + lane;
+        bool keep = false;
+        u64 rec = 0, voff = 0;
+        if (k < n) {
+            rec = ms + r[k];
+            voff = member_voff(coff, g, r[k]);
+            keep = region_keep(buf, rec, voff, sg);
+        }
+        u32 mask = __ballot_sync(FRT_FULL_MASK, keep);
+        if (keep) {
+            u32 i = at + __popc(mask & lanemask_lt());
+            out.virtual_offset[i] = voff;
+            out.record_offset[i] = rec - sg.out_base;
+            out.ref_id[i] = (int)ld_u32le(buf + rec + 4);
+            out.pos[i] = (int)ld_u32le(buf + rec + 8);
+            out.flags[i] = (u16)ld_u16le(buf + rec + 18);
+            out.mapq[i] = buf[rec + 13];
+            out.seq_len[i] = ld_u32le(buf + rec + 20);
+            out.request[i] = sg.request;
+        }
+        at += __popc(mask);
     }
 }
 
@@ -588,6 +707,29 @@ cudaError_t frt_launch_bam_decode(const u8 *buf, const u64 *starts, const u64 *c
 }
 
 size_t frt_scan_partials_len(u64 n) { return (size_t)(n / 4096 + 1); }
+
+cudaError_t frt_launch_region_scan(const u8 *buf, const FrtScanSeg *seg, const u32 *seg_of, u32 n_segs, u32 n_total,
+                                   int n_ref, const u64 *starts, const u64 *coff, u64 *entry, u32 *count, u64 *land,
+                                   u8 *flags, u16 *scratch, u32 *first_index, u64 *totals, u32 *kept, cudaStream_t s)
+{
+    if (n_total == 0 || n_segs == 0) return cudaSuccess;
+    unsigned g = (n_total + 7) / 8;
+    k_bam_spec_seg<<<g, 256, 0, s>>>(buf, seg, seg_of, n_total, n_ref, starts, entry, count, land, flags, scratch);
+    k_bam_reconcile_seg<<<n_segs, 1024, 0, s>>>(buf, seg, starts, entry, count, land, flags, scratch, first_index,
+                                                totals);
+    k_region_count<<<g, 256, 0, s>>>(buf, seg, seg_of, n_total, starts, coff, count, scratch, kept);
+    return cudaGetLastError();
+}
+
+cudaError_t frt_launch_region_emit(const u8 *buf, const FrtScanSeg *seg, const u32 *seg_of, u32 n_total,
+                                   const u64 *starts, const u64 *coff, const u32 *count, const u16 *scratch,
+                                   const u32 *kept_first, const FrtRegionColumns &out, cudaStream_t s)
+{
+    if (n_total == 0) return cudaSuccess;
+    k_region_emit<<<(n_total + 7) / 8, 256, 0, s>>>(buf, seg, seg_of, n_total, starts, coff, count, scratch,
+                                                    kept_first, out);
+    return cudaGetLastError();
+}
 
 // out has n + 1 entries; partials has frt_scan_partials_len(n) entries.
 cudaError_t frt_launch_scan_u32(const u32 *in, u64 n, u32 *partials, u32 *out, u32 *total, cudaStream_t s)

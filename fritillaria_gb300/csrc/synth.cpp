@@ -898,6 +898,161 @@ int frt_synth_fasta(int n_contigs, uint64_t total_bases, uint32_t line_width, in
     return 0;
 }
 
+// BAI (SAM specification 5.2) for a coordinate-sorted BAM already written as
+// BGZF: for each reference the bins (reg2bin with min_shift 14, depth 5) with
+// their chunks -- a chunk per run of consecutive records in the same bin, as
+// htslib's indexer forms them -- the metadata pseudo-bin 37450 (first/last
+// virtual offsets, mapped/unmapped counts), and the 16 kb linear index (the
+// start of the first record overlapping each window, gaps filled from the
+// next window).  Virtual offsets at a member boundary name the next member.
+int frt_synth_bai(const uint8_t *raw, size_t raw_len, const uint8_t *bgzf, size_t bgzf_len, uint8_t **out,
+                  size_t *out_len)
+{
+    // member layout: raw start and compressed offset of each member
+    std::vector<uint64_t> rstart, coff;
+    uint64_t r = 0;
+    for (size_t p = 0; p + 18 <= bgzf_len;) {
+        uint32_t xlen = bgzf[p + 10] | (bgzf[p + 11] << 8);
+        uint32_t bsize = 0;
+        for (uint32_t o = 0; o + 4 <= xlen;) {
+            const uint8_t *x = bgzf + p + 12 + o;
+            uint32_t sl = x[2] | (x[3] << 8);
+            if (x[0] == 'B' && x[1] == 'C' && sl == 2) bsize = (x[4] | (x[5] << 8)) + 1;
+            o += 4 + sl;
+        }
+        if (!bsize || p + bsize > bgzf_len) return -1;
+        const uint8_t *t = bgzf + p + bsize - 4;
+        uint32_t isize = t[0] | (t[1] << 8) | (t[2] << 16) | ((uint32_t)t[3] << 24);
+        rstart.push_back(r);
+        coff.push_back(p);
+        r += isize;
+        p += bsize;
+    }
+    rstart.push_back(r);
+    coff.push_back(bgzf_len);
+    if (r != raw_len) return -2;
+    auto voff = [&](uint64_t x) -> uint64_t {
+        size_t m = (size_t)(std::upper_bound(rstart.begin(), rstart.end(), x) - rstart.begin()) - 1;
+        while (m + 1 < rstart.size() && rstart[m + 1] == x) ++m; // a boundary names the next member
+        if (m + 1 >= rstart.size()) return coff.back() << 16;
+        return (coff[m] << 16) | (x - rstart[m]);
+    };
+    auto rd32 = [&](uint64_t at) { return (uint32_t)raw[at] | (raw[at + 1] << 8) | (raw[at + 2] << 16) | ((uint32_t)raw[at + 3] << 24); };
+    // header
+    uint64_t at = 4;
+    uint32_t l_text = rd32(at);
+    at += 4 + l_text;
+    int32_t n_ref = (int32_t)rd32(at);
+    at += 4;
+    for (int32_t i = 0; i < n_ref; ++i) at += 4 + rd32(at) + 4;
+    struct Ref {
+        std::vector<std::pair<uint32_t, std::vector<std::pair<uint64_t, uint64_t>>>> bins; // in first-seen order
+        std::vector<int64_t> lidx;
+        uint64_t beg = ~0ull, end = 0, mapped = 0, unmapped = 0;
+        bool any = false;
+    };
+    std::vector<Ref> refs(n_ref > 0 ? n_ref : 0);
+    std::vector<std::vector<int>> slot(refs.size()); // bin id -> index into bins (37450 + 1 entries)
+    int32_t cur_tid = -1;
+    uint32_t save_bin = 0xffffffffu;
+    uint64_t save_off = 0, last_off = 0;
+    auto flush = [&](int32_t tid) {
+        if (tid < 0 || save_bin == 0xffffffffu) return;
+        auto &rf = refs[tid];
+        auto &sl = slot[tid];
+        if (sl.empty()) sl.assign(37451, -1);
+        if (sl[save_bin] < 0) {
+            sl[save_bin] = (int)rf.bins.size();
+            rf.bins.push_back({save_bin, {}});
+        }
+        rf.bins[sl[save_bin]].second.push_back({save_off, last_off});
+    };
+    uint64_t n_no_coor = 0;
+    while (at + 4 <= raw_len) {
+        uint32_t bs = rd32(at);
+        uint64_t rec = at, end_at = at + 4 + bs;
+        int32_t tid = (int32_t)rd32(rec + 4), pos = (int32_t)rd32(rec + 8);
+        uint32_t name_len = raw[rec + 12], n_cigar = raw[rec + 16] | (raw[rec + 17] << 8);
+        uint16_t flag = (uint16_t)(raw[rec + 18] | (raw[rec + 19] << 8));
+        uint64_t v0 = voff(rec), v1 = voff(end_at);
+        if (tid < 0 || tid >= n_ref) {
+            ++n_no_coor;
+            at = end_at;
+            continue;
+        }
+        int64_t span = 0;
+        for (uint32_t k = 0; k < n_cigar; ++k) {
+            uint32_t op = rd32(rec + 36 + name_len + 4 * k), kind = op & 15;
+            if (kind == 0 || kind == 2 || kind == 3 || kind == 7 || kind == 8) span += op >> 4;
+        }
+        int64_t beg = pos, end = pos + (span > 0 ? span : 1);
+        uint32_t bin = (uint32_t)reg2bin(beg, end);
+        if (tid != cur_tid) {
+            flush(cur_tid);
+            cur_tid = tid;
+            save_bin = 0xffffffffu;
+        }
+        if (bin != save_bin) {
+            flush(tid);
+            save_bin = bin;
+            save_off = v0;
+        }
+        last_off = v1;
+        auto &rf = refs[tid];
+        for (int64_t w = beg >> 14; w <= (end - 1) >> 14; ++w) {
+            if ((int64_t)rf.lidx.size() <= w) rf.lidx.resize(w + 1, -1);
+            if (rf.lidx[w] < 0) rf.lidx[w] = (int64_t)v0;
+        }
+        rf.any = true;
+        rf.beg = std::min(rf.beg, v0);
+        rf.end = std::max(rf.end, v1);
+        if (flag & 4) ++rf.unmapped;
+        else ++rf.mapped;
+        at = end_at;
+    }
+    flush(cur_tid);
+    std::vector<uint8_t> o = {'B', 'A', 'I', 1};
+    put32(o, (uint32_t)n_ref);
+    auto put64 = [&](uint64_t v) {
+        put32(o, (uint32_t)v);
+        put32(o, (uint32_t)(v >> 32));
+    };
+    for (auto &rf : refs) {
+        put32(o, (uint32_t)(rf.bins.size() + (rf.any ? 1 : 0)));
+        for (auto &b : rf.bins) {
+            put32(o, b.first);
+            put32(o, (uint32_t)b.second.size());
+            for (auto &c : b.second) {
+                put64(c.first);
+                put64(c.second);
+            }
+        }
+        if (rf.any) {
+            put32(o, 37450);
+            put32(o, 2);
+            put64(rf.beg);
+            put64(rf.end);
+            put64(rf.mapped);
+            put64(rf.unmapped);
+        }
+        // gaps take the next window's offset
+        int64_t next = rf.lidx.empty() ? 0 : rf.lidx.back();
+        for (size_t w = rf.lidx.size(); w-- > 0;) {
+            if (rf.lidx[w] < 0) rf.lidx[w] = next;
+            else next = rf.lidx[w];
+        }
+        put32(o, (uint32_t)rf.lidx.size());
+        for (int64_t v : rf.lidx) put64((uint64_t)v);
+    }
+    put64(n_no_coor);
+    uint8_t *buf = (uint8_t *)malloc(o.size());
+    if (!buf) return -3;
+    memcpy(buf, o.data(), o.size());
+    *out = buf;
+    *out_len = o.size();
+    return 0;
+}
+
 void frt_synth_free(void *p) { free(p); }
 
 } // extern "C"

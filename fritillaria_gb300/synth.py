@@ -42,6 +42,7 @@ def _load():
         _lib.frt_synth_bgzf.argtypes = [C.c_void_p, C.c_size_t, C.c_int, C.c_uint32, C.c_void_p, C.c_size_t,
                                         C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.frt_synth_free.argtypes = [C.c_void_p]
+        _lib.frt_synth_bai.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]
         _lib.frt_synth_fastq.argtypes = [C.c_int, C.c_uint64, C.c_uint64, C.c_int, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_void_p]
         _lib.frt_synth_bcf.argtypes = [C.c_uint64, C.c_uint32, C.c_int, C.c_uint64, C.c_int, C.c_void_p,
@@ -110,6 +111,20 @@ def ultra_long_bam(n_records: int, n_long_extra: int = 0, seed: int = 3, levels=
                    member_payload: int = 65495):
     raw, ends = raw_bam("ultra_long", n_records, 1, 0, seed, n_long_extra)
     return raw, bgzf(raw, packing, levels, ends, member_payload)
+
+
+def bai(raw: np.ndarray, bgzf_bytes: np.ndarray) -> np.ndarray:
+    """A BAI for a coordinate-sorted BAM: `raw` its uncompressed bytes,
+    `bgzf_bytes` the BGZF file they were written as."""
+    lib = _load()
+    raw = np.ascontiguousarray(raw, dtype=np.uint8)
+    bg = np.ascontiguousarray(bgzf_bytes, dtype=np.uint8)
+    out = C.c_void_p()
+    n = C.c_size_t()
+    rc = lib.frt_synth_bai(raw.ctypes.data, raw.size, bg.ctypes.data, bg.size, C.byref(out), C.byref(n))
+    if rc != 0:
+        raise ValueError(f"BAI generation failed ({rc})")
+    return _take(out, n.value)
 
 
 def _with_ends(fn, *args):

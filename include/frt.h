@@ -325,6 +325,89 @@ int frt_columns_column_to_host(const frt_columns *c, int column, void *dst, size
 void *frt_columns_ready_event(const frt_columns *c);
 void frt_columns_free(frt_columns *c);
 
+/* ---- BAI region resolution -------------------------------------------------
+ * The index (crates/fritillaria-bam/src/bai.rs, the csi BinningIndex) turns a
+ * region into chunks of virtual offsets: a record is in the query when its
+ * start virtual offset lies in a chunk and it overlaps the region. */
+typedef struct frt_bai frt_bai;
+typedef struct {
+    uint64_t start; /* virtual offset: compressed member offset << 16 | in-member offset */
+    uint64_t end;
+} frt_chunk;
+
+/* Reads a BAI (SAM specification 5.2). */
+int frt_bai_parse(const uint8_t *buf, size_t len, frt_bai **out, frt_error *err);
+void frt_bai_free(frt_bai *bai);
+int32_t frt_bai_reference_count(const frt_bai *bai);
+/* BinningIndex::query (crates/fritillaria-csi/src/binning_index/index.rs:93-119)
+ * for [start, end], 1-based inclusive (0 start/end: unbounded).  *n receives
+ * the chunk count; FRT_ERR_INVALID_ARGUMENT when it exceeds cap. */
+int frt_bai_query(const frt_bai *bai, int32_t ref, uint64_t start, uint64_t end, frt_chunk *out, size_t cap,
+                  size_t *n, frt_error *err);
+
+/* ---- region serving ----------------------------------------------------------
+ * No reference counterpart as a server: the reference answers one region at a
+ * time through its indexed reader (crates/fritillaria-bam/src/io/reader/query.rs).
+ * Here BAMs with their BAIs are resident in device memory; region queries are
+ * resolved to chunks on the host, and every request admitted within the HBM
+ * budget since the last tick is served by one persistent inflate over all their
+ * members plus one segmented record scan and region filter, without blocking the
+ * caller.  A request's results are the records the reference's query yields
+ * (start virtual offset inside a chunk, reference and interval overlap), in file
+ * order, as device columns that stay resident until released. */
+typedef struct frt_server frt_server;
+
+typedef enum {
+    FRT_REGION_COL_VIRTUAL_OFFSET = 0, /* u64 */
+    FRT_REGION_COL_RECORD_OFFSET = 1,  /* u64, into the request's inflated bytes */
+    FRT_REGION_COL_REF_ID = 2,         /* i32 */
+    FRT_REGION_COL_POS = 3,            /* i32, 0-based */
+    FRT_REGION_COL_FLAGS = 4,          /* u16 */
+    FRT_REGION_COL_MAPQ = 5,           /* u8 */
+    FRT_REGION_COL_SEQ_LEN = 6,        /* u32 */
+    FRT_REGION_COL_COUNT = 7
+} frt_region_column;
+
+typedef struct {
+    int32_t state;  /* 0 queued, 1 running, 2 done */
+    int32_t status; /* frt_status once done */
+    uint64_t records;
+    double arrival_ms, done_ms; /* server clock: frt_server_clock_ms; done from the device's completion event */
+    uint64_t inflated_bytes;
+    uint32_t chunks;
+    uint64_t members;
+    uint32_t retries; /* re-reads with more trailing members for a record cut at the chunk end */
+} frt_region_info;
+
+/* `budget_bytes` bounds the device memory of admitted requests (their inflated
+ * bytes, scan scratch and results, held until released). */
+int frt_server_create(int device, void *stream, uint64_t budget_bytes, frt_server **out, frt_error *err);
+void frt_server_destroy(frt_server *s);
+/* 0 for either limit: no limit on requests per tick; 1 tick in flight. */
+void frt_server_set_limits(frt_server *s, uint32_t max_requests_per_tick, uint32_t max_ticks_in_flight);
+/* Milliseconds since the server was created (the clock of arrival_ms/done_ms). */
+double frt_server_clock_ms(const frt_server *s);
+/* Makes a BGZF BAM and its BAI resident (before the first request). */
+int frt_server_add_bam(frt_server *s, const uint8_t *bgzf, size_t len, const uint8_t *bai, size_t bai_len,
+                       int32_t *file_id, frt_error *err);
+/* Queues [start, end] (1-based inclusive; 0 = unbounded) on reference `ref`.
+ * arrival_ms < 0 stamps the request now. */
+int frt_server_submit(frt_server *s, int32_t file, int32_t ref, uint64_t start, uint64_t end, double arrival_ms,
+                      uint64_t *request, frt_error *err);
+/* Completes finished ticks and launches new ones; never waits on the device. */
+int frt_server_progress(frt_server *s, uint32_t *completed, frt_error *err);
+/* Waits until every submitted request has completed. */
+int frt_server_drain(frt_server *s, frt_error *err);
+int frt_server_request_info(const frt_server *s, uint64_t request, frt_region_info *info);
+int frt_server_request_error(const frt_server *s, uint64_t request, frt_error *err);
+int frt_server_request_column(const frt_server *s, uint64_t request, int column, void **ptr, size_t *bytes,
+                              size_t *width);
+int frt_server_request_column_to_host(const frt_server *s, uint64_t request, int column, void *dst, size_t cap,
+                                      frt_error *err);
+/* The request's inflated bytes (device), which FRT_REGION_COL_RECORD_OFFSET indexes. */
+const uint8_t *frt_server_request_inflated(const frt_server *s, uint64_t request, size_t *len);
+void frt_server_release(frt_server *s, uint64_t request);
+
 /* ---- batched, device-resident form ---------------------------------------
  * No reference counterpart: the batched launch model.  Members of a whole
  * BGZF file resident in device memory are discovered, inflated, verified,
