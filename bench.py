@@ -65,6 +65,18 @@ MIXED = {
                                 desc="the mixed-format workload at one tenth size (profiling size)"),
 }
 
+# Region serving: BAI-indexed BAMs resident on the device, a Poisson stream of
+# region queries, continuous batching into shared persistent inflates.
+SERVING = {
+    "serving": dict(files=32, min_records=50_000, max_records=2_500_000, rate=2000.0, requests=4000,
+                    plain_requests=300, budget=150 << 30,
+                    desc="32 BAI-indexed short-read BAMs (24 contigs, 3.1 Gb; record counts log-uniform "
+                         "50k-2.5M, one twentieth of 1M-50M), Poisson arrivals at 2,000 req/s, regions on a "
+                         "random contig with uniform start and log-uniform length 1 kb-10 Mb, 150 GB budget"),
+    "serving_small": dict(files=8, min_records=20_000, max_records=200_000, rate=2000.0, requests=800,
+                          plain_requests=100, budget=150 << 30, desc="the serving workload at test size"),
+}
+
 METRIC = "BAM->device-column decompressed GB/s, batched vs plain, 1 GB300, bit-exact"
 
 
@@ -74,7 +86,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(MIXED), default="short_reads_20m")
+    p.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(MIXED) + sorted(SERVING), default="short_reads_20m")
     p.add_argument("--no-plain", action="store_true", help="skip the per-batch comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     return p.parse_args()
@@ -204,6 +216,37 @@ def run_reference(args, rank, world):
     from oracle import oracle
 
     threads = os.cpu_count() or 1
+    if args.workload in SERVING:
+        import numpy as np
+
+        from oracle import bai as obai
+
+        w = SERVING[args.workload]
+        files, reqs = generate_serving(args.workload)
+        idx = [obai.parse(x) for _, x, _ in files]
+        spans = [oracle.discover(b)[0] for b, _, _ in files]
+        sample = reqs[: w["plain_requests"]]
+        svc, nbytes = [], 0
+        for a, f, ref, s0, e0 in sample:
+            t = time.perf_counter()
+            _, nb = oracle.region_query(files[f][0], spans[f], idx[f], ref, s0, e0)
+            svc.append(1e3 * (time.perf_counter() - t))
+            nbytes += nb
+        total_s = sum(svc) / 1e3
+        line = {"impl": "reference", "metric": METRIC, "value": round(nbytes / total_s / 1e9, 3), "unit": "GB/s",
+                "n_gpus": args.gpus, "steps": 1, "warmup": 0, "ms_per_step": round(1e3 * total_s, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+                "config": {"workload": args.workload, "description": w["desc"], "requests": len(sample)},
+                "serving": {"requests_per_s": round(len(sample) / total_s, 1),
+                            "service_p50_ms": round(float(np.percentile(svc, 50)), 3),
+                            "service_p99_ms": round(float(np.percentile(svc, 99)), 3)},
+                "cpu_baseline": {"value": round(nbytes / total_s / 1e9, 3), "unit": "GB/s", "cores": 1, "kind": "port",
+                                 "sample": f"the first {len(sample)} requests of the stream, served one at a time: "
+                                           "BAI chunks, zlib inflate of the chunk members, record scan and filter"},
+                "e2e": {"value": round(nbytes / total_s / 1e9, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     if args.workload in MIXED:
         files = generate_mixed(args.workload)
         fmt = {"bcf": 1, "fastq": 2, "fasta": 3}
@@ -566,6 +609,126 @@ def run_mixed(args, rank, world, local):
         dist.destroy_process_group()
 
 
+def generate_serving(name: str):
+    """Files (bgzf, bai, contig lengths) and the request stream."""
+    import numpy as np
+
+    from fritillaria_gb300 import synth
+
+    w = SERVING[name]
+    rng = np.random.default_rng(2024)
+    lo, hi = np.log(w["min_records"]), np.log(w["max_records"])
+    sizes = np.exp(rng.uniform(lo, hi, w["files"])).astype(np.int64)
+    files = []
+    for i, n in enumerate(sizes):
+        raw, bgzf = synth.short_read_bam(int(n), n_contigs=24, genome_len=3_100_000_000, seed=300 + i, levels=(1, 6))
+        files.append((bgzf, synth.bai(raw, bgzf), int(n)))
+        del raw
+    # contig lengths of the generator (human proportions over 3.1 Gb)
+    human = np.array([248956422, 242193529, 198295559, 190214555, 181538259, 170805979, 159345973, 145138636,
+                      138394717, 133797422, 135086622, 133275309, 114364328, 107043718, 101991189, 90338345,
+                      83257441, 80373285, 58617616, 64444167, 46709983, 50818468, 156040895, 57227415], float)
+    contig_len = (3_100_000_000 * human / human.sum()).astype(np.int64)
+    n = w["requests"]
+    arrivals = np.cumsum(rng.exponential(1000.0 / w["rate"], n))  # ms
+    reqs = []
+    for k in range(n):
+        f = int(rng.integers(0, w["files"]))
+        ref = int(rng.integers(0, 24))
+        length = int(np.exp(rng.uniform(np.log(1_000), np.log(10_000_000))))
+        start = int(rng.integers(1, max(2, contig_len[ref] - length)))
+        reqs.append((float(arrivals[k]), f, ref, start, start + length - 1))
+    return files, reqs
+
+
+def serve_stream(frt, srv, ids, reqs):
+    """Submits each request at its arrival time and drives the server until
+    all complete; returns per-request (arrival, done, bytes, records)."""
+    t0 = srv.clock_ms()
+    rids, k = [], 0
+    while k < len(reqs):
+        now = srv.clock_ms() - t0
+        while k < len(reqs) and reqs[k][0] <= now:
+            a, f, ref, s, e = reqs[k]
+            rids.append(srv.submit(ids[f], ref, s, e, arrival_ms=t0 + a))
+            k += 1
+        srv.progress()
+    srv.drain()
+    out = []
+    for rid in rids:
+        srv.check(rid)
+        i = srv.info(rid)
+        out.append((i.arrival_ms, i.done_ms, i.inflated_bytes, i.records, i.retries))
+    for rid in rids:
+        srv.release(rid)
+    return out
+
+
+def latency_summary(rows):
+    import numpy as np
+
+    lat = np.array([d - a for a, d, _, _, _ in rows])
+    span = max(d for _, d, _, _, _ in rows) - min(a for a, _, _, _, _ in rows)
+    nbytes = sum(b for _, _, b, _, _ in rows)
+    return {"requests": len(rows), "p50_ms": round(float(np.percentile(lat, 50)), 3),
+            "p99_ms": round(float(np.percentile(lat, 99)), 3), "mean_ms": round(float(lat.mean()), 3),
+            "span_ms": round(span, 3), "inflated_bytes": int(nbytes),
+            "gbs": round(nbytes / (span / 1e3) / 1e9, 3) if span > 0 else None,
+            "records": int(sum(r for _, _, _, r, _ in rows)), "retries": int(sum(t for *_, t in rows)),
+            "completed_per_s": round(len(rows) / (span / 1e3), 1) if span > 0 else None}
+
+
+def run_serving(args, rank, world, local):
+    import torch
+
+    import fritillaria_gb300 as frt
+
+    torch.cuda.set_device(local)
+    w = SERVING[args.workload]
+    files, reqs = generate_serving(args.workload)
+    srv = frt.RegionServer(0, budget_bytes=w["budget"])
+    ids = [srv.add_bam(b, x) for b, x, _ in files]
+    # warm-up: a few requests through every stage
+    serve_stream(frt, srv, ids, [(0.0,) + r[1:] for r in reqs[: max(3, args.warmup)]])
+    with Clocks(local) as clocks:
+        t0 = time.perf_counter()
+        rows = serve_stream(frt, srv, ids, reqs)
+        wall = time.perf_counter() - t0
+    batched = latency_summary(rows)
+    # capacity: the whole stream offered at once
+    cap_rows = serve_stream(frt, srv, ids, [(0.0,) + r[1:] for r in reqs])
+    capacity = latency_summary(cap_rows)
+    # the plain per-request form: one request per tick, one tick in flight,
+    # the same arrivals (a prefix of the stream: it cannot keep up)
+    plain_srv = frt.RegionServer(0, budget_bytes=w["budget"])
+    plain_ids = [plain_srv.add_bam(b, x) for b, x, _ in files]
+    plain_srv.set_limits(1, 1)
+    serve_stream(frt, plain_srv, plain_ids, [(0.0,) + r[1:] for r in reqs[:3]])
+    prow = serve_stream(frt, plain_srv, plain_ids, reqs[: w["plain_requests"]])
+    plain = latency_summary(prow)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": batched["gbs"], "unit": "GB/s", "n_gpus": world, "steps": 1,
+            "warmup": args.warmup, "ms_per_step": batched["span_ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": args.workload, "description": w["desc"], "files": len(files),
+                       "records": int(sum(n for *_, n in files)),
+                       "compressed_bytes": int(sum(b.size for b, _, _ in files)),
+                       "offered_req_per_s": w["rate"], "budget_bytes": w["budget"],
+                       "l2": "region requests are independent (no flush)", "parallelism": f"replicas x{world}"},
+            "serving": {"batched": batched, "capacity": capacity, "plain_per_request": plain,
+                        "note": "latency = device completion of the request's tick - arrival; plain = one request "
+                                "per tick, one tick in flight, on the first requests of the same stream"},
+            "roofline": None, "cpu_baseline": None,
+            "e2e": {"value": batched["gbs"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                    "note": "files resident on the device; results stay on the device"},
+            "gpu_launches": None,
+            "clocks": clocks.summary(),
+            "wall_s": round(wall, 3),
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_setup(args.gpus)
@@ -574,6 +737,9 @@ def main():
         return
     if args.workload in MIXED:
         run_mixed(args, rank, world, local)
+        return
+    if args.workload in SERVING:
+        run_serving(args, rank, world, local)
         return
     run_ours(args, rank, world, local)
 

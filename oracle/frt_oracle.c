@@ -691,3 +691,38 @@ int orc_baseline_file(const uint8_t *file, size_t len, int format, int threads, 
     free(spans);
     return status;
 }
+
+
+/* The reference's indexed query over one chunk, on the host: records of the
+ * chain from `start` that begin before `chunk_end` (offsets in the inflated
+ * chunk), kept when on reference `ref` their [pos + 1, pos + span] meets
+ * [beg, end] (crates/fritillaria-bam/src/io/reader/query.rs:97-122; span from
+ * the CIGAR's M/D/N/=/X, at least 1).  Writes kept record offsets; returns
+ * their count. */
+uint64_t orc_region_records(const uint8_t *buf, uint64_t len, uint64_t start, uint64_t chunk_end, int32_t ref,
+                            uint64_t beg, uint64_t end, uint64_t *out, uint64_t cap)
+{
+    uint64_t pos = start, n = 0;
+    while (pos < chunk_end && pos + 4 <= len) {
+        uint32_t bs = rd32(buf + pos);
+        if (bs < 32 || pos + 4 + (uint64_t)bs > len) break;
+        const uint8_t *r = buf + pos;
+        int32_t rid = (int32_t)rd32(r + 4), p = (int32_t)rd32(r + 8);
+        if (rid == ref && p >= 0) {
+            uint32_t name_len = r[12], n_cigar = rd16(r + 16);
+            uint64_t span = 0;
+            for (uint32_t k = 0; k < n_cigar; ++k) {
+                uint32_t op = rd32(r + 36 + name_len + 4 * k), kind = op & 15u;
+                if (kind == 0 || kind == 2 || kind == 3 || kind == 7 || kind == 8) span += op >> 4;
+            }
+            if (!span) span = 1;
+            uint64_t a0 = (uint64_t)p + 1, a1 = a0 + span - 1;
+            if (a0 <= end && beg <= a1) {
+                if (n < cap) out[n] = pos;
+                ++n;
+            }
+        }
+        pos += 4 + (uint64_t)bs;
+    }
+    return n;
+}

@@ -124,6 +124,9 @@ typedef struct {
 
 int orc_baseline_bam(const uint8_t *file, size_t len, int threads, uint64_t max_members,
                      orc_baseline_result *res);
+/* Records of one BAI chunk that a region query keeps (see frt_oracle.c). */
+uint64_t orc_region_records(const uint8_t *buf, uint64_t len, uint64_t start, uint64_t chunk_end, int32_t ref,
+                            uint64_t beg, uint64_t end, uint64_t *out, uint64_t cap);
 /* The same for a bgzipped BCF (1), FASTQ (2) or FASTA (3) file. */
 int orc_baseline_file(const uint8_t *file, size_t len, int format, int threads, orc_baseline_result *res);
 

@@ -54,6 +54,9 @@ def lib():
         _lib.orc_bam_aux.argtypes = [_P, C.c_uint32, C.c_uint32, _P, C.c_uint32, _P]
         _lib.orc_baseline_bam.argtypes = [_P, C.c_size_t, C.c_int, C.c_uint64, _P]
         _lib.orc_baseline_file.argtypes = [_P, C.c_size_t, C.c_int, C.c_int, _P]
+        _lib.orc_region_records.restype = C.c_uint64
+        _lib.orc_region_records.argtypes = [_P, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int32, C.c_uint64, C.c_uint64,
+                                            _P, C.c_uint64]
         _lib.orc_fastq_scan.argtypes = [_P, C.c_uint64, C.c_uint64, _P, C.c_size_t, _P, _P, _P, _P]
         _lib.orc_fastq_decode.argtypes = [_P, C.c_uint64, _P, C.c_size_t, _P, _P, _P, _P, _P]
         _lib.orc_bcf_header.argtypes = [_P, C.c_uint64, _P, _P, _P, _P]
@@ -360,3 +363,26 @@ def fasta_compact(buf) -> dict:
     k = n.value
     return {"sequence": seq[: total.value], "sequence_offsets": so[:k].copy(), "sequence_lengths": sl[:k].copy(),
             "record_offsets": ro[:k].copy(), "bounds": bounds[:k].copy()}
+
+
+def region_query(bgzf, spans, index, ref: int, start: int, end: int):
+    """The reference's indexed region query on the host: the BAI's chunks,
+    each chunk's members inflated with zlib (plus the members a record
+    starting in the chunk runs into), the chunk's records scanned and
+    filtered.  Returns (kept record count, inflated bytes)."""
+    from oracle import bai as obai
+
+    coff = spans["compressed_offset"].astype(np.uint64)
+    kept, inflated = 0, 0
+    for c0, c1 in obai.query(index, ref, start, end or obai.MAX_POSITION):
+        ma = int(np.searchsorted(coff, np.uint64(c0 >> 16), "right")) - 1
+        me = int(np.searchsorted(coff, np.uint64(c1 >> 16), "right")) - 1
+        mz = min(len(spans) - 1, me + 1)
+        data, offs = inflate_batch(bgzf, spans[ma: mz + 1])
+        inflated += data.size
+        s0 = int(c0 & 0xFFFF)
+        e0 = int(offs[me - ma]) + int(c1 & 0xFFFF)
+        out = np.zeros(1, np.uint64)
+        kept += lib().orc_region_records(_ptr(data), data.size, s0, e0, ref, start, end or obai.MAX_POSITION,
+                                         _ptr(out), 0)
+    return kept, inflated

@@ -95,3 +95,17 @@ def test_index_and_query_errors(frt):
         b.query(0, 1 << 30, (1 << 30) + 5)
     with pytest.raises(frt.InvalidArgument):
         b.query(0, 500, 100)
+
+
+def test_host_region_query_matches_brute_force():
+    raw, bgzf = synth.short_read_bam(20_000, n_contigs=24, genome_len=100_000_000, seed=12)
+    idx = obai.parse(synth.bai(raw, bgzf))
+    spans = oracle.discover(bgzf)[0]
+    t = _table(bgzf)
+    rng = np.random.default_rng(6)
+    for _ in range(60):
+        ref = int(rng.integers(0, 24))
+        s = int(rng.integers(1, 3_000_000))
+        e = s + int(rng.integers(1_000, 2_000_000))
+        kept, _ = oracle.region_query(bgzf, spans, idx, ref, s, e)
+        assert kept == len(obai.brute_force(t, ref, s, e))
