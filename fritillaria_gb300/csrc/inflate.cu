@@ -38,10 +38,45 @@ constexpr int LIT_BITS = INF_LIT_BITS;
 constexpr int DIST_BITS = INF_DIST_BITS;
 constexpr int CL_BITS = 7;
 constexpr u32 DIST_BASE = 1u << LIT_BITS; // distance entries follow the literal/length ones
+constexpr u32 LIT_MASK = (1u << LIT_BITS) - 1u;
+constexpr u32 DIST_MASK = (1u << DIST_BITS) - 1u;
+// After a refill the buffer holds at least 33 bits: enough for a length
+// whose code and extra bits fit the root plus a distance whose code fits its
+// root (at most 13 extra bits), so a fast match needs no second refill.
+static_assert(LIT_BITS + DIST_BITS + 13 <= 33, "a fast match must fit one refill");
 constexpr u32 WB = INF_WINBUF;            // window output buffer (bytes)
 constexpr u32 MAXQ = INF_MAXQ;            // matches per window
 static_assert(MAXQ <= 32 * 32, "a lane tracks at most 32 queued matches");
 static_assert(WB % 32 == 0, "pending bits cover whole words");
+
+// CRC-32 tables, computed at compile time: slice[k][b] is the register that
+// byte b followed by k zero bytes leaves from zero (slicing by 4; slice[0] is
+// the byte table), xpow[m] = x^(8m) mod P in the reflected order the
+// registers use (bit 31 is x^0), for every window length.
+struct CrcTables {
+    u32 slice[4][256];
+    u32 xpow[WB + 1];
+};
+
+constexpr CrcTables make_crc_tables()
+{
+    CrcTables t{};
+    for (u32 i = 0; i < 256; ++i) {
+        u32 c = i;
+        for (int k = 0; k < 8; ++k) c = (c >> 1) ^ (0xEDB88320u & (0u - (c & 1u)));
+        t.slice[0][i] = c;
+    }
+    for (int k = 1; k < 4; ++k)
+        for (u32 i = 0; i < 256; ++i) t.slice[k][i] = (t.slice[k - 1][i] >> 8) ^ t.slice[0][t.slice[k - 1][i] & 0xffu];
+    u32 v = 0x80000000u;
+    for (u32 m = 0; m <= WB; ++m) {
+        t.xpow[m] = v;
+        for (int k = 0; k < 8; ++k) v = (v >> 1) ^ (0xEDB88320u & (0u - (v & 1u)));
+    }
+    return t;
+}
+
+__device__ const CrcTables g_crc = make_crc_tables();
 
 struct CodeState {
     u32 count[16];
@@ -52,13 +87,15 @@ struct CodeState {
 // Decode-table entries (32 bits), so one lookup and one shift take a symbol
 // with its extra bits:
 //   [4:0]   bits to consume: the code plus its extra bits
-//   [7:5]   kind: 0 literal (or a valid distance), 1 length, 2 end of block,
-//           3 invalid symbol
+//   [7:5]   kind: 0 literal (or a valid distance), 1 length resolved in the
+//           table (its extra bits were part of the index), 2 end of block,
+//           3 invalid symbol, 4 length whose extra bits are read at decode
+//           time, 7 no code of at most the root length matches (the
+//           long-code path)
 //   [11:8]  the code's own length (where its extra bits start)
 //   [15:12] extra bits
-//   [31:16] literal byte, or length/distance base
-// An entry of 0 means no code of at most the root length matches: the
-// long-code path.
+//   [31:16] literal byte, resolved length, or length/distance base
+// The code-length code's table marks a missing code with 0 instead.
 struct WarpSmem {
     u32 tab[DIST_BASE + (1u << DIST_BITS)];
     CodeState lcode;
@@ -70,7 +107,7 @@ struct WarpSmem {
     u32 q_dst[MAXQ];      // matches of the window: destination (member offset)
     u32 q_ld[MAXQ];       //   len | dist << 9
     u8 lens[320];
-    u8 win[WB + 264];
+    alignas(16) u8 win[WB + 264];
 };
 
 __device__ __forceinline__ u32 lit_entry(u32 sym, u32 L)
@@ -89,7 +126,7 @@ __device__ __forceinline__ u32 lit_entry(u32 sym, u32 L)
         extra = (i - 4) >> 2;
         base = ((4u + (i & 3u)) << extra) + 3u;
     }
-    return (L + extra) | (1u << 5) | (L << 8) | (extra << 12) | (base << 16);
+    return (L + extra) | (4u << 5) | (L << 8) | (extra << 12) | (base << 16);
 }
 
 __device__ __forceinline__ u32 dist_entry(u32 sym, u32 L)
@@ -158,10 +195,19 @@ __device__ int build_table(const u8 *lens, int n, int root, u32 *table, u16 *sor
 #pragma unroll
         for (int l = 1; l < 16; ++l)
             if (l <= root) L += (v >= lim[l]) ? 1u : 0u;
-        u32 entry = 0;
+        u32 entry = kind == 2 ? 0u : (7u << 5);
         if ((int)L <= root) {
             u32 sym = sorted[cs->offs[L] + ((v >> (root - L)) - cs->first[L])];
-            entry = kind == 0 ? lit_entry(sym, L) : (kind == 1 ? dist_entry(sym, L) : cl_entry(sym, L));
+            if (kind == 0) {
+                entry = lit_entry(sym, L);
+                // a length whose extra bits also fit the root: the index holds
+                // them (they follow the code in the stream), so resolve it here
+                const u32 x = (entry >> 12) & 15u;
+                if (((entry >> 5) & 7u) == 4u && L + x <= (u32)root)
+                    entry = (L + x) | (1u << 5) | (((entry >> 16) + (((u32)e >> L) & ((1u << x) - 1u))) << 16);
+            } else {
+                entry = kind == 1 ? dist_entry(sym, L) : cl_entry(sym, L);
+            }
         }
         table[e] = entry;
     }
@@ -311,29 +357,158 @@ __device__ void resolve(WarpSmem *sm, const u8 *out, u32 wstart, u32 nq)
 }
 
 // Writes the window's n bytes to out[wstart, wstart + n) with coalesced
-// stores and folds their CRC into *crc: 32 slices from shared memory, merged
-// pairwise by the GF(2) combine.
-__device__ void write_window(const WarpSmem *sm, u8 *out, u32 wstart, u32 n, const u32 *crc_tab, u32 *crc)
+// stores and advances the member's CRC-32 over them.  The CRC register is
+// linear in (state, data): the register after A||B is the register after A
+// shifted by |B| bytes (times x^(8|B|) mod P) XOR the register B alone
+// produces from zero.  So lane 0 runs the first slice from the member's
+// register, every other lane its slice from zero (slicing by 4), each lane
+// shifts its result past the bytes after its slice with one multiply by a
+// tabulated power, and an XOR across the warp gives the new register.
+__device__ void write_window(const WarpSmem *sm, u8 *out, u32 wstart, u32 n, u32 *crc)
 {
     const u32 lane = lane_id();
     for (u32 j = lane; j < n; j += 32) out[wstart + j] = sm->win[j];
-    u32 slice = (n + 31) / 32;
-    u32 b0 = min(n, lane * slice), b1 = min(n, b0 + slice);
-    u32 c = 0xffffffffu;
-    for (u32 i = b0; i < b1; ++i) c = crc_tab[(c ^ sm->win[i]) & 0xffu] ^ (c >> 8);
-    c = ~c;
-    u32 mylen = b1 - b0;
-    for (int d = 1; d < 32; d <<= 1) {
-        u32 oc = __shfl_down_sync(FRT_FULL_MASK, c, d);
-        u32 ol = __shfl_down_sync(FRT_FULL_MASK, mylen, d);
-        if ((lane & (2 * d - 1)) == 0 && lane + d < 32) {
-            c = crc_combine(c, oc, ol);
-            mylen += ol;
-        }
+    const u32 s = ((n + 31u) / 32u + 3u) & ~3u; // slice length, whole words
+    const u32 b0 = min(n, lane * s), b1 = min(n, b0 + s);
+    u32 c = lane == 0 ? ~*crc : 0u;
+    u32 i = b0;
+    for (; i + 4u <= b1; i += 4u) {
+        c ^= *(const u32 *)(sm->win + i);
+        c = g_crc.slice[3][c & 0xffu] ^ g_crc.slice[2][(c >> 8) & 0xffu] ^ g_crc.slice[1][(c >> 16) & 0xffu] ^
+            g_crc.slice[0][c >> 24];
     }
-    c = __shfl_sync(FRT_FULL_MASK, c, 0);
-    *crc = crc_combine(*crc, c, n);
+    for (; i < b1; ++i) c = g_crc.slice[0][(c ^ sm->win[i]) & 0xffu] ^ (c >> 8);
+    c = gf2_mulmod(g_crc.xpow[n - b1], c);
+#pragma unroll
+    for (int d = 16; d; d >>= 1) c ^= __shfl_xor_sync(FRT_FULL_MASK, c, d);
+    *crc = ~c;
     __syncwarp();
+}
+
+// The common symbols, decoded with as little control flow as possible: on
+// GB300 lane 0's chain is bound by dependent instructions (about 5.5 cycles
+// each), and the SIMT reconvergence bookkeeping that nested branches and
+// breaks cost per symbol made up a third of them.  Takes literals and
+// lengths resolved in the table, with distances whose code fits the distance
+// root, while every symbol is sure to fit (o < lim, and a match adds at most
+// 258 bytes); stops in front of any other symbol, which slow_symbol then
+// decodes, and leaves a distance it rejects to slow_symbol as well.  One
+// exit test at the bottom of the loop, and the refill takes a word loaded
+// one refill earlier, so its load latency is off the chain.
+__device__ __forceinline__ void fast_run(WarpSmem *sm, LaneBits &r, u32 pos, u32 lim, u32 &o_io, u32 &nq_io)
+{
+    u64 buf = r.buf;
+    int cnt = r.cnt;
+    u32 nw = r.nw, o = o_io, nq = nq_io;
+    const u32 *tab = sm->tab;
+    u32 nextw = r.word(nw); // loaded one refill ahead
+    bool go;
+    do {
+        if (cnt <= 32) {
+            buf |= (u64)nextw << cnt;
+            cnt += 32;
+            ++nw;
+            nextw = r.word(nw);
+        }
+        const u32 e = tab[(u32)buf & LIT_MASK];
+        go = false;
+        if ((e & 0xE0u) == 0u) { // literal
+            sm->win[o++] = (u8)(e >> 16);
+            buf >>= (e & 31u);
+            cnt -= (int)(e & 31u);
+            go = true;
+        } else if ((e & 0xE0u) == 0x20u) { // resolved length
+            const u64 b2 = buf >> (e & 31u);
+            const u32 d = tab[DIST_BASE + ((u32)b2 & DIST_MASK)];
+            const u32 lo = (u32)b2;
+            const u32 dist = (d >> 16) + ((lo >> ((d >> 8) & 15u)) & ((1u << ((d >> 12) & 15u)) - 1u));
+            const u32 dst = pos + o;
+            if ((d & 0xE0u) == 0u && dist <= dst) {
+                buf = b2 >> (d & 31u);
+                cnt -= (int)((e & 31u) + (d & 31u));
+                const u32 len = e >> 16;
+                sm->q_dst[nq] = dst;
+                sm->q_ld[nq] = len | (dist << 9);
+                ++nq;
+                o += len;
+                go = nq < MAXQ;
+            }
+        }
+    } while (go && o < lim);
+    r.buf = buf;
+    r.cnt = cnt;
+    r.nw = nw;
+    o_io = o;
+    nq_io = nq;
+}
+
+// One symbol (a literal, or a length with its distance) with every check,
+// in the order of the reference kernel.  Returns 0 to go on, 1 at the end of
+// the block, 2 on an error (status set).
+__device__ __forceinline__ int slow_symbol(WarpSmem *sm, LaneBits &r, u32 pos, u32 cap, u32 &o, u32 &nq, u32 &status)
+{
+    r.refill();
+    u32 e = sm->tab[(u32)r.buf & LIT_MASK];
+    if (((e >> 5) & 7u) == 7u) {
+        u32 sym, L = decode_long(r.buf, LIT_BITS, &sm->lcode, sm->lsorted, &sym);
+        if (L == 0) {
+            r.drop(15); // the reference reads 15 bits before giving up
+            status = INF_BAD_CODE;
+            return 2;
+        }
+        e = lit_entry(sym, L);
+    }
+    const u32 kind = (e >> 5) & 7u;
+    if (kind == 0) {
+        if (pos + o >= cap) {
+            status = INF_OUTPUT_OVERFLOW;
+            return 2;
+        }
+        sm->win[o++] = (u8)(e >> 16);
+        r.drop((int)(e & 31u));
+        return 0;
+    }
+    if (kind == 2 || kind == 3) {
+        r.drop((int)(e & 31u));
+        if (kind == 2) return 1;
+        status = INF_BAD_CODE;
+        return 2;
+    }
+    u32 len = e >> 16;
+    if (kind == 4) len += (u32)(r.buf >> ((e >> 8) & 15u)) & ((1u << ((e >> 12) & 15u)) - 1u);
+    r.drop((int)(e & 31u));
+    r.refill();
+    u32 d = sm->tab[DIST_BASE + ((u32)r.buf & DIST_MASK)];
+    if (((d >> 5) & 7u) == 7u) {
+        u32 sym, L = decode_long(r.buf, DIST_BITS, &sm->dcode, sm->dsorted, &sym);
+        if (L == 0) {
+            r.drop(15);
+            status = INF_BAD_DISTANCE;
+            return 2;
+        }
+        d = dist_entry(sym, L);
+    }
+    if ((d >> 5) & 7u) {
+        r.drop((int)(d & 31u));
+        status = INF_BAD_DISTANCE;
+        return 2;
+    }
+    u32 dist = (d >> 16) + ((u32)(r.buf >> ((d >> 8) & 15u)) & ((1u << ((d >> 12) & 15u)) - 1u));
+    r.drop((int)(d & 31u));
+    const u32 dst = pos + o;
+    if (dist > dst) {
+        status = INF_BAD_DISTANCE;
+        return 2;
+    }
+    if (dst + len > cap) {
+        status = INF_OUTPUT_OVERFLOW;
+        return 2;
+    }
+    sm->q_dst[nq] = dst;
+    sm->q_ld[nq] = len | (dist << 9);
+    ++nq;
+    o += len;
+    return 0;
 }
 
 // One window of a Huffman block.  Lane 0 walks the serial chain -- one
@@ -343,76 +518,25 @@ __device__ void write_window(const WarpSmem *sm, u8 *out, u32 wstart, u32 n, con
 // and writes the window to HBM with its CRC.  Truncation is checked once per
 // burst: bits past the payload read as zero, and a symbol that used one is
 // where a sequential decoder reports it.
-__device__ u32 decode_burst(WarpSmem *sm, LaneBits &r, u32 total, u8 *out, u32 *pos_io, u32 cap, const u32 *crc_tab,
-                            u32 *crc, int *eob_out)
+__device__ u32 decode_burst(WarpSmem *sm, LaneBits &r, u32 total, u8 *out, u32 *pos_io, u32 cap, u32 *crc,
+                            int *eob_out)
 {
     const u32 lane = lane_id();
     const u32 pos = *pos_io;
     u32 o = 0, nq = 0, status = INF_OK;
     int eob = 0;
     if (lane == 0) {
-        const bool checked = cap - pos < WB; // near the declared size: check every symbol
+        // below lim every symbol fits the window and the declared size
+        const u32 room = cap - pos;
+        const u32 lim = room >= WB ? WB - 258u : (room > 258u ? room - 258u : 0u);
         while (o < WB - 258u && nq < MAXQ) {
-            r.refill();
-            u32 e = sm->tab[(u32)r.buf & ((1u << LIT_BITS) - 1u)];
-            if (e == 0) {
-                u32 sym, L = decode_long(r.buf, LIT_BITS, &sm->lcode, sm->lsorted, &sym);
-                if (L == 0) {
-                    r.drop(15); // the reference reads 15 bits before giving up
-                    status = INF_BAD_CODE;
-                    break;
-                }
-                e = lit_entry(sym, L);
+            if (o < lim) {
+                fast_run(sm, r, pos, lim, o, nq);
+                if (o >= WB - 258u || nq >= MAXQ) break;
             }
-            const u32 kind = (e >> 5) & 7u;
-            if (kind == 0) {
-                if (checked && pos + o >= cap) {
-                    status = INF_OUTPUT_OVERFLOW;
-                    break;
-                }
-                sm->win[o++] = (u8)(e >> 16);
-                r.drop((int)(e & 31u));
-                continue;
-            }
-            if (kind != 1) {
-                r.drop((int)(e & 31u));
-                if (kind == 2) eob = 1;
-                else status = INF_BAD_CODE;
-                break;
-            }
-            u32 len = (e >> 16) + ((u32)(r.buf >> ((e >> 8) & 15u)) & ((1u << ((e >> 12) & 15u)) - 1u));
-            r.drop((int)(e & 31u));
-            r.refill();
-            u32 d = sm->tab[DIST_BASE + ((u32)r.buf & ((1u << DIST_BITS) - 1u))];
-            if (d == 0) {
-                u32 sym, L = decode_long(r.buf, DIST_BITS, &sm->dcode, sm->dsorted, &sym);
-                if (L == 0) {
-                    r.drop(15);
-                    status = INF_BAD_DISTANCE;
-                    break;
-                }
-                d = dist_entry(sym, L);
-            }
-            if ((d >> 5) & 7u) {
-                r.drop((int)(d & 31u));
-                status = INF_BAD_DISTANCE;
-                break;
-            }
-            u32 dist = (d >> 16) + ((u32)(r.buf >> ((d >> 8) & 15u)) & ((1u << ((d >> 12) & 15u)) - 1u));
-            r.drop((int)(d & 31u));
-            const u32 dst = pos + o;
-            if (dist > dst) {
-                status = INF_BAD_DISTANCE;
-                break;
-            }
-            if (checked && dst + len > cap) {
-                status = INF_OUTPUT_OVERFLOW;
-                break;
-            }
-            sm->q_dst[nq] = dst;
-            sm->q_ld[nq] = len | (dist << 9);
-            ++nq;
-            o += len;
+            const int rc = slow_symbol(sm, r, pos, cap, o, nq, status);
+            if (rc == 1) eob = 1;
+            if (rc != 0) break;
         }
         if (r.tell() > total) status = INF_TRUNCATED; // a symbol needed bits past the payload
     }
@@ -423,7 +547,7 @@ __device__ u32 decode_burst(WarpSmem *sm, LaneBits &r, u32 total, u8 *out, u32 *
     __syncwarp();
     if (status != INF_OK) return status;
     resolve(sm, out, pos, nq);
-    write_window(sm, out, pos, o, crc_tab, crc);
+    write_window(sm, out, pos, o, crc);
     *pos_io = pos + o;
     return INF_OK;
 }
@@ -432,8 +556,8 @@ __device__ u32 decode_burst(WarpSmem *sm, LaneBits &r, u32 total, u8 *out, u32 *
 
 // Inflates one member with the calling warp into out[0, cap).  Returns the
 // status; *produced_out and *crc_out are valid in every lane.
-__device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, void *smem_v, const u32 *crc_tab,
-                                   u32 *produced_out, u32 *crc_out)
+__device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, void *smem_v, u32 *produced_out,
+                                   u32 *crc_out)
 {
     WarpSmem *sm = (WarpSmem *)smem_v;
     const u32 lane = lane_id();
@@ -493,7 +617,7 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
                 u32 n = min(len, WB);
                 for (u32 j = lane; j < n; j += 32) sm->win[j] = src[j];
                 __syncwarp();
-                write_window(sm, out, pos, n, crc_tab, &crc);
+                write_window(sm, out, pos, n, &crc);
                 pos += n;
                 src += n;
                 len -= n;
@@ -618,7 +742,7 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
         if (lane == 0) r.seek(bitpos);
         while (true) {
             int eob = 0;
-            status = decode_burst(sm, r, total, out, &pos, cap, crc_tab, &crc, &eob);
+            status = decode_burst(sm, r, total, out, &pos, cap, &crc, &eob);
             if (status != INF_OK || eob) break;
         }
         if (status != INF_OK) break;
@@ -634,15 +758,6 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
 
 size_t frt_inflate_warp_smem() { return sizeof(WarpSmem); }
 
-__device__ __forceinline__ void init_crc_table(u32 *tab)
-{
-    for (u32 i = threadIdx.x; i < 256; i += blockDim.x) {
-        u32 c = i;
-        for (int k = 0; k < 8; ++k) c = (c >> 1) ^ (0xEDB88320u & (0u - (c & 1u)));
-        tab[i] = c;
-    }
-}
-
 #define WSM_BYTES ((sizeof(WarpSmem) + 15) & ~(size_t)15)
 
 // Plain form: one warp per member of this launch, members in span order.
@@ -651,15 +766,12 @@ k_inflate_members(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out, c
                   const u32 *out_cap, u32 *status, u32 *produced, u32 *crc, u32 n)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    u32 *crc_tab = (u32 *)smem;
-    init_crc_table(crc_tab);
-    __syncthreads();
     const u32 warp = threadIdx.x / 32;
-    void *wsm = smem + 1024 + warp * WSM_BYTES;
+    void *wsm = smem + warp * WSM_BYTES;
     u32 m = blockIdx.x * (blockDim.x / 32) + warp;
     if (m >= n) return;
     u32 p = 0, c = 0;
-    u32 st = inflate_member_warp(in + in_off[m], in_len[m], out + out_off[m], out_cap[m], wsm, crc_tab, &p, &c);
+    u32 st = inflate_member_warp(in + in_off[m], in_len[m], out + out_off[m], out_cap[m], wsm, &p, &c);
     if (lane_id() == 0) {
         status[m] = st;
         produced[m] = p;
@@ -679,11 +791,8 @@ k_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out
                      unsigned long long *block_err)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    u32 *crc_tab = (u32 *)smem;
-    init_crc_table(crc_tab);
-    __syncthreads();
     const u32 warp = threadIdx.x / 32;
-    void *wsm = smem + 1024 + warp * WSM_BYTES;
+    void *wsm = smem + warp * WSM_BYTES;
     u64 n64 = *n_ptr;
     const u32 n = (u32)(n64 < n_cap ? n64 : n_cap);
     if (chunk == 0) chunk = 1;
@@ -701,7 +810,7 @@ k_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out
             if (out_off[m] + cap > out_capacity) {
                 st = INF_OUTPUT_OVERFLOW; // sizes changed since the buffers were planned
             } else {
-                st = inflate_member_warp(in + in_off[m], in_len[m], out + out_off[m], cap, wsm, crc_tab, &p, &c);
+                st = inflate_member_warp(in + in_off[m], in_len[m], out + out_off[m], cap, wsm, &p, &c);
             }
             if (lane_id() == 0) {
                 status[m] = st;
@@ -718,9 +827,7 @@ k_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out
 // crates/fritillaria-cuda/kernels/crc32.cu:13-38), one warp per member.
 __global__ void k_crc32_members(const u8 *data, const u64 *offsets, const u32 *lengths, u32 *out, u32 n)
 {
-    __shared__ u32 tab[256];
-    init_crc_table(tab);
-    __syncthreads();
+    const u32 *tab = g_crc.slice[0];
     u32 m = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     if (m >= n) return;
     const u8 *p = data + offsets[m];
@@ -744,7 +851,7 @@ __global__ void k_crc32_members(const u8 *data, const u64 *offsets, const u32 *l
 }
 
 // ---- host launchers --------------------------------------------------------
-size_t frt_inflate_smem_bytes(int warps) { return 1024 + (size_t)warps * WSM_BYTES; }
+size_t frt_inflate_smem_bytes(int warps) { return (size_t)warps * WSM_BYTES; }
 
 cudaError_t frt_inflate_prepare()
 {

@@ -21,8 +21,8 @@
 #define INF_MAXQ 384
 #endif
 
-__device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, void *smem, const u32 *crc_tab,
-                                   u32 *produced_out, u32 *crc_out);
+__device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, void *smem, u32 *produced_out,
+                                   u32 *crc_out);
 
 size_t frt_inflate_warp_smem();
 
