@@ -78,6 +78,9 @@ SERVING = {
 }
 
 METRIC = "BAM->device-column decompressed GB/s, batched vs plain, 1 GB300, bit-exact"
+# Inflate tunings measured on GB300 (written by the autotuner, one entry per
+# device and workload class); a miss is tuned at start-up and added.
+TUNING_CACHE = ROOT / "fritillaria_gb300" / "inflate_tuning.json"
 
 
 def parse_args():
@@ -89,6 +92,9 @@ def parse_args():
     p.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(MIXED) + sorted(SERVING), default="short_reads_20m")
     p.add_argument("--no-plain", action="store_true", help="skip the per-batch comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    p.add_argument("--tuning-cache", default=str(TUNING_CACHE),
+                   help="JSON cache of inflate tunings (read, and written on a miss)")
+    p.add_argument("--retune", action="store_true", help="time the inflate tunings again even on a cache hit")
     return p.parse_args()
 
 
@@ -349,6 +355,9 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     eng = frt.BatchEngine(0, stream=stream.cuda_stream)
     eng.bind_bam(dev.data_ptr(), dev.numel())
+    # the inflate tuning for this device and workload (from the cache, or
+    # timed now); it also becomes the default the plain arm's codec starts from
+    tuning = eng.autotune(args.tuning_cache, force=args.retune)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             eng.run()
@@ -443,7 +452,8 @@ def run_ours(args, rank, world, local):
                        "aux_fields": st.aux_fields, "column_bytes": col_bytes, "speculation_fallbacks": st.fallbacks,
                        "l2": "inputs larger than L2 (no flush)", "queue": "sorted by compressed size",
                        "graph": True, "parallelism": f"replicas x{world}",
-                       "records_per_s": round(world * st.records * args.steps / (ms / 1e3), 1)},
+                       "records_per_s": round(world * st.records * args.steps / (ms / 1e3), 1),
+                       "tuning": tuning},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
@@ -500,6 +510,7 @@ def run_mixed(args, rank, world, local):
     torch.cuda.synchronize()
     eng = frt.BatchEngine(0, stream=stream.cuda_stream)
     eng.bind_files(dev.data_ptr(), dev.numel(), layout)
+    tuning = eng.autotune(args.tuning_cache, force=args.retune)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             eng.run()
@@ -596,7 +607,7 @@ def run_mixed(args, rank, world, local):
                        "compressed_bytes": int(blob.size), "inflated_bytes": int(inflated), "records": int(st.records),
                        "column_bytes": int(col_bytes), "files": per, "l2": "inputs larger than L2 (no flush)",
                        "queue": "sorted by compressed size", "graph": "discovery + plan + inflate",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}", "tuning": tuning},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
@@ -686,6 +697,14 @@ def run_serving(args, rank, world, local):
     torch.cuda.set_device(local)
     w = SERVING[args.workload]
     files, reqs = generate_serving(args.workload)
+    # the inflate tuning, from an engine over the first file: servers made
+    # afterwards start from it
+    dev0 = torch.from_numpy(files[0][0]).to("cuda")
+    torch.cuda.synchronize()
+    tune_eng = frt.BatchEngine(0)
+    tune_eng.bind_bam(dev0.data_ptr(), dev0.numel())
+    tuning = tune_eng.autotune(args.tuning_cache, force=args.retune)
+    del tune_eng, dev0
     srv = frt.RegionServer(0, budget_bytes=w["budget"])
     ids = [srv.add_bam(b, x) for b, x, _ in files]
     # warm-up: a few requests through every stage
@@ -715,7 +734,8 @@ def run_serving(args, rank, world, local):
                        "records": int(sum(n for *_, n in files)),
                        "compressed_bytes": int(sum(b.size for b, _, _ in files)),
                        "offered_req_per_s": w["rate"], "budget_bytes": w["budget"],
-                       "l2": "region requests are independent (no flush)", "parallelism": f"replicas x{world}"},
+                       "l2": "region requests are independent (no flush)", "parallelism": f"replicas x{world}",
+                       "tuning": tuning},
             "serving": {"batched": batched, "capacity": capacity, "plain_per_request": plain,
                         "note": "latency = device completion of the request's tick - arrival; plain = one request "
                                 "per tick, one tick in flight, on the first requests of the same stream"},

@@ -137,6 +137,36 @@ class EngineConfig(C.Structure):
                 ("sort_queue", C.c_uint32)]
 
 
+class InflateTuning(C.Structure):
+    """A tuning of the member inflate: a compiled variant, warps per CTA (one
+    member per warp), CTAs per SM (0: as many as fit), members per queue pop."""
+    _fields_ = [("variant", C.c_int32), ("warps_per_cta", C.c_int32), ("ctas_per_sm", C.c_int32),
+                ("queue_chunk", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+class InflateVariant(C.Structure):
+    _fields_ = [("lit_bits", C.c_int32), ("dist_bits", C.c_int32), ("window", C.c_int32), ("queue", C.c_int32),
+                ("smem_per_warp", C.c_uint64)]
+
+    def as_dict(self) -> dict:
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+class AutotuneResult(C.Structure):
+    _fields_ = [("tuning", InflateTuning), ("ms", C.c_double), ("gbs", C.c_double), ("members", C.c_uint64),
+                ("from_cache", C.c_int32), ("candidates", C.c_int32), ("key", C.c_char * 192)]
+
+    def as_dict(self) -> dict:
+        d = self.tuning.as_dict()
+        d.update(variant_shape=inflate_variants()[self.tuning.variant], sample_ms=float(self.ms),
+                 sample_gbs=float(self.gbs), sample_members=int(self.members), from_cache=bool(self.from_cache),
+                 candidates=int(self.candidates), key=self.key.decode())
+        return d
+
+
 class EngineStats(C.Structure):
     _fields_ = [("members", C.c_uint64), ("compressed_bytes", C.c_uint64), ("inflated_bytes", C.c_uint64),
                 ("records", C.c_uint64), ("tail", C.c_uint64), ("aux_fields", C.c_uint64),
@@ -235,6 +265,16 @@ def lib():
         "frt_engine_get_file_info": (C.c_int, [_P, C.c_size_t, _P]),
         "frt_engine_file_bam": (_P, [_P, C.c_size_t]),
         "frt_engine_file_columns": (_P, [_P, C.c_size_t]),
+        "frt_engine_inflated_to_host": (C.c_int, [_P, _P, C.c_size_t, _P]),
+        "frt_engine_get_tuning": (C.c_int, [_P, _P]),
+        "frt_engine_set_tuning": (C.c_int, [_P, _P, _P]),
+        "frt_engine_time_inflate": (C.c_int, [_P, _P, C.c_uint64, C.c_int32, _P, _P, _P]),
+        "frt_autotune": (C.c_int, [_P, C.c_char_p, C.c_int32, _P, _P]),
+        "frt_inflate_variant_count": (C.c_int, []),
+        "frt_inflate_variant_info": (C.c_int, [C.c_int32, _P, _P]),
+        "frt_inflate_get_default_tuning": (None, [_P]),
+        "frt_inflate_set_default_tuning": (C.c_int, [C.c_int, _P, _P]),
+        "frt_inflate_tuning_ctas_per_sm": (C.c_int, [C.c_int, _P]),
         "frt_bai_parse": (C.c_int, [_P, C.c_size_t, _P, _P]),
         "frt_bai_free": (None, [_P]),
         "frt_bai_reference_count": (C.c_int32, [_P]),
@@ -923,6 +963,30 @@ class RegionServer:
             self._h = None
 
 
+def inflate_variants() -> list[dict]:
+    """The compiled variants of the member inflate: table roots, window buffer
+    and match queue per warp, shared memory per warp."""
+    out = []
+    for v in range(int(lib().frt_inflate_variant_count())):
+        info = InflateVariant()
+        err = _Err()
+        _raise(lib().frt_inflate_variant_info(v, C.byref(info), C.byref(err)), err)
+        out.append(info.as_dict())
+    return out
+
+
+def default_tuning() -> InflateTuning:
+    t = InflateTuning()
+    lib().frt_inflate_get_default_tuning(C.byref(t))
+    return t
+
+
+def set_default_tuning(tuning: InflateTuning, device: int = 0) -> None:
+    """The tuning codecs, engines and servers created afterwards start from."""
+    err = _Err()
+    _raise(lib().frt_inflate_set_default_tuning(device, C.byref(tuning), C.byref(err)), err)
+
+
 class BatchEngine:
     """The batched form: a whole BGZF BAM resident on the device, inflated,
     verified, scanned and decoded by persistent kernels fed from a device work
@@ -970,6 +1034,33 @@ class BatchEngine:
         err = _Err()
         _raise(lib().frt_engine_run(self._h, C.byref(err)), err)
 
+    @property
+    def tuning(self) -> InflateTuning:
+        t = InflateTuning()
+        lib().frt_engine_get_tuning(self._h, C.byref(t))
+        return t
+
+    def set_tuning(self, tuning: InflateTuning) -> None:
+        err = _Err()
+        _raise(lib().frt_engine_set_tuning(self._h, C.byref(tuning), C.byref(err)), err)
+
+    def time_inflate(self, tuning: InflateTuning, members: int = 0, reps: int = 3) -> tuple[float, int]:
+        """Best time (ms) of the persistent inflate alone under a tuning over the
+        first `members` members (0: all), and the bytes they inflate to."""
+        ms, nbytes, err = C.c_double(), C.c_uint64(), _Err()
+        _raise(lib().frt_engine_time_inflate(self._h, C.byref(tuning), members, reps, C.byref(ms), C.byref(nbytes),
+                                             C.byref(err)), err)
+        return ms.value, nbytes.value
+
+    def autotune(self, cache_path: str | None = None, force: bool = False) -> dict:
+        """Picks the inflate tuning for this engine's workload: from the JSON
+        cache, or by timing the candidates and caching the winner.  The winner
+        becomes this engine's tuning and the process default."""
+        res, err = AutotuneResult(), _Err()
+        path = None if cache_path is None else str(cache_path).encode()
+        _raise(lib().frt_autotune(self._h, path, int(force), C.byref(res), C.byref(err)), err)
+        return res.as_dict()
+
     def finish(self) -> EngineStats:
         st = EngineStats()
         err = _Err()
@@ -1006,6 +1097,14 @@ class BatchEngine:
         n = C.c_size_t()
         p = lib().frt_engine_inflated(self._h, C.byref(n))
         return p or 0, n.value
+
+    def inflated(self) -> np.ndarray:
+        """The last run's inflated bytes, copied to host memory."""
+        _, n = self.inflated_ptr()
+        out = np.empty(n, np.uint8)
+        err = _Err()
+        _raise(lib().frt_engine_inflated_to_host(self._h, out.ctypes.data, out.size, C.byref(err)), err)
+        return out
 
     @property
     def stream(self) -> int:

@@ -390,6 +390,7 @@ struct frt_engine {
     SharedStream *shared = nullptr;
     cudaStream_t stream = nullptr;
     frt_engine_config cfg{};
+    frt_inflate_tuning tuning{};
     int grid = 0;
     // bound file
     const uint8_t *in = nullptr;
@@ -516,9 +517,8 @@ cudaError_t enqueue_inflate(frt_engine *e)
 {
     return frt_launch_inflate_persistent(e->in, e->in_off, e->in_len, e->out, e->out_off, e->isize, e->crc_expect,
                                          e->status, e->produced, e->crc, e->cfg.sort_queue ? e->order : nullptr,
-                                         &e->st->n_members, e->n_cap, e->out_cap, &e->st->queue_head,
-                                         e->cfg.queue_chunk ? e->cfg.queue_chunk : 1, (u32)e->grid,
-                                         (unsigned long long *)&e->st->block_err, e->stream);
+                                         &e->st->n_members, e->n_cap, e->out_cap, &e->st->queue_head, (u32)e->grid,
+                                         (unsigned long long *)&e->st->block_err, e->tuning, e->stream);
 }
 
 void column_ptrs(frt_engine *e, FrtBamColumnsDev &c)
@@ -567,6 +567,26 @@ cudaError_t enqueue_records(frt_engine *e, bool with_columns)
                                   ecol<u32>(e, FRT_COL_AUX_FIRST), e->aux_entries, &e->st->totals[0], e->rec_cap,
                                   e->aux_cap, s);
     return cudaGetLastError();
+}
+
+// Captures the steady state as a graph (when the engine uses one): front,
+// inflate and, for one BAM, the record stages; several files replay front and
+// inflate, their decoders running eagerly.  Drops any earlier graph.
+cudaError_t capture_graph(frt_engine *e)
+{
+    if (e->exec) cudaGraphExecDestroy(e->exec);
+    if (e->graph) cudaGraphDestroy(e->graph);
+    e->exec = nullptr;
+    e->graph = nullptr;
+    if (!e->cfg.use_graph) return cudaSuccess;
+    cudaError_t ce = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
+    if (ce != cudaSuccess) return ce;
+    enqueue_front(e);
+    enqueue_inflate(e);
+    if (!e->multi) enqueue_records(e, true);
+    ce = cudaStreamEndCapture(e->stream, &e->graph);
+    if (ce == cudaSuccess) ce = cudaGraphInstantiate(&e->exec, e->graph, 0);
+    return ce;
 }
 
 int stats_from_state(frt_engine *e, frt_engine_stats *stats, frt_error *err)
@@ -668,7 +688,18 @@ extern "C" int frt_engine_create(int device, void *stream, const frt_engine_conf
     e->stream = ss->s;
     if (cfg) e->cfg = *cfg;
     else e->cfg = frt_engine_config{0, 0, 1, 1};
-    e->grid = frt_inflate_persistent_grid();
+    e->tuning = frt_inflate_default();
+    if (e->cfg.warps_per_cta) e->tuning.warps_per_cta = (int32_t)e->cfg.warps_per_cta;
+    if (e->cfg.queue_chunk) e->tuning.queue_chunk = (int32_t)e->cfg.queue_chunk;
+    e->grid = frt_inflate_persistent_grid(e->tuning);
+    if (e->grid < 1) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr,
+                  "inflate tuning (variant %d, %d warps per CTA, chunk %d) does not fit device %d", e->tuning.variant,
+                  e->tuning.warps_per_cta, e->tuning.queue_chunk, device);
+        stream_release(ss);
+        delete e;
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
     *out = e;
     return FRT_OK;
 }
@@ -781,17 +812,7 @@ extern "C" int frt_engine_bind_bam(frt_engine *e, const uint8_t *dev_bgzf, size_
     if ((rc = ealloc(e, &e->aux_entries, 3 * (e->aux_cap + 1), err))) return rc;
     e->col_bytes[FRT_COL_AUX_ENTRIES] = 12 * e->aux_cap;
     // Capture the steady state.
-    if (e->cfg.use_graph) {
-        ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-        if (ce == cudaSuccess) {
-            enqueue_front(e);
-            enqueue_inflate(e);
-            enqueue_records(e, true);
-            ce = cudaStreamEndCapture(s, &e->graph);
-        }
-        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&e->exec, e->graph, 0);
-        if (ce != cudaSuccess) return cuda_fail(err, ce, "capturing the engine graph");
-    }
+    if ((ce = capture_graph(e)) != cudaSuccess) return cuda_fail(err, ce, "capturing the engine graph");
     return FRT_OK;
 }
 
@@ -984,16 +1005,7 @@ extern "C" int frt_engine_bind_files(frt_engine *e, const uint8_t *dev, size_t l
     }
     cudaStreamSynchronize(s); // the offsets uploads read from host vectors
     if ((rc = decode_files(e, err))) return rc;
-    if (e->cfg.use_graph) {
-        ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-        if (ce == cudaSuccess) {
-            enqueue_front(e);
-            enqueue_inflate(e);
-            ce = cudaStreamEndCapture(s, &e->graph);
-        }
-        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&e->exec, e->graph, 0);
-        if (ce != cudaSuccess) return cuda_fail(err, ce, "capturing the engine graph");
-    }
+    if ((ce = capture_graph(e)) != cudaSuccess) return cuda_fail(err, ce, "capturing the engine graph");
     return FRT_OK;
 }
 
@@ -1056,6 +1068,105 @@ extern "C" int frt_engine_run(frt_engine *e, frt_error *err)
         ce = enqueue_records(e, true);
     }
     if (ce != cudaSuccess) return cuda_fail(err, ce, "launching the engine");
+    return FRT_OK;
+}
+
+extern "C" int frt_engine_get_tuning(const frt_engine *e, frt_inflate_tuning *out)
+{
+    if (!e || !out) return FRT_ERR_INVALID_ARGUMENT;
+    *out = e->tuning;
+    return FRT_OK;
+}
+
+extern "C" int frt_engine_set_tuning(frt_engine *e, const frt_inflate_tuning *t, frt_error *err)
+{
+    if (!e || !t) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    DeviceGuardLite g(e->device);
+    const int grid = frt_inflate_persistent_grid(*t);
+    if (grid < 1) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr,
+                  "inflate tuning (variant %d, %d warps per CTA, %d CTAs per SM, chunk %d) is invalid or does not "
+                  "fit device %d",
+                  t->variant, t->warps_per_cta, t->ctas_per_sm, t->queue_chunk, e->device);
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    e->tuning = *t;
+    e->grid = grid;
+    if (e->in) {
+        cudaError_t ce = capture_graph(e);
+        if (ce != cudaSuccess) return cuda_fail(err, ce, "capturing the engine graph");
+    }
+    return FRT_OK;
+}
+
+extern "C" int frt_engine_time_inflate(frt_engine *e, const frt_inflate_tuning *t, uint64_t members, int32_t reps,
+                                       double *ms, uint64_t *inflated_bytes, frt_error *err)
+{
+    if (!e || !t || !ms) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    DeviceGuardLite g(e->device);
+    if (!e->in || e->n_cap == 0) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "no file bound");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    const int grid = frt_inflate_persistent_grid(*t);
+    if (grid < 1) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr,
+                  "inflate tuning (variant %d, %d warps per CTA, %d CTAs per SM, chunk %d) is invalid or does not "
+                  "fit device %d",
+                  t->variant, t->warps_per_cta, t->ctas_per_sm, t->queue_chunk, e->device);
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    const u64 k = members && members < e->n_cap ? members : e->n_cap;
+    cudaStream_t s = e->stream;
+    cudaError_t ce;
+    u64 last_off = 0;
+    u32 last_size = 0;
+    if ((ce = cudaMemcpyAsync(&last_off, e->out_off + (k - 1), 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(&last_size, e->isize + (k - 1), 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (ce = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(err, ce, "reading the plan");
+    if (inflated_bytes) *inflated_bytes = last_off + last_size;
+    cudaEvent_t ev[2];
+    if ((ce = cudaEventCreate(&ev[0])) != cudaSuccess) return cuda_fail(err, ce, "creating events");
+    if ((ce = cudaEventCreate(&ev[1])) != cudaSuccess) {
+        cudaEventDestroy(ev[0]);
+        return cuda_fail(err, ce, "creating events");
+    }
+    double best = 0;
+    unsigned long long block_err = ~0ull;
+    for (int r = 0; r <= (reps > 0 ? reps : 1) && ce == cudaSuccess; ++r) { // the first launch warms up
+        if ((ce = cudaMemsetAsync(&e->st->queue_head, 0, sizeof(u32), s)) != cudaSuccess) break;
+        if ((ce = cudaMemsetAsync(&e->st->block_err, 0xff, sizeof(unsigned long long), s)) != cudaSuccess) break;
+        if ((ce = cudaEventRecord(ev[0], s)) != cudaSuccess) break;
+        if ((ce = frt_launch_inflate_persistent(e->in, e->in_off, e->in_len, e->out, e->out_off, e->isize,
+                                                e->crc_expect, e->status, e->produced, e->crc, nullptr,
+                                                &e->st->n_members, k, e->out_cap, &e->st->queue_head, (u32)grid,
+                                                (unsigned long long *)&e->st->block_err, *t, s)) != cudaSuccess)
+            break;
+        if ((ce = cudaEventRecord(ev[1], s)) != cudaSuccess) break;
+        if ((ce = cudaMemcpyAsync(&block_err, &e->st->block_err, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) break;
+        if ((ce = cudaEventSynchronize(ev[1])) != cudaSuccess || (ce = cudaStreamSynchronize(s)) != cudaSuccess) break;
+        float t_ms = 0;
+        if ((ce = cudaEventElapsedTime(&t_ms, ev[0], ev[1])) != cudaSuccess) break;
+        if (block_err != ~0ull) break;
+        if (r > 0 && (best == 0 || t_ms < best)) best = t_ms;
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "timing the inflate");
+    if (block_err != ~0ull) {
+        const u64 m = block_err >> 8;
+        set_error(err, FRT_ERR_MALFORMED, m, 0, block_err & 0xff, 0, "bgzf",
+                  "member %llu failed its trailer check while timing the inflate", (unsigned long long)m);
+        return FRT_ERR_MALFORMED;
+    }
+    *ms = best;
     return FRT_OK;
 }
 
@@ -1142,7 +1253,29 @@ extern "C" const uint8_t *frt_engine_inflated(const frt_engine *e, size_t *len)
     return e ? e->out : nullptr;
 }
 
+extern "C" int frt_engine_inflated_to_host(const frt_engine *e, uint8_t *dst, size_t cap, frt_error *err)
+{
+    size_t len = 0;
+    const uint8_t *p = e ? frt_engine_inflated(e, &len) : nullptr;
+    if (!e || (len && (!p || !dst))) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    if (cap < len) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, len, cap, 0, nullptr, "destination too small");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    if (!len) return FRT_OK;
+    DeviceGuardLite g(e->device);
+    cudaError_t ce = cudaMemcpyAsync(dst, p, len, cudaMemcpyDeviceToHost, e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "downloading the inflated bytes");
+    return FRT_OK;
+}
+
 extern "C" void *frt_engine_stream(const frt_engine *e) { return e ? (void *)e->stream : nullptr; }
+
+int frt::engine_device(const frt_engine *e) { return e ? e->device : 0; }
 
 // Per-stage timing of an eager run (front / inflate / records), averaged over
 // `repeats` runs, with CUDA events on the engine stream.

@@ -29,25 +29,37 @@
 // reference kernel (crates/fritillaria-cuda/kernels/inflate.cu:78-458), so a
 // stream it rejects is rejected here with the same code.
 
+#include <mutex>
+
 #include "common.cuh"
 #include "inflate.cuh"
+#include "runtime.h"
 
 namespace {
 
-constexpr int LIT_BITS = INF_LIT_BITS;
-constexpr int DIST_BITS = INF_DIST_BITS;
 constexpr int CL_BITS = 7;
-constexpr u32 DIST_BASE = 1u << LIT_BITS; // distance entries follow the literal/length ones
-constexpr u32 LIT_MASK = (1u << LIT_BITS) - 1u;
-constexpr u32 DIST_MASK = (1u << DIST_BITS) - 1u;
-// After a refill the buffer holds at least 33 bits: enough for a length
-// whose code and extra bits fit the root plus a distance whose code fits its
-// root (at most 13 extra bits), so a fast match needs no second refill.
-static_assert(LIT_BITS + DIST_BITS + 13 <= 33, "a fast match must fit one refill");
-constexpr u32 WB = INF_WINBUF;            // window output buffer (bytes)
-constexpr u32 MAXQ = INF_MAXQ;            // matches per window
-static_assert(MAXQ <= 32 * 32, "a lane tracks at most 32 queued matches");
-static_assert(WB % 32 == 0, "pending bits cover whole words");
+constexpr u32 MAX_WB = 4096; // the largest window buffer of any variant
+
+// One configuration of the member inflate: the literal/length and distance
+// table roots, the window output buffer and the window's match queue.  The
+// library carries a few (kVariants below); a tuning picks one per device and
+// workload.
+template <int LB, int DB, u32 W, u32 Q> struct Cfg {
+    static constexpr int LIT_BITS = LB;
+    static constexpr int DIST_BITS = DB;
+    static constexpr u32 DIST_BASE = 1u << LB; // distance entries follow the literal/length ones
+    static constexpr u32 LIT_MASK = (1u << LB) - 1u;
+    static constexpr u32 DIST_MASK = (1u << DB) - 1u;
+    static constexpr u32 WB = W;   // window output buffer (bytes)
+    static constexpr u32 MAXQ = Q; // matches per window
+    // After a refill the buffer holds at least 33 bits: enough for a length
+    // whose code and extra bits fit the root plus a distance whose code fits
+    // its root (at most 13 extra bits), so a fast match needs no second refill.
+    static_assert(LB + DB + 13 <= 33, "a fast match must fit one refill");
+    static_assert(LB <= 15 && DB <= 15, "roots are at most the longest code");
+    static_assert(Q <= 32 * 32, "a lane tracks at most 32 queued matches");
+    static_assert(W % 32 == 0 && W > 2 * 258 && W <= MAX_WB, "pending bits cover whole words");
+};
 
 // CRC-32 tables, computed at compile time: slice[k][b] is the register that
 // byte b followed by k zero bytes leaves from zero (slicing by 4; slice[0] is
@@ -55,7 +67,7 @@ static_assert(WB % 32 == 0, "pending bits cover whole words");
 // registers use (bit 31 is x^0), for every window length.
 struct CrcTables {
     u32 slice[4][256];
-    u32 xpow[WB + 1];
+    u32 xpow[MAX_WB + 1];
 };
 
 constexpr CrcTables make_crc_tables()
@@ -69,7 +81,7 @@ constexpr CrcTables make_crc_tables()
     for (int k = 1; k < 4; ++k)
         for (u32 i = 0; i < 256; ++i) t.slice[k][i] = (t.slice[k - 1][i] >> 8) ^ t.slice[0][t.slice[k - 1][i] & 0xffu];
     u32 v = 0x80000000u;
-    for (u32 m = 0; m <= WB; ++m) {
+    for (u32 m = 0; m <= MAX_WB; ++m) {
         t.xpow[m] = v;
         for (int k = 0; k < 8; ++k) v = (v >> 1) ^ (0xEDB88320u & (0u - (v & 1u)));
     }
@@ -96,18 +108,18 @@ struct CodeState {
 //   [15:12] extra bits
 //   [31:16] literal byte, resolved length, or length/distance base
 // The code-length code's table marks a missing code with 0 instead.
-struct WarpSmem {
-    u32 tab[DIST_BASE + (1u << DIST_BITS)];
+template <class C> struct WarpSmem {
+    u32 tab[C::DIST_BASE + (1u << C::DIST_BITS)];
     CodeState lcode;
     CodeState dcode;
     u16 lsorted[288];
     u16 dsorted[32];
     u32 run[16];
-    u32 pend[WB / 32];    // unresolved match destinations in the window
-    u32 q_dst[MAXQ];      // matches of the window: destination (member offset)
-    u32 q_ld[MAXQ];       //   len | dist << 9
+    u32 pend[C::WB / 32]; // unresolved match destinations in the window
+    u32 q_dst[C::MAXQ];   // matches of the window: destination (member offset)
+    u32 q_ld[C::MAXQ];    //   len | dist << 9
     u8 lens[320];
-    alignas(16) u8 win[WB + 264];
+    alignas(16) u8 win[C::WB + 264];
 };
 
 __device__ __forceinline__ u32 lit_entry(u32 sym, u32 L)
@@ -306,7 +318,7 @@ __device__ __forceinline__ bool pend_any(const u32 *pend, u32 a, u32 b)
 // The earliest unresolved match is always ready, so rounds make progress.
 // A source byte before the window (wstart) is read from HBM, where earlier
 // windows were written; a byte inside it from the window buffer.
-__device__ void resolve(WarpSmem *sm, const u8 *out, u32 wstart, u32 nq)
+template <class C> __device__ void resolve(WarpSmem<C> *sm, const u8 *out, u32 wstart, u32 nq)
 {
     const u32 lane = lane_id();
     for (u32 k = lane; k < nq; k += 32) {
@@ -364,7 +376,7 @@ __device__ void resolve(WarpSmem *sm, const u8 *out, u32 wstart, u32 nq)
 // register, every other lane its slice from zero (slicing by 4), each lane
 // shifts its result past the bytes after its slice with one multiply by a
 // tabulated power, and an XOR across the warp gives the new register.
-__device__ void write_window(const WarpSmem *sm, u8 *out, u32 wstart, u32 n, u32 *crc)
+template <class C> __device__ void write_window(const WarpSmem<C> *sm, u8 *out, u32 wstart, u32 n, u32 *crc)
 {
     const u32 lane = lane_id();
     for (u32 j = lane; j < n; j += 32) out[wstart + j] = sm->win[j];
@@ -395,8 +407,10 @@ __device__ void write_window(const WarpSmem *sm, u8 *out, u32 wstart, u32 n, u32
 // decodes, and leaves a distance it rejects to slow_symbol as well.  One
 // exit test at the bottom of the loop, and the refill takes a word loaded
 // one refill earlier, so its load latency is off the chain.
-__device__ __forceinline__ void fast_run(WarpSmem *sm, LaneBits &r, u32 pos, u32 lim, u32 &o_io, u32 &nq_io)
+template <class C>
+__device__ __forceinline__ void fast_run(WarpSmem<C> *sm, LaneBits &r, u32 pos, u32 lim, u32 &o_io, u32 &nq_io)
 {
+    constexpr u32 LIT_MASK = C::LIT_MASK, DIST_MASK = C::DIST_MASK, DIST_BASE = C::DIST_BASE, MAXQ = C::MAXQ;
     u64 buf = r.buf;
     int cnt = r.cnt;
     u32 nw = r.nw, o = o_io, nq = nq_io;
@@ -445,8 +459,11 @@ __device__ __forceinline__ void fast_run(WarpSmem *sm, LaneBits &r, u32 pos, u32
 // One symbol (a literal, or a length with its distance) with every check,
 // in the order of the reference kernel.  Returns 0 to go on, 1 at the end of
 // the block, 2 on an error (status set).
-__device__ __forceinline__ int slow_symbol(WarpSmem *sm, LaneBits &r, u32 pos, u32 cap, u32 &o, u32 &nq, u32 &status)
+template <class C>
+__device__ __forceinline__ int slow_symbol(WarpSmem<C> *sm, LaneBits &r, u32 pos, u32 cap, u32 &o, u32 &nq, u32 &status)
 {
+    constexpr int LIT_BITS = C::LIT_BITS, DIST_BITS = C::DIST_BITS;
+    constexpr u32 LIT_MASK = C::LIT_MASK, DIST_MASK = C::DIST_MASK, DIST_BASE = C::DIST_BASE;
     r.refill();
     u32 e = sm->tab[(u32)r.buf & LIT_MASK];
     if (((e >> 5) & 7u) == 7u) {
@@ -518,9 +535,11 @@ __device__ __forceinline__ int slow_symbol(WarpSmem *sm, LaneBits &r, u32 pos, u
 // and writes the window to HBM with its CRC.  Truncation is checked once per
 // burst: bits past the payload read as zero, and a symbol that used one is
 // where a sequential decoder reports it.
-__device__ u32 decode_burst(WarpSmem *sm, LaneBits &r, u32 total, u8 *out, u32 *pos_io, u32 cap, u32 *crc,
+template <class C>
+__device__ u32 decode_burst(WarpSmem<C> *sm, LaneBits &r, u32 total, u8 *out, u32 *pos_io, u32 cap, u32 *crc,
                             int *eob_out)
 {
+    constexpr u32 WB = C::WB, MAXQ = C::MAXQ;
     const u32 lane = lane_id();
     const u32 pos = *pos_io;
     u32 o = 0, nq = 0, status = INF_OK;
@@ -552,14 +571,15 @@ __device__ u32 decode_burst(WarpSmem *sm, LaneBits &r, u32 total, u8 *out, u32 *
     return INF_OK;
 }
 
-} // namespace
-
 // Inflates one member with the calling warp into out[0, cap).  Returns the
 // status; *produced_out and *crc_out are valid in every lane.
-__device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, void *smem_v, u32 *produced_out,
+template <class C>
+__device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, WarpSmem<C> *sm, u32 *produced_out,
                                    u32 *crc_out)
 {
-    WarpSmem *sm = (WarpSmem *)smem_v;
+    constexpr int LIT_BITS = C::LIT_BITS, DIST_BITS = C::DIST_BITS;
+    constexpr u32 DIST_BASE = C::DIST_BASE, WB = C::WB;
+    static_assert((1u << C::DIST_BITS) >= (1u << CL_BITS), "the code-length table shares the distance region");
     const u32 lane = lane_id();
     LaneBits r;
     r.attach(in, in_len);
@@ -756,22 +776,21 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, v
     return status;
 }
 
-size_t frt_inflate_warp_smem() { return sizeof(WarpSmem); }
-
-#define WSM_BYTES ((sizeof(WarpSmem) + 15) & ~(size_t)15)
+template <class C> __host__ __device__ constexpr size_t warp_smem_bytes() { return (sizeof(WarpSmem<C>) + 15) & ~(size_t)15; }
 
 // Plain form: one warp per member of this launch, members in span order.
-__global__ void __launch_bounds__(INF_WARPS_PER_CTA * 32, 1)
+template <class C>
+__global__ void __launch_bounds__(FRT_INFLATE_MAX_WARPS * 32, 1)
 k_inflate_members(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out, const u64 *out_off,
                   const u32 *out_cap, u32 *status, u32 *produced, u32 *crc, u32 n)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const u32 warp = threadIdx.x / 32;
-    void *wsm = smem + warp * WSM_BYTES;
+    WarpSmem<C> *wsm = (WarpSmem<C> *)(smem + warp * warp_smem_bytes<C>());
     u32 m = blockIdx.x * (blockDim.x / 32) + warp;
     if (m >= n) return;
     u32 p = 0, c = 0;
-    u32 st = inflate_member_warp(in + in_off[m], in_len[m], out + out_off[m], out_cap[m], wsm, &p, &c);
+    u32 st = inflate_member_warp<C>(in + in_off[m], in_len[m], out + out_off[m], out_cap[m], wsm, &p, &c);
     if (lane_id() == 0) {
         status[m] = st;
         produced[m] = p;
@@ -784,7 +803,8 @@ k_inflate_members(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out, c
 // one warp per member, and verifies each member against its trailer as it
 // finishes: the first failing member in file order wins the error word
 // (member << 8 | frt_status), as in verify_and_offsets (backend.rs:221-256).
-__global__ void __launch_bounds__(INF_WARPS_PER_CTA * 32, 1)
+template <class C>
+__global__ void __launch_bounds__(FRT_INFLATE_MAX_WARPS * 32, 1)
 k_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out, const u64 *out_off,
                      const u32 *isize, const u32 *crc_expect, u32 *status, u32 *produced, u32 *crc,
                      const u32 *order, const u64 *n_ptr, u64 n_cap, u64 out_capacity, u32 *queue_head, u32 chunk,
@@ -792,7 +812,7 @@ k_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out
 {
     extern __shared__ __align__(16) unsigned char smem[];
     const u32 warp = threadIdx.x / 32;
-    void *wsm = smem + warp * WSM_BYTES;
+    WarpSmem<C> *wsm = (WarpSmem<C> *)(smem + warp * warp_smem_bytes<C>());
     u64 n64 = *n_ptr;
     const u32 n = (u32)(n64 < n_cap ? n64 : n_cap);
     if (chunk == 0) chunk = 1;
@@ -810,7 +830,7 @@ k_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out
             if (out_off[m] + cap > out_capacity) {
                 st = INF_OUTPUT_OVERFLOW; // sizes changed since the buffers were planned
             } else {
-                st = inflate_member_warp(in + in_off[m], in_len[m], out + out_off[m], cap, wsm, &p, &c);
+                st = inflate_member_warp<C>(in + in_off[m], in_len[m], out + out_off[m], cap, wsm, &p, &c);
             }
             if (lane_id() == 0) {
                 status[m] = st;
@@ -822,6 +842,8 @@ k_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out
         }
     }
 }
+
+} // namespace
 
 // Standalone CRC of already-inflated members (the reference's crc32_blocks,
 // crates/fritillaria-cuda/kernels/crc32.cu:13-38), one warp per member.
@@ -850,25 +872,152 @@ __global__ void k_crc32_members(const u8 *data, const u64 *offsets, const u32 *l
     if (lane == 0) out[m] = c;
 }
 
-// ---- host launchers --------------------------------------------------------
-size_t frt_inflate_smem_bytes(int warps) { return (size_t)warps * WSM_BYTES; }
+// ---- variants, tunings, launchers -----------------------------------------
+namespace {
+
+using MembersKernel = void (*)(const u8 *, const u64 *, const u32 *, u8 *, const u64 *, const u32 *, u32 *, u32 *,
+                               u32 *, u32);
+using PersistentKernel = void (*)(const u8 *, const u64 *, const u32 *, u8 *, const u64 *, const u32 *, const u32 *,
+                                  u32 *, u32 *, u32 *, const u32 *, const u64 *, u64, u64, u32 *, u32,
+                                  unsigned long long *);
+
+struct Variant {
+    frt_inflate_variant info;
+    MembersKernel members;
+    PersistentKernel persistent;
+};
+
+template <class C> Variant make_variant()
+{
+    return {{C::LIT_BITS, C::DIST_BITS, (int32_t)C::WB, (int32_t)C::MAXQ, (uint64_t)warp_smem_bytes<C>()},
+            k_inflate_members<C>, k_inflate_persistent<C>};
+}
+
+// The compiled variants: the table roots trade shared memory (members in
+// flight) against codes that take the long path; the window buffer and its
+// queue trade shared memory against bursts per member.  Variant 0 is the
+// default before any tuning.
+const Variant kVariants[] = {
+    make_variant<Cfg<10, 8, 2048, 384>>(), make_variant<Cfg<9, 8, 2048, 384>>(),
+    make_variant<Cfg<11, 8, 2048, 384>>(), make_variant<Cfg<10, 8, 1024, 256>>(),
+    make_variant<Cfg<9, 7, 1024, 256>>(),  make_variant<Cfg<10, 8, 4096, 768>>(),
+};
+constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+
+std::mutex g_tuning_mu;
+frt_inflate_tuning g_tuning = {0, 3, 0, 1};
+
+int sm_count()
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+} // namespace
+
+extern "C" int frt_inflate_variant_count(void) { return kNumVariants; }
+
+const frt_inflate_variant *frt_inflate_variant_at(int v) { return v >= 0 && v < kNumVariants ? &kVariants[v].info : nullptr; }
+
+extern "C" int frt_inflate_variant_info(int32_t variant, frt_inflate_variant *out, frt_error *err)
+{
+    if (!out || variant < 0 || variant >= kNumVariants) {
+        frt::set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, kNumVariants, (uint64_t)variant, 0, nullptr,
+                       "no inflate variant %d (%d compiled)", variant, kNumVariants);
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    *out = kVariants[variant].info;
+    return FRT_OK;
+}
+
+frt_inflate_tuning frt_inflate_default()
+{
+    std::lock_guard<std::mutex> lk(g_tuning_mu);
+    return g_tuning;
+}
+
+void frt_inflate_set_default(const frt_inflate_tuning &t)
+{
+    std::lock_guard<std::mutex> lk(g_tuning_mu);
+    g_tuning = t;
+}
+
+size_t frt_inflate_smem_bytes(const frt_inflate_tuning &t)
+{
+    return (size_t)t.warps_per_cta * kVariants[t.variant].info.smem_per_warp;
+}
 
 cudaError_t frt_inflate_prepare()
 {
-    cudaError_t e = cudaFuncSetAttribute(k_inflate_members, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)frt_inflate_smem_bytes(INF_WARPS_PER_CTA));
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_inflate_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)frt_inflate_smem_bytes(INF_WARPS_PER_CTA));
+    for (const Variant &v : kVariants) {
+        if ((e = cudaFuncSetAttribute(v.members, cudaFuncAttributeMaxDynamicSharedMemorySize, optin)) != cudaSuccess)
+            return e;
+        if ((e = cudaFuncSetAttribute(v.persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, optin)) != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
+}
+
+int frt_inflate_ctas_per_sm(const frt_inflate_tuning &t)
+{
+    if (t.variant < 0 || t.variant >= kNumVariants || t.warps_per_cta < 1 || t.warps_per_cta > FRT_INFLATE_MAX_WARPS ||
+        t.ctas_per_sm < 0 || t.queue_chunk < 1 || t.queue_chunk > FRT_INFLATE_MAX_CHUNK)
+        return 0;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kVariants[t.variant].persistent, t.warps_per_cta * 32,
+                                                      frt_inflate_smem_bytes(t)) != cudaSuccess)
+        return 0;
+    if (t.ctas_per_sm > 0 && t.ctas_per_sm < per_sm) per_sm = t.ctas_per_sm;
+    return per_sm;
+}
+
+int frt_inflate_persistent_grid(const frt_inflate_tuning &t) { return sm_count() * frt_inflate_ctas_per_sm(t); }
+
+extern "C" void frt_inflate_get_default_tuning(frt_inflate_tuning *out)
+{
+    if (out) *out = frt_inflate_default();
+}
+
+extern "C" int frt_inflate_tuning_ctas_per_sm(int device, const frt_inflate_tuning *t)
+{
+    if (!t || frt::check_device(device, nullptr) != FRT_OK) return 0;
+    frt::DeviceGuardLite g(device);
+    if (frt_inflate_prepare() != cudaSuccess) return 0;
+    return frt_inflate_ctas_per_sm(*t);
+}
+
+extern "C" int frt_inflate_set_default_tuning(int device, const frt_inflate_tuning *t, frt_error *err)
+{
+    if (!t) {
+        frt::set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null tuning");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    int rc = frt::check_device(device, err);
+    if (rc != FRT_OK) return rc;
+    if (frt_inflate_tuning_ctas_per_sm(device, t) < 1) {
+        frt::set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr,
+                       "inflate tuning (variant %d, %d warps per CTA, %d CTAs per SM, chunk %d) is invalid or does "
+                       "not fit device %d",
+                       t->variant, t->warps_per_cta, t->ctas_per_sm, t->queue_chunk, device);
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    frt_inflate_set_default(*t);
+    return FRT_OK;
 }
 
 cudaError_t frt_launch_inflate_members(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out,
                                        const u64 *out_off, const u32 *out_cap, u32 *status, u32 *produced,
-                                       u32 *crc, u32 n, cudaStream_t s)
+                                       u32 *crc, u32 n, const frt_inflate_tuning &t, cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
-    u32 grid = (n + INF_WARPS_PER_CTA - 1) / INF_WARPS_PER_CTA;
-    k_inflate_members<<<grid, INF_WARPS_PER_CTA * 32, frt_inflate_smem_bytes(INF_WARPS_PER_CTA), s>>>(
+    const u32 w = (u32)t.warps_per_cta;
+    kVariants[t.variant].members<<<(n + w - 1) / w, w * 32, frt_inflate_smem_bytes(t), s>>>(
         in, in_off, in_len, out, out_off, out_cap, status, produced, crc, n);
     return cudaGetLastError();
 }
@@ -876,24 +1025,13 @@ cudaError_t frt_launch_inflate_members(const u8 *in, const u64 *in_off, const u3
 cudaError_t frt_launch_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out,
                                           const u64 *out_off, const u32 *isize, const u32 *crc_expect, u32 *status,
                                           u32 *produced, u32 *crc, const u32 *order, const u64 *n_ptr, u64 n_cap,
-                                          u64 out_capacity, u32 *queue_head, u32 chunk, u32 grid,
-                                          unsigned long long *block_err, cudaStream_t s)
+                                          u64 out_capacity, u32 *queue_head, u32 grid, unsigned long long *block_err,
+                                          const frt_inflate_tuning &t, cudaStream_t s)
 {
-    k_inflate_persistent<<<grid, INF_WARPS_PER_CTA * 32, frt_inflate_smem_bytes(INF_WARPS_PER_CTA), s>>>(
+    kVariants[t.variant].persistent<<<grid, t.warps_per_cta * 32, frt_inflate_smem_bytes(t), s>>>(
         in, in_off, in_len, out, out_off, isize, crc_expect, status, produced, crc, order, n_ptr, n_cap,
-        out_capacity, queue_head, chunk, block_err);
+        out_capacity, queue_head, (u32)t.queue_chunk, block_err);
     return cudaGetLastError();
-}
-
-int frt_inflate_persistent_grid()
-{
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_inflate_persistent, INF_WARPS_PER_CTA * 32,
-                                                  frt_inflate_smem_bytes(INF_WARPS_PER_CTA));
-    if (per_sm < 1) per_sm = 1;
-    return sms * per_sm;
 }
 
 cudaError_t frt_launch_crc32_members(const u8 *data, const u64 *offsets, const u32 *lengths, u32 *out, u32 n,

@@ -236,6 +236,7 @@ extern "C" int frt_codec_create(int device, void *stream, frt_codec **out, frt_e
     if (!ss) return FRT_ERR_CUDA;
     frt_codec *c = new frt_codec;
     c->device = device;
+    c->tuning = frt_inflate_default();
     c->shared = ss;
     c->stream = ss->s;
     *out = c;
@@ -353,7 +354,7 @@ int inflate_batch(frt_codec *c, const uint8_t *batch, size_t batch_len, const fr
     if ((e = cudaMemcpyAsync(work, plan64.data(), 8 * (2 * n + 1), cudaMemcpyHostToDevice, st)) != cudaSuccess) return fail(e, "uploading plan");
     if ((e = cudaMemcpyAsync(d_in_len, plan32.data(), 8 * n, cudaMemcpyHostToDevice, st)) != cudaSuccess) return fail(e, "uploading plan");
     if ((e = frt_launch_inflate_members(input, d_in_off, d_in_len, output, d_out_off, d_cap, d_status, d_produced,
-                                        d_crc, (u32)n, st)) != cudaSuccess)
+                                        d_crc, (u32)n, c->tuning, st)) != cudaSuccess)
         return fail(e, "launching inflate");
     std::vector<uint32_t> res(3 * n);
     if (n && (e = cudaMemcpyAsync(res.data(), d_status, 12 * n, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return fail(e, "downloading status");

@@ -18,6 +18,7 @@ void set_error(frt_error *err, int code, uint64_t offset, uint64_t expected, uin
 int cuda_fail(frt_error *err, cudaError_t e, const char *what);
 const char *inflate_status_message(uint32_t s);
 int check_device(int device, frt_error *err);
+int engine_device(const frt_engine *e);
 int dev_alloc(void **p, size_t bytes, cudaStream_t s, frt_error *err);
 void dev_free(void *p, cudaStream_t s);
 void configure_pool(int device);
@@ -67,6 +68,7 @@ void stream_release(SharedStream *s);
 
 struct frt_codec {
     int device = 0;
+    frt_inflate_tuning tuning{}; // the process default when the codec was made
     cudaStream_t stream = nullptr;
     frt::SharedStream *shared = nullptr;
     std::mutex mu;

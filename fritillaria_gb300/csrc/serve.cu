@@ -125,6 +125,7 @@ struct frt_server {
     std::chrono::steady_clock::time_point t0;
     cudaEvent_t origin = nullptr; // server clock zero on the device
     frt_codec *codec = nullptr;   // for reading BAM headers at add time
+    frt_inflate_tuning tuning{};
     int inflate_grid = 0;
     uint64_t pending = 0;         // submitted, not yet completed
 };
@@ -300,8 +301,8 @@ int launch_tick(frt_server *sv, std::vector<SrvReq *> &batch, frt_error *err)
         return cuda_fail(err, e, "uploading a tick");
     // inflate every member of the tick
     if ((e = frt_launch_inflate_persistent(sv->files_arena, in_off, in_len, t->arena, out_off, isize, crc, status,
-                                           produced, crc_out, order, n_dev, n, pl.arena_bytes, (u32 *)queue_head, 1,
-                                           (u32)sv->inflate_grid, block_err, st)) != cudaSuccess)
+                                           produced, crc_out, order, n_dev, n, pl.arena_bytes, (u32 *)queue_head,
+                                           (u32)sv->inflate_grid, block_err, sv->tuning, st)) != cudaSuccess)
         return cuda_fail(err, e, "launching the inflate");
     int32_t n_ref = 0; // bounds refID in the record-start test
     for (SrvReq *r : batch) n_ref = std::max(n_ref, sv->files[r->file].n_ref < 0 ? (1 << 24) : sv->files[r->file].n_ref);
@@ -400,7 +401,8 @@ extern "C" int frt_server_create(int device, void *stream, uint64_t budget_bytes
     s->shared = ss;
     s->stream = ss->s;
     s->budget = budget_bytes;
-    s->inflate_grid = frt_inflate_persistent_grid();
+    s->tuning = frt_inflate_default();
+    s->inflate_grid = frt_inflate_persistent_grid(s->tuning);
     s->t0 = std::chrono::steady_clock::now();
     cudaEventCreate(&s->origin);
     cudaEventRecord(s->origin, s->stream);

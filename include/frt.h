@@ -408,6 +408,41 @@ int frt_server_request_column_to_host(const frt_server *s, uint64_t request, int
 const uint8_t *frt_server_request_inflated(const frt_server *s, uint64_t request, size_t *len);
 void frt_server_release(frt_server *s, uint64_t request);
 
+/* ---- inflate tuning ----------------------------------------------------------
+ * No reference counterpart: the reference launches one fixed kernel shape
+ * (crates/fritillaria-cuda/src/backend.rs:178-219).  The member inflate here
+ * is compiled in several variants -- literal/length and distance table roots,
+ * window buffer and match queue per warp -- and a tuning picks a variant, the
+ * warps per CTA (one member per warp), the CTAs per SM and the members a warp
+ * takes per pop of the device work queue.  Codecs, engines and servers start
+ * from the process-wide default; frt_autotune times candidates on an engine's
+ * bound input and caches the winner in a JSON file keyed by device, variant
+ * set and workload class. */
+typedef struct {
+    int32_t variant;       /* index of a compiled variant */
+    int32_t warps_per_cta; /* 1..8; one member per warp */
+    int32_t ctas_per_sm;   /* 0: as many as fit */
+    int32_t queue_chunk;   /* members per queue pop, 1..64 */
+} frt_inflate_tuning;
+
+typedef struct {
+    int32_t lit_bits;       /* literal/length table root */
+    int32_t dist_bits;      /* distance table root */
+    int32_t window;         /* window buffer per warp, bytes */
+    int32_t queue;          /* matches queued per window */
+    uint64_t smem_per_warp; /* shared memory per warp, bytes */
+} frt_inflate_variant;
+
+int frt_inflate_variant_count(void);
+int frt_inflate_variant_info(int32_t variant, frt_inflate_variant *out, frt_error *err);
+void frt_inflate_get_default_tuning(frt_inflate_tuning *out);
+/* Checks that the tuning fits `device` (at least one CTA per SM) and makes it
+ * the default of codecs, engines and servers created afterwards. */
+int frt_inflate_set_default_tuning(int device, const frt_inflate_tuning *t, frt_error *err);
+/* CTAs per SM the tuning runs with on `device`; 0 when it is invalid or does
+ * not fit. */
+int frt_inflate_tuning_ctas_per_sm(int device, const frt_inflate_tuning *t);
+
 /* ---- batched, device-resident form ---------------------------------------
  * No reference counterpart: the batched launch model.  Members of a whole
  * BGZF file resident in device memory are discovered, inflated, verified,
@@ -416,8 +451,8 @@ void frt_server_release(frt_server *s, uint64_t request);
 typedef struct frt_engine frt_engine;
 
 typedef struct {
-    uint32_t warps_per_cta;   /* 0: autotuned */
-    uint32_t queue_chunk;     /* members taken per queue pop; 0: autotuned */
+    uint32_t warps_per_cta;   /* 0: from the default inflate tuning */
+    uint32_t queue_chunk;     /* members taken per queue pop; 0: from the default inflate tuning */
     uint32_t use_graph;       /* replay the steady state as a CUDA graph */
     uint32_t sort_queue;      /* longest member first */
 } frt_engine_config;
@@ -445,9 +480,41 @@ int frt_engine_finish(frt_engine *e, frt_engine_stats *stats, frt_error *err);
 /* Host-buffer convenience: H2D copy, run, and read the stats back. */
 int frt_engine_run_host(frt_engine *e, const uint8_t *host_bgzf, size_t len, frt_engine_stats *stats,
                         frt_error *err);
+/* The engine's inflate tuning; a new one takes effect at the next run (the
+ * graph is captured again). */
+int frt_engine_get_tuning(const frt_engine *e, frt_inflate_tuning *out);
+int frt_engine_set_tuning(frt_engine *e, const frt_inflate_tuning *t, frt_error *err);
+/* Times the persistent inflate alone under a tuning, after a completed run:
+ * the first `members` members of the bound input in file order (0: all), best
+ * of `reps` launches on the engine's stream.  *inflated_bytes is what the
+ * timed members inflate to.  Leaves the columns of the last run invalid until
+ * the next run. */
+int frt_engine_time_inflate(frt_engine *e, const frt_inflate_tuning *t, uint64_t members, int32_t reps, double *ms,
+                            uint64_t *inflated_bytes, frt_error *err);
+
+typedef struct {
+    frt_inflate_tuning tuning;
+    double ms;          /* best launch time of the winner on the sample */
+    double gbs;         /* inflated GB/s of the winner on the sample */
+    uint64_t members;   /* sample size, members */
+    int32_t from_cache; /* 1: taken from the cache, nothing timed */
+    int32_t candidates; /* tunings timed */
+    char key[192];      /* cache key: device, variant set, workload class */
+} frt_autotune_result;
+
+/* The autotuner.  After a completed run of the engine, looks its workload up
+ * in the JSON cache at `cache_path` (NULL: $FRT_TUNING_CACHE, else
+ * ~/.cache/fritillaria_gb300/inflate_tuning.json); on a miss, or with
+ * `force`, times the candidates (every variant at 2, 3, 4, 6 and 8 warps per
+ * CTA, then queue chunks 1..8 for the best) on a sample of the bound input,
+ * and writes the winner back.  The winner becomes the engine's tuning and the
+ * process default. */
+int frt_autotune(frt_engine *e, const char *cache_path, int32_t force, frt_autotune_result *out, frt_error *err);
 int frt_engine_column(const frt_engine *e, int column, void **ptr, size_t *bytes, size_t *width);
 int frt_engine_column_to_host(const frt_engine *e, int column, void *dst, size_t cap, frt_error *err);
 const uint8_t *frt_engine_inflated(const frt_engine *e, size_t *len);
+/* Copies the inflated bytes of the last run to host memory (cap >= len). */
+int frt_engine_inflated_to_host(const frt_engine *e, uint8_t *dst, size_t cap, frt_error *err);
 void *frt_engine_stream(const frt_engine *e);
 /* Several files, several formats, one inflate.  No reference counterpart:
  * BGZF files laid out back to back in one device buffer (each a whole BGZF

@@ -117,3 +117,39 @@ def test_format_scanners_refuse_without_a_gpu(frt):
     for cls in (frt.FastqScanner, frt.BcfScanner, frt.FastaCompactor):
         with pytest.raises(frt.CudaUnavailable):
             cls(0)
+
+
+def test_inflate_variants_and_default_tuning():
+    import fritillaria_gb300 as frt
+
+    frt.lib()
+    vs = frt.inflate_variants()
+    assert len(vs) >= 2
+    for v in vs:
+        assert 7 <= v["dist_bits"] <= v["lit_bits"] + 1 and v["lit_bits"] + v["dist_bits"] + 13 <= 33
+        assert v["window"] % 32 == 0 and v["queue"] <= 1024 and v["smem_per_warp"] > v["window"]
+    t = frt.default_tuning().as_dict()
+    assert t == {"variant": 0, "warps_per_cta": 3, "ctas_per_sm": 0, "queue_chunk": 1}
+    with pytest.raises(frt.InvalidArgument):
+        err = frt._Err()
+        frt._raise(frt.lib().frt_inflate_variant_info(len(vs), frt.C.byref(frt.InflateVariant()), frt.C.byref(err)),
+                   err)
+
+
+def test_shipped_tuning_cache_names_compiled_variants():
+    """Every entry of the committed tuning cache names a compiled variant of
+    the shape it records (a stale entry would be ignored and re-tuned)."""
+    import json
+
+    import fritillaria_gb300 as frt
+
+    frt.lib()
+    path = Path(frt.__file__).resolve().parent / "inflate_tuning.json"
+    doc = json.loads(path.read_text())
+    assert doc["version"] == 1 and doc["entries"]
+    vs = frt.inflate_variants()
+    for key, e in doc["entries"].items():
+        v = vs[e["variant"]]
+        assert (e["lit_bits"], e["dist_bits"], e["window"], e["queue"]) == (
+            v["lit_bits"], v["dist_bits"], v["window"], v["queue"]), key
+        assert 1 <= e["warps_per_cta"] <= 8 and 1 <= e["queue_chunk"] <= 64 and e["warps_per_member"] == 1
