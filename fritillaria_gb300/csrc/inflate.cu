@@ -116,8 +116,7 @@ template <class C> struct WarpSmem {
     u16 dsorted[32];
     u32 run[16];
     u32 pend[C::WB / 32]; // unresolved match destinations in the window
-    u32 q_dst[C::MAXQ];   // matches of the window: destination (member offset)
-    u32 q_ld[C::MAXQ];    //   len | dist << 9
+    u64 q[C::MAXQ];       // matches of the window: destination (member offset) | (len | dist << 9) << 32
     u8 lens[320];
     alignas(16) u8 win[C::WB + 264];
 };
@@ -313,55 +312,67 @@ __device__ __forceinline__ bool pend_any(const u32 *pend, u32 a, u32 b)
     return false;
 }
 
-// Resolves the window's nq queued matches in parallel rounds: in each round
-// every match whose source bytes are final is copied, one lane per match.
-// The earliest unresolved match is always ready, so rounds make progress.
-// A source byte before the window (wstart) is read from HBM, where earlier
-// windows were written; a byte inside it from the window buffer.
+// Copies one queued match into the window.  Source bytes before the window
+// (wstart) are read from HBM, where earlier windows were written, in groups
+// so the loads overlap; bytes inside it come from the window buffer (with a
+// distance shorter than the length, from the match's own first bytes).
+template <class C> __device__ __forceinline__ void copy_match(WarpSmem<C> *sm, const u8 *out, u32 wstart, u64 q)
+{
+    const u32 d = (u32)q, len = (u32)(q >> 32) & 511u, s = d - (u32)(q >> 41);
+    u32 i = 0;
+    while (i < len && s + i < wstart) {
+        u32 n = min(min(8u, len - i), wstart - (s + i));
+        u8 b[8];
+#pragma unroll
+        for (u32 x = 0; x < 8; ++x)
+            if (x < n) b[x] = out[s + i + x];
+#pragma unroll
+        for (u32 x = 0; x < 8; ++x)
+            if (x < n) sm->win[d + i + x - wstart] = b[x];
+        i += n;
+    }
+    for (; i < len; ++i) sm->win[d + i - wstart] = sm->win[s + i - wstart];
+}
+
+// Resolves the window's nq queued matches.  A match whose source lies before
+// the window (its first min(len, dist) bytes: later ones are its own) reads
+// only final bytes, so all of those are copied in a first pass, one lane per
+// match.  The others read the window, where a source byte is final once it is
+// a literal, a byte of a match from the first pass, or a byte of another
+// window match already copied: those go in parallel rounds, each copying every
+// match whose source bytes carry no pending mark; the earliest unresolved one
+// is always ready, so rounds make progress.
 template <class C> __device__ void resolve(WarpSmem<C> *sm, const u8 *out, u32 wstart, u32 nq)
 {
     const u32 lane = lane_id();
-    for (u32 k = lane; k < nq; k += 32) {
-        u32 d = sm->q_dst[k];
-        pend_set(sm->pend, d - wstart, d + (sm->q_ld[k] & 511u) - wstart, true);
+    u32 todo = 0;
+    for (u32 j = 0, k = lane; k < nq; ++j, k += 32) {
+        const u64 q = sm->q[k];
+        const u32 d = (u32)q, len = (u32)(q >> 32) & 511u, dist = (u32)(q >> 41);
+        if (d - dist + min(len, dist) <= wstart) {
+            copy_match(sm, out, wstart, q);
+        } else {
+            pend_set(sm->pend, d - wstart, d + len - wstart, true);
+            todo |= 1u << j;
+        }
     }
     __syncwarp();
-    u32 todo = 0;
-    for (u32 j = 0; lane + 32 * j < nq; ++j) todo |= 1u << j;
     while (__any_sync(FRT_FULL_MASK, todo != 0)) {
         u32 ready = 0;
         for (u32 t = todo; t; t &= t - 1) {
-            u32 j = __ffs(t) - 1, k = lane + 32 * j;
-            u32 d = sm->q_dst[k], ld = sm->q_ld[k];
-            u32 len = ld & 511u, dist = ld >> 9;
-            u32 s = d - dist, e = s + min(len, dist);
-            if (e <= wstart || !pend_any(sm->pend, max(s, wstart) - wstart, e - wstart)) ready |= 1u << j;
+            const u32 j = __ffs(t) - 1;
+            const u64 q = sm->q[lane + 32 * j];
+            const u32 d = (u32)q, len = (u32)(q >> 32) & 511u, dist = (u32)(q >> 41);
+            const u32 s = d - dist, e = s + min(len, dist);
+            if (!pend_any(sm->pend, max(s, wstart) - wstart, e - wstart)) ready |= 1u << j;
         }
         __syncwarp();
-        for (u32 t = ready; t; t &= t - 1) {
-            u32 j = __ffs(t) - 1, k = lane + 32 * j;
-            u32 d = sm->q_dst[k], ld = sm->q_ld[k];
-            u32 len = ld & 511u, s = d - (ld >> 9);
-            u32 i = 0;
-            // bytes before the window: gather in groups so the HBM loads overlap
-            while (i < len && s + i < wstart) {
-                u32 n = min(min(8u, len - i), wstart - (s + i));
-                u8 b[8];
-#pragma unroll
-                for (u32 x = 0; x < 8; ++x)
-                    if (x < n) b[x] = out[s + i + x];
-#pragma unroll
-                for (u32 x = 0; x < 8; ++x)
-                    if (x < n) sm->win[d + i + x - wstart] = b[x];
-                i += n;
-            }
-            for (; i < len; ++i) sm->win[d + i - wstart] = sm->win[s + i - wstart];
-        }
+        for (u32 t = ready; t; t &= t - 1) copy_match(sm, out, wstart, sm->q[lane + 32 * (__ffs(t) - 1)]);
         __syncwarp();
         for (u32 t = ready; t; t &= t - 1) {
-            u32 j = __ffs(t) - 1, k = lane + 32 * j;
-            u32 d = sm->q_dst[k];
-            pend_set(sm->pend, d - wstart, d + (sm->q_ld[k] & 511u) - wstart, false);
+            const u64 q = sm->q[lane + 32 * (__ffs(t) - 1)];
+            const u32 d = (u32)q;
+            pend_set(sm->pend, d - wstart, d + ((u32)(q >> 32) & 511u) - wstart, false);
         }
         todo &= ~ready;
         __syncwarp();
@@ -380,7 +391,8 @@ template <class C> __device__ void write_window(const WarpSmem<C> *sm, u8 *out, 
 {
     const u32 lane = lane_id();
     for (u32 j = lane; j < n; j += 32) out[wstart + j] = sm->win[j];
-    const u32 s = ((n + 31u) / 32u + 3u) & ~3u; // slice length, whole words
+    u32 s = ((n + 31u) / 32u + 3u) & ~3u; // slice length, whole words,
+    if ((s & 4u) == 0u) s += 4u;          // an odd number of them: no bank conflicts
     const u32 b0 = min(n, lane * s), b1 = min(n, b0 + s);
     u32 c = lane == 0 ? ~*crc : 0u;
     u32 i = b0;
@@ -406,7 +418,9 @@ template <class C> __device__ void write_window(const WarpSmem<C> *sm, u8 *out, 
 // 258 bytes); stops in front of any other symbol, which slow_symbol then
 // decodes, and leaves a distance it rejects to slow_symbol as well.  One
 // exit test at the bottom of the loop, and the refill takes a word loaded
-// one refill earlier, so its load latency is off the chain.
+// one refill earlier, so its load latency is off the chain.  A literal is
+// followed by a second lookup without going round the loop (the buffer still
+// holds a root's worth of bits), as literals come in runs.
 template <class C>
 __device__ __forceinline__ void fast_run(WarpSmem<C> *sm, LaneBits &r, u32 pos, u32 lim, u32 &o_io, u32 &nq_io)
 {
@@ -430,6 +444,13 @@ __device__ __forceinline__ void fast_run(WarpSmem<C> *sm, LaneBits &r, u32 pos, 
             sm->win[o++] = (u8)(e >> 16);
             buf >>= (e & 31u);
             cnt -= (int)(e & 31u);
+            // a second literal needs no refill: at least 33 - LIT_BITS bits remain
+            const u32 e2 = tab[(u32)buf & LIT_MASK];
+            if ((e2 & 0xE0u) == 0u) {
+                sm->win[o++] = (u8)(e2 >> 16);
+                buf >>= (e2 & 31u);
+                cnt -= (int)(e2 & 31u);
+            }
             go = true;
         } else if ((e & 0xE0u) == 0x20u) { // resolved length
             const u64 b2 = buf >> (e & 31u);
@@ -441,8 +462,7 @@ __device__ __forceinline__ void fast_run(WarpSmem<C> *sm, LaneBits &r, u32 pos, 
                 buf = b2 >> (d & 31u);
                 cnt -= (int)((e & 31u) + (d & 31u));
                 const u32 len = e >> 16;
-                sm->q_dst[nq] = dst;
-                sm->q_ld[nq] = len | (dist << 9);
+                sm->q[nq] = (u64)dst | ((u64)(len | (dist << 9)) << 32);
                 ++nq;
                 o += len;
                 go = nq < MAXQ;
@@ -521,8 +541,7 @@ __device__ __forceinline__ int slow_symbol(WarpSmem<C> *sm, LaneBits &r, u32 pos
         status = INF_OUTPUT_OVERFLOW;
         return 2;
     }
-    sm->q_dst[nq] = dst;
-    sm->q_ld[nq] = len | (dist << 9);
+    sm->q[nq] = (u64)dst | ((u64)(len | (dist << 9)) << 32);
     ++nq;
     o += len;
     return 0;
