@@ -41,10 +41,12 @@ constexpr int CL_BITS = 7;
 constexpr u32 MAX_WB = 4096; // the largest window buffer of any variant
 
 // One configuration of the member inflate: the literal/length and distance
-// table roots, the window output buffer and the window's match queue.  The
+// table roots, the window output buffer, the window's match queue and a
+// register cap (more warps per SM against fewer registers per lane).  The
 // library carries a few (kVariants below); a tuning picks one per device and
 // workload.
-template <int LB, int DB, u32 W, u32 Q> struct Cfg {
+template <int LB, int DB, u32 W, u32 Q, int R = 128> struct Cfg {
+    static constexpr int REGS = R; // register cap per thread (ptxas), trading per-warp speed for occupancy
     static constexpr int LIT_BITS = LB;
     static constexpr int DIST_BITS = DB;
     static constexpr u32 DIST_BASE = 1u << LB; // distance entries follow the literal/length ones
@@ -117,7 +119,6 @@ template <class C> struct WarpSmem {
     u32 run[16];
     u32 pend[C::WB / 32]; // unresolved match destinations in the window
     u64 q[C::MAXQ];       // matches of the window: destination (member offset) | (len | dist << 9) << 32
-    u8 lens[320];
     alignas(16) u8 win[C::WB + 264];
 };
 
@@ -599,6 +600,10 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, W
     constexpr int LIT_BITS = C::LIT_BITS, DIST_BITS = C::DIST_BITS;
     constexpr u32 DIST_BASE = C::DIST_BASE, WB = C::WB;
     static_assert((1u << C::DIST_BITS) >= (1u << CL_BITS), "the code-length table shares the distance region");
+    // A block's code lengths are read and turned into tables before its first
+    // symbol, while the window buffer holds nothing: they live there.
+    static_assert(C::WB >= 320, "the code lengths fit the window buffer");
+    u8 *const lens = sm->win;
     const u32 lane = lane_id();
     LaneBits r;
     r.attach(in, in_len);
@@ -667,12 +672,12 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, W
 
         // ---- Huffman block: tables ------------------------------------------
         if (type == 1) {
-            for (int s = lane; s < 288; s += 32) sm->lens[s] = s < 144 ? 8 : (s < 256 ? 9 : (s < 280 ? 7 : 8));
+            for (int s = lane; s < 288; s += 32) lens[s] = s < 144 ? 8 : (s < 256 ? 9 : (s < 280 ? 7 : 8));
             __syncwarp();
-            build_table(sm->lens, 288, LIT_BITS, sm->tab, sm->lsorted, &sm->lcode, sm->run, 0);
-            sm->lens[lane] = 5;
+            build_table(lens, 288, LIT_BITS, sm->tab, sm->lsorted, &sm->lcode, sm->run, 0);
+            lens[lane] = 5;
             __syncwarp();
-            build_table(sm->lens, 32, DIST_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode, sm->run, 1);
+            build_table(lens, 32, DIST_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode, sm->run, 1);
         } else {
             int nlen = 0, ndist = 0, ncode = 0;
             u32 bp = bitpos;
@@ -690,14 +695,14 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, W
                 if (status == INF_OK) {
                     // the code-length code lengths arrive in this permuted order
                     const u8 order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
-                    for (int i = 0; i < 19; ++i) sm->lens[order[i]] = 0;
+                    for (int i = 0; i < 19; ++i) lens[order[i]] = 0;
                     for (int i = 0; i < ncode; ++i) {
                         r.refill();
                         if (r.tell() + 3 > total) {
                             status = INF_TRUNCATED;
                             break;
                         }
-                        sm->lens[order[i]] = (u8)r.peek(3);
+                        lens[order[i]] = (u8)r.peek(3);
                         r.drop(3);
                     }
                 }
@@ -710,7 +715,7 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, W
             __syncwarp();
             // the code-length code must be complete (all-zero counts as
             // complete and fails at first use, as in the reference)
-            if (build_table(sm->lens, 19, CL_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode, sm->run, 2) != 0) {
+            if (build_table(lens, 19, CL_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode, sm->run, 2) != 0) {
                 status = INF_BAD_TABLE;
                 break;
             }
@@ -733,7 +738,7 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, W
                     r.drop((int)L);
                     u32 sym = e >> 16;
                     if (sym < 16) {
-                        sm->lens[index++] = (u8)sym;
+                        lens[index++] = (u8)sym;
                         continue;
                     }
                     u32 val = 0;
@@ -743,7 +748,7 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, W
                             status = INF_BAD_LENGTH_REPEAT;
                             break;
                         }
-                        val = sm->lens[index - 1];
+                        val = lens[index - 1];
                     }
                     if (r.tell() + nb > total) {
                         status = INF_TRUNCATED;
@@ -755,21 +760,21 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, W
                         status = INF_BAD_LENGTH_REPEAT;
                         break;
                     }
-                    while (rep--) sm->lens[index++] = (u8)val;
+                    while (rep--) lens[index++] = (u8)val;
                 }
-                if (status == INF_OK && sm->lens[256] == 0) status = INF_BAD_TABLE;
+                if (status == INF_OK && lens[256] == 0) status = INF_BAD_TABLE;
                 bp = r.tell();
             }
             status = __shfl_sync(FRT_FULL_MASK, status, 0);
             if (status != INF_OK) break;
             bitpos = __shfl_sync(FRT_FULL_MASK, bp, 0);
             __syncwarp();
-            int rl = build_table(sm->lens, nlen, LIT_BITS, sm->tab, sm->lsorted, &sm->lcode, sm->run, 0);
+            int rl = build_table(lens, nlen, LIT_BITS, sm->tab, sm->lsorted, &sm->lcode, sm->run, 0);
             if (rl != 0 && (rl < 0 || nlen != (int)sm->lcode.count[0] + 1)) { // incomplete only with one code
                 status = INF_BAD_TABLE;
                 break;
             }
-            int rd = build_table(sm->lens + nlen, ndist, DIST_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode,
+            int rd = build_table(lens + nlen, ndist, DIST_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode,
                                  sm->run, 1);
             if (rd != 0 && (rd < 0 || ndist != (int)sm->dcode.count[0] + 1)) {
                 status = INF_BAD_TABLE;
@@ -799,7 +804,7 @@ template <class C> __host__ __device__ constexpr size_t warp_smem_bytes() { retu
 
 // Plain form: one warp per member of this launch, members in span order.
 template <class C>
-__global__ void __launch_bounds__(FRT_INFLATE_MAX_WARPS * 32, 1)
+__global__ void __maxnreg__(C::REGS)
 k_inflate_members(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out, const u64 *out_off,
                   const u32 *out_cap, u32 *status, u32 *produced, u32 *crc, u32 n)
 {
@@ -823,7 +828,7 @@ k_inflate_members(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out, c
 // finishes: the first failing member in file order wins the error word
 // (member << 8 | frt_status), as in verify_and_offsets (backend.rs:221-256).
 template <class C>
-__global__ void __launch_bounds__(FRT_INFLATE_MAX_WARPS * 32, 1)
+__global__ void __maxnreg__(C::REGS)
 k_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out, const u64 *out_off,
                      const u32 *isize, const u32 *crc_expect, u32 *status, u32 *produced, u32 *crc,
                      const u32 *order, const u64 *n_ptr, u64 n_cap, u64 out_capacity, u32 *queue_head, u32 chunk,
@@ -908,18 +913,22 @@ struct Variant {
 
 template <class C> Variant make_variant()
 {
-    return {{C::LIT_BITS, C::DIST_BITS, (int32_t)C::WB, (int32_t)C::MAXQ, (uint64_t)warp_smem_bytes<C>()},
+    return {{C::LIT_BITS, C::DIST_BITS, (int32_t)C::WB, (int32_t)C::MAXQ, C::REGS, (uint64_t)warp_smem_bytes<C>()},
             k_inflate_members<C>, k_inflate_persistent<C>};
 }
 
 // The compiled variants: the table roots trade shared memory (members in
 // flight) against codes that take the long path; the window buffer and its
-// queue trade shared memory against bursts per member.  Variant 0 is the
-// default before any tuning.
+// queue trade shared memory against bursts per member; a register cap (80:
+// no spills; 72, 64 and 56: up to ~120 spilled bytes) lets more CTAs fit an SM.
+// Variant 0 is the default before any tuning.
 const Variant kVariants[] = {
-    make_variant<Cfg<10, 8, 2048, 384>>(), make_variant<Cfg<9, 8, 2048, 384>>(),
-    make_variant<Cfg<11, 8, 2048, 384>>(), make_variant<Cfg<10, 8, 1024, 256>>(),
-    make_variant<Cfg<9, 7, 1024, 256>>(),  make_variant<Cfg<10, 8, 4096, 768>>(),
+    make_variant<Cfg<10, 8, 2048, 384>>(),     make_variant<Cfg<9, 8, 2048, 384>>(),
+    make_variant<Cfg<11, 8, 2048, 384>>(),     make_variant<Cfg<10, 8, 1024, 256>>(),
+    make_variant<Cfg<9, 7, 1024, 256>>(),      make_variant<Cfg<10, 8, 4096, 768>>(),
+    make_variant<Cfg<9, 8, 2048, 384, 80>>(),  make_variant<Cfg<9, 7, 1024, 256, 80>>(),
+    make_variant<Cfg<10, 8, 2048, 384, 80>>(), make_variant<Cfg<9, 7, 1024, 256, 72>>(),
+    make_variant<Cfg<9, 7, 1024, 192, 64>>(), make_variant<Cfg<9, 7, 1024, 160, 56>>(),
 };
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 

@@ -319,6 +319,7 @@ uint32_t variant_set_hash()
         mix(info.dist_bits);
         mix(info.window);
         mix(info.queue);
+        mix(info.max_registers);
         mix((int64_t)info.smem_per_warp);
     }
     return h;
@@ -362,6 +363,7 @@ Json tuning_json(const frt_inflate_tuning &t, double ms, double gbs, uint64_t me
     j.set("dist_bits", Json::number(info.dist_bits));
     j.set("window", Json::number(info.window));
     j.set("queue", Json::number(info.queue));
+    j.set("max_registers", Json::number(info.max_registers));
     j.set("warps_per_cta", Json::number(t.warps_per_cta));
     j.set("ctas_per_sm", Json::number(t.ctas_per_sm));
     j.set("queue_chunk", Json::number(t.queue_chunk));
@@ -387,14 +389,16 @@ bool tuning_from_json(const Json &j, frt_inflate_tuning *t)
         *v = x->num;
         return true;
     };
-    double v, w, c, q, lb, db, win, qu;
+    double v, w, c, q, lb, db, win, qu, mr;
     if (!num("variant", &v) || !num("warps_per_cta", &w) || !num("ctas_per_sm", &c) || !num("queue_chunk", &q) ||
-        !num("lit_bits", &lb) || !num("dist_bits", &db) || !num("window", &win) || !num("queue", &qu))
+        !num("lit_bits", &lb) || !num("dist_bits", &db) || !num("window", &win) || !num("queue", &qu) ||
+        !num("max_registers", &mr))
         return false;
     frt_inflate_variant info{};
     if (frt_inflate_variant_info((int32_t)v, &info, nullptr) != FRT_OK) return false;
     // the variant index must still name the same shape
-    if (info.lit_bits != (int)lb || info.dist_bits != (int)db || info.window != (int)win || info.queue != (int)qu)
+    if (info.lit_bits != (int)lb || info.dist_bits != (int)db || info.window != (int)win || info.queue != (int)qu ||
+        info.max_registers != (int)mr)
         return false;
     *t = frt_inflate_tuning{(int32_t)v, (int32_t)w, (int32_t)c, (int32_t)q};
     return true;

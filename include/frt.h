@@ -430,6 +430,7 @@ typedef struct {
     int32_t dist_bits;      /* distance table root */
     int32_t window;         /* window buffer per warp, bytes */
     int32_t queue;          /* matches queued per window */
+    int32_t max_registers;  /* register cap per thread */
     uint64_t smem_per_warp; /* shared memory per warp, bytes */
 } frt_inflate_variant;
 
