@@ -128,7 +128,7 @@ def test_inflate_variants_and_default_tuning():
     for v in vs:
         assert 7 <= v["dist_bits"] <= v["lit_bits"] + 1 and v["lit_bits"] + v["dist_bits"] + 13 <= 33
         assert v["window"] % 32 == 0 and v["queue"] <= 1024 and v["smem_per_warp"] > v["window"]
-        assert 64 <= v["max_registers"] <= 255
+        assert 32 <= v["max_registers"] <= 255
     t = frt.default_tuning().as_dict()
     assert t == {"variant": 0, "warps_per_cta": 3, "ctas_per_sm": 0, "queue_chunk": 1}
     with pytest.raises(frt.InvalidArgument):
