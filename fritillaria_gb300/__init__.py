@@ -265,6 +265,14 @@ def lib():
         "frt_engine_get_file_info": (C.c_int, [_P, C.c_size_t, _P]),
         "frt_engine_file_bam": (_P, [_P, C.c_size_t]),
         "frt_engine_file_columns": (_P, [_P, C.c_size_t]),
+        "frt_record_batch_aux_lookup": (C.c_int, [_P, C.c_char_p, _P, _P]),
+        "frt_record_batch_cigar_resolved": (C.c_int, [_P, _P, _P]),
+        "frt_record_batch_unpack_sequences": (C.c_int, [_P, _P, _P]),
+        "frt_record_batch_compact": (C.c_int, [_P, _P, _P]),
+        "frt_engine_aux_lookup": (C.c_int, [_P, C.c_char_p, _P, _P]),
+        "frt_engine_cigar_resolved": (C.c_int, [_P, _P, _P]),
+        "frt_engine_unpack_sequences": (C.c_int, [_P, _P, _P]),
+        "frt_engine_compact": (C.c_int, [_P, _P, _P]),
         "frt_engine_inflated_to_host": (C.c_int, [_P, _P, C.c_size_t, _P]),
         "frt_engine_get_tuning": (C.c_int, [_P, _P]),
         "frt_engine_set_tuning": (C.c_int, [_P, _P, _P]),
@@ -617,8 +625,62 @@ def bam_scan_noalloc(data_ptr: int, length: int, member_offsets_ptr: int, n_memb
     return n.value, tail.value
 
 
-class DeviceRecordBatch:
+# Record fields: opt-in device kernels over decoded BAM records (one aux tag for
+# every record, CIGARs resolved through CG, bases unpacked, payloads compacted).
+AUX_VALUE_COLUMNS = {"status": (0, np.uint8), "type": (1, np.uint8), "subtype": (2, np.uint8),
+                     "count": (3, np.uint32), "value": (4, np.int64), "offset": (5, np.uint64)}
+CIGAR_COLUMNS = {"offset": (0, np.uint64), "ops": (1, np.uint32), "status": (2, np.uint8)}
+BASES_COLUMNS = {"offsets": (0, np.uint64), "data": (1, np.uint8)}
+COMPACT_COLUMNS = {"name_offsets": (0, np.uint64), "name_data": (1, np.uint8),
+                   "cigar_offsets": (2, np.uint64), "cigar_data": (3, np.uint32),
+                   "sequence_offsets": (4, np.uint64), "sequence_data": (5, np.uint8),
+                   "quality_offsets": (6, np.uint64), "quality_data": (7, np.uint8),
+                   "aux_offsets": (8, np.uint64), "aux_data": (9, np.uint8)}
+
+
+def _tag(tag) -> bytes:
+    t = tag.encode() if isinstance(tag, str) else bytes(tag)
+    if len(t) != 2:
+        raise InvalidArgument(message=f"an aux tag is two bytes, got {t!r}")
+    return t
+
+
+def _fields_call(prefix: str, handle, op: str, tag=None) -> "ColumnBatch":
+    cols = {"aux_lookup": AUX_VALUE_COLUMNS, "cigar_resolved": CIGAR_COLUMNS,
+            "unpack_sequences": BASES_COLUMNS, "compact": COMPACT_COLUMNS}[op]
+    h, err = _P(), _Err()
+    fn = getattr(lib(), f"{prefix}_{op}")
+    if op == "aux_lookup":
+        _raise(fn(handle, _tag(tag), C.byref(h), C.byref(err)), err)
+    else:
+        _raise(fn(handle, C.byref(h), C.byref(err)), err)
+    return ColumnBatch(h, cols)
+
+
+class _RecordFields:
+    """The record-field kernels, for classes whose handle names decoded records."""
+    _fields_prefix = ""
+
+    def aux_lookup(self, tag) -> "ColumnBatch":
+        """One aux tag for every record (Record::aux_get): AUX_VALUE_COLUMNS."""
+        return _fields_call(self._fields_prefix, self._h, "aux_lookup", tag)
+
+    def cigar_resolved(self) -> "ColumnBatch":
+        """Where each record's CIGAR ops are, following CG for the long-CIGAR placeholder."""
+        return _fields_call(self._fields_prefix, self._h, "cigar_resolved")
+
+    def unpack_sequences(self) -> "ColumnBatch":
+        """The bases as ASCII, one byte each, records back to back."""
+        return _fields_call(self._fields_prefix, self._h, "unpack_sequences")
+
+    def compact(self) -> "ColumnBatch":
+        """The name, CIGAR, sequence, quality and aux payloads copied out of the inflated batch."""
+        return _fields_call(self._fields_prefix, self._h, "compact")
+
+
+class DeviceRecordBatch(_RecordFields):
     """DeviceRecordBatch: device columns; keeps its inflate batch alive."""
+    _fields_prefix = "frt_record_batch"
 
     def __init__(self, handle, owned: bool = True):
         self._h = handle
@@ -987,12 +1049,13 @@ def set_default_tuning(tuning: InflateTuning, device: int = 0) -> None:
     _raise(lib().frt_inflate_set_default_tuning(device, C.byref(tuning), C.byref(err)), err)
 
 
-class BatchEngine:
+class BatchEngine(_RecordFields):
     """The batched form: a whole BGZF BAM resident on the device, inflated,
     verified, scanned and decoded by persistent kernels fed from a device work
     queue, the steady state replayed as a CUDA graph.  bind_files() takes
     several BGZF files of different formats laid out back to back: one inflate
     over all their members, then each file's decoder."""
+    _fields_prefix = "frt_engine"
 
     def __init__(self, device: int = 0, stream: int | None = None, warps_per_cta: int = 0, queue_chunk: int = 0,
                  use_graph: bool = True, sort_queue: bool = True):

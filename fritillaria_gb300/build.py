@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
                      f"-I{INCLUDE}", "-diag-suppress", "550"]
 
-CUDA_SOURCES = ["inflate.cu", "bam.cu", "runtime.cu", "decoder.cu", "engine.cu", "formats.cu", "noalloc.cu", "bai.cpp", "tune.cpp",
+CUDA_SOURCES = ["inflate.cu", "bam.cu", "runtime.cu", "decoder.cu", "engine.cu", "formats.cu", "noalloc.cu", "bai.cpp", "tune.cpp", "fields.cu",
                 "serve.cu"]
 LIB = PKG / "libfrt_gb300.so"
 SYNTH_LIB = PKG / "libfrt_synth.so"

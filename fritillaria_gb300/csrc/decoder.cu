@@ -8,6 +8,7 @@
 #include <cstring>
 
 #include "bam.cuh"
+#include "fields.h"
 #include "runtime.h"
 
 using namespace frt;
@@ -307,6 +308,60 @@ extern "C" int frt_record_batch_column_to_host(const frt_record_batch *rb, int c
     if (e == cudaSuccess) e = cudaStreamSynchronize(rb->stream);
     if (e != cudaSuccess) return cuda_fail(err, e, "downloading column");
     return FRT_OK;
+}
+
+// ---- record fields over a record batch ----------------------------------------
+static RecordView view_of(const frt_record_batch *rb)
+{
+    auto col = [rb](int k) { return (const void *)(rb->cols + rb->col_off[k]); };
+    RecordView v;
+    v.buf = rb->source ? rb->source->data : nullptr;
+    v.n = rb->n;
+    v.record_offsets = (const uint64_t *)col(FRT_COL_RECORD_OFFSETS);
+    v.cigar_start = (const uint32_t *)col(FRT_COL_CIGAR_START);
+    v.sequence_start = (const uint32_t *)col(FRT_COL_SEQUENCE_START);
+    v.quality_start = (const uint32_t *)col(FRT_COL_QUALITY_START);
+    v.aux_start = (const uint32_t *)col(FRT_COL_AUX_START);
+    v.record_end = (const uint32_t *)col(FRT_COL_RECORD_END);
+    v.seq_len = (const uint32_t *)col(FRT_COL_SEQ_LEN);
+    v.aux_count = (const uint32_t *)col(FRT_COL_AUX_COUNT);
+    v.aux_first = (const uint32_t *)col(FRT_COL_AUX_FIRST);
+    v.aux_entries = (const uint32_t *)rb->aux;
+    v.n_cigar = (const uint16_t *)col(FRT_COL_N_CIGAR);
+    v.name_len = (const uint8_t *)col(FRT_COL_NAME_LEN);
+    v.aux_status = (const uint8_t *)col(FRT_COL_AUX_STATUS);
+    return v;
+}
+
+static int rb_fields(const frt_record_batch *rb, int op, const char *tag, frt_columns **out, frt_error *err)
+{
+    if (!rb) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null record batch");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    DeviceGuardLite g(rb->device);
+    return fields_run(view_of(rb), op, tag, rb->device, rb->stream, rb->shared, rb->ready, rb->source, out, err);
+}
+
+extern "C" int frt_record_batch_aux_lookup(const frt_record_batch *rb, const char tag[2], frt_columns **out,
+                                           frt_error *err)
+{
+    return rb_fields(rb, FIELDS_AUX_LOOKUP, tag, out, err);
+}
+
+extern "C" int frt_record_batch_cigar_resolved(const frt_record_batch *rb, frt_columns **out, frt_error *err)
+{
+    return rb_fields(rb, FIELDS_CIGAR_RESOLVED, nullptr, out, err);
+}
+
+extern "C" int frt_record_batch_unpack_sequences(const frt_record_batch *rb, frt_columns **out, frt_error *err)
+{
+    return rb_fields(rb, FIELDS_UNPACK_SEQUENCES, nullptr, out, err);
+}
+
+extern "C" int frt_record_batch_compact(const frt_record_batch *rb, frt_columns **out, frt_error *err)
+{
+    return rb_fields(rb, FIELDS_COMPACT, nullptr, out, err);
 }
 
 extern "C" void frt_record_batch_free(frt_record_batch *rb)

@@ -26,6 +26,7 @@
 
 #include "bam.cuh"
 #include "engine_kernels.cuh"
+#include "fields.h"
 #include "inflate.cuh"
 #include "runtime.h"
 
@@ -1251,6 +1252,55 @@ extern "C" const uint8_t *frt_engine_inflated(const frt_engine *e, size_t *len)
 {
     if (len) *len = e ? e->host_state.inflated_total : 0;
     return e ? e->out : nullptr;
+}
+
+// ---- record fields over the engine's last run -------------------------------
+static int engine_fields(const frt_engine *e, int op, const char *tag, frt_columns **out, frt_error *err)
+{
+    if (!e || !e->in || e->multi) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr,
+                  "record fields need an engine with one BAM bound (a batch of several files: use its file's records)");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    frt_engine *m = const_cast<frt_engine *>(e);
+    RecordView v;
+    v.buf = e->out;
+    v.n = e->host_state.totals[0] < e->rec_cap ? e->host_state.totals[0] : e->rec_cap;
+    v.record_offsets = ecol<uint64_t>(m, FRT_COL_RECORD_OFFSETS);
+    v.cigar_start = ecol<uint32_t>(m, FRT_COL_CIGAR_START);
+    v.sequence_start = ecol<uint32_t>(m, FRT_COL_SEQUENCE_START);
+    v.quality_start = ecol<uint32_t>(m, FRT_COL_QUALITY_START);
+    v.aux_start = ecol<uint32_t>(m, FRT_COL_AUX_START);
+    v.record_end = ecol<uint32_t>(m, FRT_COL_RECORD_END);
+    v.seq_len = ecol<uint32_t>(m, FRT_COL_SEQ_LEN);
+    v.aux_count = ecol<uint32_t>(m, FRT_COL_AUX_COUNT);
+    v.aux_first = ecol<uint32_t>(m, FRT_COL_AUX_FIRST);
+    v.aux_entries = e->aux_entries;
+    v.n_cigar = ecol<uint16_t>(m, FRT_COL_N_CIGAR);
+    v.name_len = ecol<uint8_t>(m, FRT_COL_NAME_LEN);
+    v.aux_status = ecol<uint8_t>(m, FRT_COL_AUX_STATUS);
+    DeviceGuardLite g(e->device);
+    return fields_run(v, op, tag, e->device, e->stream, e->shared, nullptr, nullptr, out, err);
+}
+
+extern "C" int frt_engine_aux_lookup(const frt_engine *e, const char tag[2], frt_columns **out, frt_error *err)
+{
+    return engine_fields(e, FIELDS_AUX_LOOKUP, tag, out, err);
+}
+
+extern "C" int frt_engine_cigar_resolved(const frt_engine *e, frt_columns **out, frt_error *err)
+{
+    return engine_fields(e, FIELDS_CIGAR_RESOLVED, nullptr, out, err);
+}
+
+extern "C" int frt_engine_unpack_sequences(const frt_engine *e, frt_columns **out, frt_error *err)
+{
+    return engine_fields(e, FIELDS_UNPACK_SEQUENCES, nullptr, out, err);
+}
+
+extern "C" int frt_engine_compact(const frt_engine *e, frt_columns **out, frt_error *err)
+{
+    return engine_fields(e, FIELDS_COMPACT, nullptr, out, err);
 }
 
 extern "C" int frt_engine_inflated_to_host(const frt_engine *e, uint8_t *dst, size_t cap, frt_error *err)

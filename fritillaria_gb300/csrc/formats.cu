@@ -892,21 +892,6 @@ struct frt_fasta_compactor {
     Scanner s;
 };
 
-struct frt_columns {
-    int device = 0;
-    int format = 0;
-    cudaStream_t stream = nullptr;
-    SharedStream *shared = nullptr;
-    uint64_t n = 0, tail = 0, total = 0;
-    uint64_t info[3] = {0, 0, 0}; // proof, survivors, validated
-    int n_cols = 0;
-    const size_t *widths = nullptr;
-    uint8_t *cols = nullptr;
-    uint8_t *seq = nullptr; // FASTA bases
-    size_t col_off[16] = {}, col_bytes[16] = {};
-    const frt_inflate_batch *source = nullptr;
-    cudaEvent_t ready = nullptr;
-};
 
 namespace {
 

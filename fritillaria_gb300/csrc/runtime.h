@@ -91,6 +91,25 @@ struct frt_inflate_batch {
     bool owns_data = true; // false for a view into memory owned elsewhere (an engine's output)
 };
 
+// A set of device columns (FASTQ/BCF/FASTA scans, record fields): column k is
+// col_bytes[k] bytes at cols + col_off[k] (FASTA's bases in `seq`), elements of
+// widths[k] bytes.  Holds its source batch when its columns point into it.
+struct frt_columns {
+    int device = 0;
+    int format = 0;
+    cudaStream_t stream = nullptr;
+    frt::SharedStream *shared = nullptr;
+    uint64_t n = 0, tail = 0, total = 0;
+    uint64_t info[3] = {0, 0, 0}; // proof, survivors, validated
+    int n_cols = 0;
+    const size_t *widths = nullptr;
+    uint8_t *cols = nullptr;
+    uint8_t *seq = nullptr; // FASTA bases
+    size_t col_off[16] = {}, col_bytes[16] = {};
+    const frt_inflate_batch *source = nullptr;
+    cudaEvent_t ready = nullptr;
+};
+
 namespace frt {
 void batch_release(const frt_inflate_batch *b);
 int inflate_batch(frt_codec *c, const uint8_t *batch, size_t batch_len, const frt_span *spans, size_t n,

@@ -325,6 +325,56 @@ int frt_columns_column_to_host(const frt_columns *c, int column, void *dst, size
 void *frt_columns_ready_event(const frt_columns *c);
 void frt_columns_free(frt_columns *c);
 
+/* ---- record fields: opt-in device kernels over decoded BAM records ---------
+ * The reference reads these on the host, record by record: Record::aux_get
+ * (crates/fritillaria-bam/src/columnar/record.rs:286-294, over the Fields
+ * iterator of aux.rs:301-479), Record::cigar_resolved and
+ * has_long_cigar_placeholder (record.rs:316-357), decode_sequence (seq.rs), and
+ * the payload accessors name/cigar_raw/sequence_packed/qualities/aux_raw
+ * (record.rs:222-270).  Here each runs for every record of a decoded batch at
+ * once and returns an frt_columns; `unpack_sequences` and `compact` are the
+ * opt-ins of docs/device-api.md:261-263 and :443-444.  The record-batch forms
+ * keep the batch's inflated bytes alive as long as the result (offsets point
+ * into them); the engine forms read the engine's last run (one BAM bound) and
+ * their offsets are valid until its next run.  Results are ready when
+ * frt_columns_ready_event completes on the source's stream. */
+typedef enum {
+    FRT_AUXV_STATUS = 0,  /* u8: 0 absent, 1 present, 2 aux block malformed before the tag (aux_get's Err) */
+    FRT_AUXV_TYPE = 1,    /* u8: 'A' 'c' 'C' 's' 'S' 'i' 'I' 'f' 'Z' 'H' 'B' */
+    FRT_AUXV_SUBTYPE = 2, /* u8: the B array's element type */
+    FRT_AUXV_COUNT = 3,   /* u32: 1 for a scalar, string length for Z/H, elements for B */
+    FRT_AUXV_VALUE = 4,   /* i64: an integer scalar (sign- or zero-extended), the byte of A, the IEEE bits of f */
+    FRT_AUXV_OFFSET = 5,  /* u64: the value's bytes in the inflated batch (B: its first element) */
+    FRT_AUXV_COL_COUNT = 6
+} frt_aux_value_column;
+
+typedef enum {
+    FRT_CIGAR_COL_OFFSET = 0, /* u64: first op (u32 each) in the inflated batch */
+    FRT_CIGAR_COL_OPS = 1,    /* u32: ops */
+    FRT_CIGAR_COL_STATUS = 2, /* u8: 0 stored CIGAR, 1 long CIGAR from CG, 2 placeholder without a B:I CG */
+    FRT_CIGAR_COL_COUNT = 3
+} frt_cigar_column;
+
+typedef enum {
+    FRT_BASES_COL_OFFSETS = 0, /* u64, n + 1: record i's bases are DATA[OFFSETS[i], OFFSETS[i + 1]) */
+    FRT_BASES_COL_DATA = 1,    /* u8: "=ACMGRSVTWYHKDBN"[nibble], high nibble first */
+    FRT_BASES_COL_COUNT = 2
+} frt_bases_column;
+
+typedef enum {
+    FRT_COMPACT_COL_NAME_OFFSETS = 0, FRT_COMPACT_COL_NAME_DATA = 1,         /* name without its NUL */
+    FRT_COMPACT_COL_CIGAR_OFFSETS = 2, FRT_COMPACT_COL_CIGAR_DATA = 3,       /* stored ops, u32 each */
+    FRT_COMPACT_COL_SEQUENCE_OFFSETS = 4, FRT_COMPACT_COL_SEQUENCE_DATA = 5, /* 4-bit packed */
+    FRT_COMPACT_COL_QUALITY_OFFSETS = 6, FRT_COMPACT_COL_QUALITY_DATA = 7,
+    FRT_COMPACT_COL_AUX_OFFSETS = 8, FRT_COMPACT_COL_AUX_DATA = 9,           /* raw aux block */
+    FRT_COMPACT_COL_COUNT = 10 /* offsets: u64, n + 1 entries, in bytes of the data column */
+} frt_compact_column;
+
+int frt_record_batch_aux_lookup(const frt_record_batch *rb, const char tag[2], frt_columns **out, frt_error *err);
+int frt_record_batch_cigar_resolved(const frt_record_batch *rb, frt_columns **out, frt_error *err);
+int frt_record_batch_unpack_sequences(const frt_record_batch *rb, frt_columns **out, frt_error *err);
+int frt_record_batch_compact(const frt_record_batch *rb, frt_columns **out, frt_error *err);
+
 /* ---- BAI region resolution -------------------------------------------------
  * The index (crates/fritillaria-bam/src/bai.rs, the csi BinningIndex) turns a
  * region into chunks of virtual offsets: a record is in the query when its
@@ -514,6 +564,11 @@ int frt_autotune(frt_engine *e, const char *cache_path, int32_t force, frt_autot
 int frt_engine_column(const frt_engine *e, int column, void **ptr, size_t *bytes, size_t *width);
 int frt_engine_column_to_host(const frt_engine *e, int column, void *dst, size_t cap, frt_error *err);
 const uint8_t *frt_engine_inflated(const frt_engine *e, size_t *len);
+/* Record fields (see "record fields" above) over the engine's last run of one bound BAM. */
+int frt_engine_aux_lookup(const frt_engine *e, const char tag[2], frt_columns **out, frt_error *err);
+int frt_engine_cigar_resolved(const frt_engine *e, frt_columns **out, frt_error *err);
+int frt_engine_unpack_sequences(const frt_engine *e, frt_columns **out, frt_error *err);
+int frt_engine_compact(const frt_engine *e, frt_columns **out, frt_error *err);
 /* Copies the inflated bytes of the last run to host memory (cap >= len). */
 int frt_engine_inflated_to_host(const frt_engine *e, uint8_t *dst, size_t cap, frt_error *err);
 void *frt_engine_stream(const frt_engine *e);
