@@ -92,6 +92,7 @@ def parse_args():
     p.add_argument("--workload", choices=sorted(WORKLOADS) + sorted(MIXED) + sorted(SERVING), default="short_reads_20m")
     p.add_argument("--no-plain", action="store_true", help="skip the per-batch comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    p.add_argument("--no-fields", action="store_true", help="skip timing the record-field kernels")
     p.add_argument("--tuning-cache", default=str(TUNING_CACHE),
                    help="JSON cache of inflate tunings (read, and written on a miss)")
     p.add_argument("--retune", action="store_true", help="time the inflate tunings again even on a cache hit")
@@ -336,6 +337,41 @@ def run_plain(frt, host_bytes, blocks_per_batch=256):
     return records, inflated, dt, batches
 
 
+def record_fields(eng, records: int, peak: float) -> dict:
+    """The opt-in record-field kernels over the engine's records, each timed
+    once after a warm-up call (wall time of the call, result allocation and
+    totals read-back included), with the bytes each must read and write."""
+    import numpy as np
+    import torch
+
+    out = {}
+    seq = eng.column("seq_len").astype(np.uint64)
+    n_fields = int(eng.column("aux_count").astype(np.uint64).sum())
+    bases = int(seq.sum())
+    payload = int((eng.column("record_end").astype(np.int64) - 36).sum())
+    # per record: the columns read (record offset, starts, counts), the aux
+    # directory entries scanned (12 B each), the value or op bytes, the row written
+    algo = {"aux_lookup NM": records * (8 + 4 + 4 + 1 + 4 + 23) + 12 * n_fields,
+            "cigar_resolved": records * (8 + 2 + 4 + 4 + 8 + 13),
+            "unpack_sequences": bases // 2 + bases + records * (8 + 4 + 4 + 8 + 8),
+            "compact": 2 * payload + records * (8 + 6 * 4 + 5 * 8)}
+    calls = {"aux_lookup NM": lambda: eng.aux_lookup("NM"), "cigar_resolved": eng.cigar_resolved,
+             "unpack_sequences": eng.unpack_sequences, "compact": eng.compact}
+    for name, fn in calls.items():
+        fn().free()  # warm: allocator pools, module load
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = fn()
+        res.column_ptr(next(iter(res._cols)))
+        torch.cuda.synchronize()
+        ms = 1e3 * (time.perf_counter() - t0)
+        res.free()
+        gbs = algo[name] / (ms / 1e3) / 1e9
+        out[name] = {"ms": round(ms, 3), "algorithmic_bytes": algo[name], "gbs": round(gbs, 2),
+                     "hbm_frac": round(gbs / peak, 4)}
+    return out
+
+
 def run_ours(args, rank, world, local):
     import numpy as np
     import torch
@@ -420,13 +456,18 @@ def run_ours(args, rank, world, local):
     for _ in range(1):
         eng.run_host(hbuf)
     torch.cuda.synchronize()
+    steps_ms = []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        t1 = time.perf_counter()
         st2 = eng.run_host(hbuf)
+        steps_ms.append(round(1e3 * (time.perf_counter() - t1), 3))
         assert st2.status == 0
     e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, dist, "cuda")
     e2e = {"value": round(whole_job_gbs(inflated, world, 1, 1e3 * e2e_s), 3), "unit": "GB/s", "h2d_bytes_per_step": len(bgzf),
-           "d2h_bytes_per_step": 128, "ms_per_step": round(1e3 * e2e_s, 3)}
+           "d2h_bytes_per_step": 128, "ms_per_step": round(1e3 * e2e_s, 3), "step_ms": steps_ms}
+
+    fields = record_fields(eng, st.records, peak) if rank == 0 and not args.no_fields else None
 
     plain = None
     if not args.no_plain:
@@ -458,6 +499,7 @@ def run_ours(args, rank, world, local):
             "cpu_baseline": cpu,
             "e2e": e2e,
             "plain": plain,
+            "record_fields": fields,
             "gpu_launches": eng.launches_per_run() * args.steps,
             "clocks": clocks.summary(),
             "wall_s": round(wall, 3),
