@@ -304,6 +304,9 @@ def lib():
         "frt_fastq_scanner_create": (C.c_int, [C.c_int, _P, _P, _P]),
         "frt_fastq_scanner_destroy": (None, [_P]),
         "frt_fastq_decode": (C.c_int, [_P, _P, C.c_uint64, _P, _P]),
+        "frt_text_scanner_create": (C.c_int, [C.c_int, _P, _P, _P]),
+        "frt_text_scanner_destroy": (None, [_P]),
+        "frt_text_scan": (C.c_int, [_P, _P, C.c_uint64, C.c_int32, C.c_int32, _P, _P]),
         "frt_bcf_parse_header": (C.c_int, [_P, C.c_size_t, _P, _P, _P, _P]),
         "frt_bcf_scanner_create": (C.c_int, [C.c_int, _P, _P, _P]),
         "frt_bcf_scanner_destroy": (None, [_P]),
@@ -847,6 +850,31 @@ class FastqScanner(_Scanner):
         cb = self.decode(batch, start)
         proof, surv, val = cb.scan_info()
         return SpeculativeScan(cb.column("record_offsets"), cb.tail(), surv, val, proof)
+
+
+TEXT_COLUMNS = {"record_offsets": (0, np.uint64), "record_ends": (1, np.uint64), "header_offsets": (2, np.uint64),
+                "tabs": (3, np.uint64), "field_starts": (4, np.uint64)}
+
+
+class Dialect:
+    """Which leading bytes mark a header line (batch.rs:23-76): (comment, secondary or None)."""
+    SAM = (ord("@"), None)
+    VCF = (ord("#"), None)
+    GFF = (ord("#"), None)
+    BED = (ord("#"), None)
+
+
+class TextScanner(_Scanner):
+    """TextScanner (crates/fritillaria-cuda/src/text.rs:33-96) for SAM, VCF, BED,
+    GFF and GTF: records, header lines and each record's tab offsets."""
+    _create, _destroy = "frt_text_scanner_create", "frt_text_scanner_destroy"
+
+    def scan(self, batch: DeviceInflateBatch | None, start: int, dialect=Dialect.SAM) -> ColumnBatch:
+        comment, secondary = dialect
+        out, err = _P(), _Err()
+        _raise(lib().frt_text_scan(self._h, batch.handle if batch is not None else None, int(start), int(comment),
+                                   -1 if secondary is None else int(secondary), C.byref(out), C.byref(err)), err)
+        return ColumnBatch(out, TEXT_COLUMNS)
 
 
 def parse_bcf_header(data):

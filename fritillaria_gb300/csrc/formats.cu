@@ -172,6 +172,82 @@ struct FqIndex {
     }
 };
 
+// =============================================================================
+// Tab-delimited text: SAM, VCF, BED, GFF, GTF (kernels/text_scan.cu, src/text.rs)
+// =============================================================================
+// The reference appends line starts with an atomic, sorts them on the host and
+// walks each line with one thread.  Here the line starts come in order from the
+// newline index (the FASTQ one), the records and header lines are compacted by
+// scans, and a warp per record counts, then writes, its tab offsets in order.
+
+// Per line: record (not blank, not a header), header line, or blank
+// (text_find_lines, text_scan.cu:41-72).
+__global__ void k_tx_lines(FqIndex ix, u32 comment, u32 secondary, u32 *is_rec, u32 *is_hdr)
+{
+    u32 k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ix.n_lines) return;
+    const u64 s = ix.ls(k);
+    u32 r = 0, h = 0;
+    if (s < ix.len) {
+        const u32 first = ix.buf[s];
+        if (first != '\n') {
+            h = (first == comment || (secondary < 256u && first == secondary)) ? 1u : 0u;
+            r = 1u - h;
+        }
+    }
+    is_rec[k] = r;
+    is_hdr[k] = h;
+}
+
+// A line ends at its newline, or at the end of the batch (text_count_fields).
+__global__ void k_tx_place(FqIndex ix, const u32 *is_rec, const u32 *rec_pos, const u32 *is_hdr,
+                           const u32 *hdr_pos, u64 *rec_off, u64 *rec_end, u64 *hdr_off)
+{
+    u32 k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ix.n_lines) return;
+    const u64 s = ix.ls(k);
+    if (is_rec[k]) {
+        rec_off[rec_pos[k]] = s;
+        rec_end[rec_pos[k]] = k < ix.n_nl ? ix.nl[k] : ix.len;
+    }
+    if (is_hdr[k]) hdr_off[hdr_pos[k]] = s;
+}
+
+// A warp per record, consecutive lanes on consecutive bytes.
+__global__ void k_tx_count_tabs(const u8 *buf, const u64 *rec_off, const u64 *rec_end, u32 n, u32 *counts)
+{
+    const u32 r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (r >= n) return;
+    const u64 a = rec_off[r], b = rec_end[r];
+    u32 c = 0;
+    for (u64 q = a + lane; q < b; q += 32) c += buf[q] == '\t' ? 1u : 0u;
+#pragma unroll
+    for (int d = 16; d; d >>= 1) c += __shfl_down_sync(FRT_FULL_MASK, c, d);
+    if (lane == 0) counts[r] = c;
+}
+
+__global__ void k_tx_emit_tabs(const u8 *buf, const u64 *rec_off, const u64 *rec_end, u32 n, const u32 *tab_base,
+                               u64 *tabs)
+{
+    const u32 r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (r >= n) return;
+    const u64 a = rec_off[r], b = rec_end[r];
+    u32 at = tab_base[r];
+    for (u64 q0 = a; q0 < b; q0 += 32) {
+        const u64 q = q0 + lane;
+        const bool t = q < b && buf[q] == '\t';
+        const u32 m = __ballot_sync(FRT_FULL_MASK, t);
+        if (t) tabs[at + __popc(m & lanemask_lt())] = q;
+        at += __popc(m);
+    }
+}
+
+__global__ void k_tx_starts(const u32 *tab_base, u32 n1, u64 *starts)
+{
+    u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n1) starts[i] = tab_base[i];
+}
+
 __global__ void k_fq_lines(FqIndex ix, u32 *flags)
 {
     u32 k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -853,7 +929,8 @@ unsigned grid_for(u64 n, unsigned block) { return (unsigned)((n + block - 1) / b
 
 namespace {
 
-enum { FMT_FASTQ = 1, FMT_BCF = 2, FMT_FASTA = 3 };
+enum { FMT_FASTQ = 1, FMT_BCF = 2, FMT_FASTA = 3, FMT_TEXT = 4 };
+const size_t kTextWidths[FRT_TEXT_COL_COUNT] = {8, 8, 8, 8, 8};
 
 const size_t kFastqWidths[FRT_FASTQ_COL_COUNT] = {8, 4, 4, 4, 4, 4};
 const size_t kBcfWidths[FRT_BCF_COL_COUNT] = {4, 4, 4, 4, 2, 2, 4, 1, 8, 4, 4, 4, 4, 4};
@@ -889,6 +966,9 @@ struct frt_bcf_scanner {
     Scanner s;
 };
 struct frt_fasta_compactor {
+    Scanner s;
+};
+struct frt_text_scanner {
     Scanner s;
 };
 
@@ -1521,4 +1601,164 @@ extern "C" void frt_columns_free(frt_columns *c)
         columns_discard(c);
     }
     if (src) batch_release(src);
+}
+
+// ---- tab-delimited text --------------------------------------------------------
+
+extern "C" int frt_text_scanner_create(int device, void *stream, frt_text_scanner **out, frt_error *err)
+{
+    if (!out) return FRT_ERR_INVALID_ARGUMENT;
+    frt_text_scanner *s = new frt_text_scanner;
+    int rc = scanner_create(device, stream, &s->s, err);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return FRT_OK;
+}
+
+extern "C" void frt_text_scanner_destroy(frt_text_scanner *s)
+{
+    if (!s) return;
+    stream_release(s->s.shared);
+    delete s;
+}
+
+// TextScanner::scan (crates/fritillaria-cuda/src/text.rs:233-420): records,
+// their ends, header lines and the field table; the tail is the last record's
+// start when that record runs to the end of the batch, else the batch end.
+extern "C" int frt_text_scan(frt_text_scanner *sc, const frt_inflate_batch *b, uint64_t start, int32_t comment,
+                             int32_t secondary, frt_columns **out, frt_error *err)
+{
+    if (!sc || !out || comment < 0 || comment > 255 || secondary > 255) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr,
+                  "null argument, or a header byte outside 0..255 (secondary -1: none)");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    Scanner &s = sc->s;
+    DeviceGuardLite g(s.device);
+    std::lock_guard<std::mutex> lk(s.mu);
+    uint64_t len = b && b->data ? b->len : 0;
+    auto finish = [&](frt_columns *c, uint64_t n_hdr, uint64_t n_tabs) {
+        c->col_bytes[FRT_TEXT_COL_HEADER_OFFSETS] = 8 * n_hdr;
+        c->col_bytes[FRT_TEXT_COL_TABS] = 8 * n_tabs;
+        c->col_bytes[FRT_TEXT_COL_FIELD_STARTS] = c->n ? 8 * (c->n + 1) : 0;
+        size_t off = 0;
+        for (int k = 0; k < FRT_TEXT_COL_COUNT; ++k) {
+            c->col_off[k] = off;
+            off += (c->col_bytes[k] + 255) & ~(size_t)255;
+        }
+        c->info[0] = n_hdr;
+        c->total = n_tabs;
+        return columns_alloc(c, err);
+    };
+    if (start >= len) { // empty(start.min(len))
+        frt_columns *c = columns_new(s, FMT_TEXT, kTextWidths, FRT_TEXT_COL_COUNT, 0);
+        c->tail = start < len ? start : len;
+        int rc = finish(c, 0, 0);
+        if (rc) {
+            columns_discard(c);
+            return rc;
+        }
+        return columns_finish(c, b, out);
+    }
+    int rc = check_batch(s, b, err);
+    if (rc) return rc;
+    if (len - start >= 0xffffffffull) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "text batch of %llu bytes exceeds 4 GiB",
+                  (unsigned long long)(len - start));
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    cudaStream_t st = s.stream;
+    Work w(st);
+    const u64 tbase = start & ~15ull;
+    const u64 n_tiles = (len - tbase + TILE - 1) / TILE;
+    const bool aligned = ((uintptr_t)b->data & 15) == 0;
+    u32 *tile_count, *tile_base, *partials, *d_u32;
+    if ((rc = w.get(&tile_count, n_tiles, err)) || (rc = w.get(&tile_base, n_tiles + 1, err)) ||
+        (rc = w.get(&partials, frt_scan_partials_len(n_tiles) + frt_scan_partials_len(len) + 8, err)) ||
+        (rc = w.get(&d_u32, 8, err)))
+        return rc;
+    k_fq_nl_count<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, tbase, aligned, tile_count);
+    LAUNCH_OK("launching the newline count");
+    cudaError_t e = frt_launch_scan_u32(tile_count, n_tiles, partials, tile_base, d_u32, st);
+    if (e != cudaSuccess) return cuda_fail(err, e, "scanning newline counts");
+    uint32_t n_nl = 0;
+    if ((rc = read_back(st, d_u32, &n_nl, 4, err, "newline count"))) return rc;
+    u64 *nl;
+    if ((rc = w.get(&nl, (size_t)n_nl + 1, err))) return rc;
+    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, tbase, aligned, tile_base, nl);
+    LAUNCH_OK("launching the newline index");
+    uint32_t n_lines = n_nl + 1; // line starts: start, and one past every newline that is not the last byte
+    {
+        uint64_t last_nl = 0;
+        if (n_nl && (rc = read_back(st, nl + n_nl - 1, &last_nl, 8, err, "last newline"))) return rc;
+        if (n_nl && last_nl + 1 >= len) n_lines = n_nl;
+    }
+    FqIndex ix{b->data, start, len, nl, n_nl, n_lines};
+    u32 *is_rec, *is_hdr, *rec_pos, *hdr_pos;
+    if ((rc = w.get(&is_rec, n_lines, err)) || (rc = w.get(&is_hdr, n_lines, err)) ||
+        (rc = w.get(&rec_pos, (size_t)n_lines + 1, err)) || (rc = w.get(&hdr_pos, (size_t)n_lines + 1, err)))
+        return rc;
+    k_tx_lines<<<grid_for(n_lines, 256), 256, 0, st>>>(ix, (u32)comment, secondary < 0 ? 0xffffffffu : (u32)secondary,
+                                                         is_rec, is_hdr);
+    LAUNCH_OK("launching the line kinds");
+    uint32_t counts[2] = {0, 0};
+    if ((e = frt_launch_scan_u32(is_rec, n_lines, partials, rec_pos, d_u32, st)) != cudaSuccess ||
+        (e = frt_launch_scan_u32(is_hdr, n_lines, partials, hdr_pos, d_u32 + 1, st)) != cudaSuccess)
+        return cuda_fail(err, e, "scanning line kinds");
+    if ((rc = read_back(st, d_u32, counts, 8, err, "line kinds"))) return rc;
+    const uint32_t n_rec = counts[0], n_hdr = counts[1];
+    u64 *rec_off, *rec_end, *hdr_off;
+    if ((rc = w.get(&rec_off, (size_t)n_rec + 1, err)) || (rc = w.get(&rec_end, (size_t)n_rec + 1, err)) ||
+        (rc = w.get(&hdr_off, (size_t)n_hdr + 1, err)))
+        return rc;
+    k_tx_place<<<grid_for(n_lines, 256), 256, 0, st>>>(ix, is_rec, rec_pos, is_hdr, hdr_pos, rec_off, rec_end,
+                                                         hdr_off);
+    LAUNCH_OK("placing lines");
+    u32 *tab_count, *tab_base;
+    uint32_t n_tabs = 0;
+    uint64_t tail = len;
+    if (n_rec) {
+        if ((rc = w.get(&tab_count, n_rec, err)) || (rc = w.get(&tab_base, (size_t)n_rec + 1, err))) return rc;
+        k_tx_count_tabs<<<grid_for((u64)n_rec * 32, 256), 256, 0, st>>>(b->data, rec_off, rec_end, n_rec, tab_count);
+        LAUNCH_OK("counting fields");
+        if ((e = frt_launch_scan_u32(tab_count, n_rec, partials, tab_base, d_u32, st)) != cudaSuccess)
+            return cuda_fail(err, e, "scanning field counts");
+        uint64_t last[2] = {0, 0};
+        if ((rc = read_back(st, d_u32, &n_tabs, 4, err, "field count")) ||
+            (rc = read_back(st, rec_off + n_rec - 1, &last[0], 8, err, "last record")) ||
+            (rc = read_back(st, rec_end + n_rec - 1, &last[1], 8, err, "last record")))
+            return rc;
+        tail = last[1] >= len ? last[0] : len; // text.rs:393-397
+    }
+    frt_columns *c = columns_new(s, FMT_TEXT, kTextWidths, FRT_TEXT_COL_COUNT, n_rec);
+    c->tail = tail;
+    if ((rc = finish(c, n_hdr, n_tabs))) {
+        columns_discard(c);
+        return rc;
+    }
+    auto put = [&](int k, const void *src) {
+        return c->col_bytes[k] ? cudaMemcpyAsync(colp<u8>(c, k), src, c->col_bytes[k], cudaMemcpyDeviceToDevice, st)
+                               : cudaSuccess;
+    };
+    if ((e = put(FRT_TEXT_COL_RECORD_OFFSETS, rec_off)) != cudaSuccess ||
+        (e = put(FRT_TEXT_COL_RECORD_ENDS, rec_end)) != cudaSuccess ||
+        (e = put(FRT_TEXT_COL_HEADER_OFFSETS, hdr_off)) != cudaSuccess) {
+        columns_discard(c);
+        return cuda_fail(err, e, "placing text columns");
+    }
+    if (n_rec) {
+        if (n_tabs)
+            k_tx_emit_tabs<<<grid_for((u64)n_rec * 32, 256), 256, 0, st>>>(
+                b->data, rec_off, rec_end, n_rec, tab_base, colp<u64>(c, FRT_TEXT_COL_TABS));
+        k_tx_starts<<<grid_for((u64)n_rec + 1, 256), 256, 0, st>>>(tab_base, n_rec + 1,
+                                                                   colp<u64>(c, FRT_TEXT_COL_FIELD_STARTS));
+        if ((e = cudaGetLastError()) != cudaSuccess) {
+            columns_discard(c);
+            return cuda_fail(err, e, "launching the field table");
+        }
+    }
+    return columns_finish(c, b, out);
 }

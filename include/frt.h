@@ -242,6 +242,7 @@ void frt_record_batch_free(frt_record_batch *rb);
  * order, the tail to carry into the next batch, and how the boundaries were
  * established.  The handle keeps its inflate batch alive. */
 typedef struct frt_fastq_scanner frt_fastq_scanner;
+typedef struct frt_text_scanner frt_text_scanner;
 typedef struct frt_bcf_scanner frt_bcf_scanner;
 typedef struct frt_fasta_compactor frt_fasta_compactor;
 typedef struct frt_columns frt_columns;
@@ -324,6 +325,32 @@ int frt_columns_column(const frt_columns *c, int column, void **ptr, size_t *byt
 int frt_columns_column_to_host(const frt_columns *c, int column, void *dst, size_t cap, frt_error *err);
 void *frt_columns_ready_event(const frt_columns *c);
 void frt_columns_free(frt_columns *c);
+
+/* ---- tab-delimited text (SAM, VCF, BED, GFF, GTF) ---------------------------
+ * TextScanner::scan (crates/fritillaria-cuda/src/text.rs:79-96, 233-420) over
+ * kernels/text_scan.cu: the lines of a device batch from `start`, split into
+ * records and header lines by their first byte (Dialect, crates/fritillaria-text/
+ * src/columnar/batch.rs:23-76: `comment`, and `secondary` or -1), blank lines
+ * skipped, each record's tab offsets in a flat table.  As the reference's
+ * device path: a last line without a newline is a record ending at the batch
+ * end, and the tail is then its start (else the batch end; an empty batch or
+ * start at/after its end: min(start, len)).  Tables are sized from exact
+ * counts, so there is no line-capacity error.  frt_columns_len = records;
+ * frt_columns_tail = tail; scan_info's first value = header lines. */
+typedef enum {
+    FRT_TEXT_COL_RECORD_OFFSETS = 0, /* u64, records */
+    FRT_TEXT_COL_RECORD_ENDS = 1,    /* u64, records: one past the last byte, newline excluded */
+    FRT_TEXT_COL_HEADER_OFFSETS = 2, /* u64, header lines */
+    FRT_TEXT_COL_TABS = 3,           /* u64: every tab offset, grouped by record */
+    FRT_TEXT_COL_FIELD_STARTS = 4,   /* u64, records + 1 (none for no records): record i's tabs are
+                                        TABS[FIELD_STARTS[i], FIELD_STARTS[i + 1]) */
+    FRT_TEXT_COL_COUNT = 5
+} frt_text_column;
+
+int frt_text_scanner_create(int device, void *stream, frt_text_scanner **out, frt_error *err);
+void frt_text_scanner_destroy(frt_text_scanner *s);
+int frt_text_scan(frt_text_scanner *s, const frt_inflate_batch *batch, uint64_t start, int32_t comment,
+                  int32_t secondary, frt_columns **out, frt_error *err);
 
 /* ---- record fields: opt-in device kernels over decoded BAM records ---------
  * The reference reads these on the host, record by record: Record::aux_get

@@ -43,7 +43,7 @@ def build_ref() -> Path | None:
     REF_DIR.mkdir(exist_ok=True)
     deps = [HERE / "ref_driver.cpp", HERE / "ref_shim.h"] + [REFERENCE_KERNELS / f for f in
                                                             ("inflate.cu", "crc32.cu", "bam_decode.cu", "fastq_scan.cu", "bcf_scan.cu",
-                                                             "fasta_compact.cu")]
+                                                             "fasta_compact.cu", "text_scan.cu")]
     if _newer(REF_LIB, deps):
         _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-w", f"-I{HERE}", f"-I{REFERENCE_KERNELS}",
               "-o", str(REF_LIB), str(HERE / "ref_driver.cpp")])

@@ -143,3 +143,29 @@ def fasta_compact(buf) -> dict:
             L.ref_fasta_compact_scan(src.ctypes.data_as(_P), C.c_ulonglong(src.size), dst.ctypes.data_as(_P))
     return {"sequence": seq[:-1], "sequence_offsets": layout["sequence_offsets"],
             "sequence_lengths": layout["sequence_lengths"], "record_offsets": starts[:n].copy()}
+
+
+def text_scan(buf: np.ndarray, start: int, comment: int, secondary: int | None):
+    """TextScanner::scan (text.rs:233-420) over text_scan.cu: dict of record
+    offsets, record ends, header offsets, tabs, field starts and the tail;
+    raises when the reference reports more lines than its slots."""
+    L = _need()
+    buf = np.ascontiguousarray(buf, dtype=np.uint8)
+    cap_lines = buf.size + 1
+    cap_tabs = int(np.count_nonzero(buf == 9)) + 1
+    rec_off = np.zeros(cap_lines, np.uint64)
+    rec_end = np.zeros(cap_lines, np.uint64)
+    hdr_off = np.zeros(cap_lines, np.uint64)
+    tabs = np.zeros(cap_tabs, np.uint64)
+    starts = np.zeros(cap_lines + 1, np.uint64)
+    n_rec, n_hdr, n_tabs, tail = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+    rc = L.ref_text_scan(buf.ctypes.data_as(_P), C.c_uint64(buf.size), C.c_uint64(start), C.c_uint(comment),
+                         C.c_uint(0xFFFFFFFF if secondary is None else secondary), rec_off.ctypes.data_as(_P),
+                         rec_end.ctypes.data_as(_P), hdr_off.ctypes.data_as(_P), tabs.ctypes.data_as(_P),
+                         starts.ctypes.data_as(_P), C.c_uint64(cap_lines), C.c_uint64(cap_tabs), C.byref(n_rec),
+                         C.byref(n_hdr), C.byref(n_tabs), C.byref(tail))
+    if rc:
+        raise RuntimeError(f"reference text scan failed ({rc})")
+    n = n_rec.value
+    return {"record_offsets": rec_off[:n], "record_ends": rec_end[:n], "header_offsets": hdr_off[:n_hdr.value],
+            "tabs": tabs[:n_tabs.value], "field_starts": starts[:n + 1] if n else starts[:0], "tail": tail.value}

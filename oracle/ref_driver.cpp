@@ -34,6 +34,9 @@ namespace ref_bcf {
 namespace ref_fasta {
 #include "fasta_compact.cu"
 }
+namespace ref_text {
+#include "text_scan.cu"
+}
 
 namespace {
 
@@ -317,6 +320,62 @@ void ref_fasta_compact_scan(const unsigned char *src, unsigned long long span, u
     threadIdx.x = 0;
     blockDim.x = 1;
     ref_fasta::fasta_compact_scan(src, span, dst);
+}
+
+/*
+ * TextScanner::scan (crates/fritillaria-cuda/src/text.rs:233-420): text_find_lines
+ * over every byte from start into max(len / 8, 1024) slots (overflow is an
+ * error), the offsets sorted and split by kind, text_count_fields per record,
+ * the host prefix sum, text_write_fields, and the tail rule.  Returns 0, 1 when
+ * the line slots overflow, 2 when the caller's arrays are too small.
+ */
+int ref_text_scan(const unsigned char *buf, unsigned long long len, unsigned long long start, unsigned int comment,
+                  unsigned int secondary, unsigned long long *rec_off, unsigned long long *rec_end,
+                  unsigned long long *hdr_off, unsigned long long *tabs, unsigned long long *starts,
+                  unsigned long long cap_lines, unsigned long long cap_tabs, unsigned long long *n_rec,
+                  unsigned long long *n_hdr, unsigned long long *n_tabs, unsigned long long *tail)
+{
+    *n_rec = *n_hdr = *n_tabs = 0;
+    if (start >= len) {
+        *tail = start < len ? start : len;
+        return 0;
+    }
+    unsigned long long capacity = len / 8 > 1024 ? len / 8 : 1024;
+    std::vector<unsigned long long> lines(capacity);
+    std::vector<unsigned char> kinds(capacity);
+    unsigned int count = 0, overflow = 0;
+    for_threads(len - start, [&] {
+        ref_text::text_find_lines(buf, len, start, comment, secondary, lines.data(), kinds.data(), &count,
+                                  (unsigned)capacity, &overflow);
+    });
+    if (overflow) return 1;
+    std::vector<std::pair<unsigned long long, unsigned char>> pairs;
+    for (unsigned i = 0; i < count; ++i) pairs.emplace_back(lines[i], kinds[i]);
+    std::sort(pairs.begin(), pairs.end());
+    std::vector<unsigned long long> recs, hdrs;
+    for (auto &pr : pairs) (pr.second == 1 ? hdrs : recs).push_back(pr.first);
+    if (recs.size() > cap_lines || hdrs.size() > cap_lines) return 2;
+    for (size_t i = 0; i < hdrs.size(); ++i) hdr_off[i] = hdrs[i];
+    *n_hdr = hdrs.size();
+    *tail = len;
+    const unsigned n = (unsigned)recs.size();
+    if (n == 0) return 0;
+    std::vector<unsigned int> counts(n);
+    std::vector<unsigned long long> ends(n);
+    for_threads(n, [&] { ref_text::text_count_fields(buf, len, recs.data(), n, counts.data(), ends.data()); });
+    std::vector<unsigned long long> st(n + 1, 0);
+    for (unsigned i = 0; i < n; ++i) st[i + 1] = st[i] + counts[i];
+    if (st[n] > cap_tabs) return 2;
+    for_threads(n, [&] { ref_text::text_write_fields(buf, recs.data(), ends.data(), n, st.data(), tabs); });
+    for (unsigned i = 0; i < n; ++i) {
+        rec_off[i] = recs[i];
+        rec_end[i] = ends[i];
+    }
+    for (unsigned i = 0; i <= n; ++i) starts[i] = st[i];
+    *n_rec = n;
+    *n_tabs = st[n];
+    *tail = ends[n - 1] >= len ? recs[n - 1] : len;
+    return 0;
 }
 
 } // extern "C"

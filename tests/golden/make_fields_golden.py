@@ -16,6 +16,12 @@ malformed aux block after a valid field, odd and empty sequences.  Their
 expected fields come from oracle/fields.py at test time, which
 tests/test_oracle_fields.py pins to those unit tests' assertions.
 
+text_real.npz: the reference's text fixtures written by samtools, bcftools,
+NCBI and UCSC (reads.sam cut at a line end after 120 KB, calls.vcf,
+cytoband.bed, lambda.gff3, lambda.gtf), for the text scanner; its expected
+tables come from oracle/text.py, which tests/test_oracle_text.py pins to the
+reference's text_scan.cu compiled as host code.
+
 Run from the repository root with the reference tree present:
     python tests/golden/make_fields_golden.py
 """
@@ -103,7 +109,22 @@ def cases() -> bytes:
     return header() + b"".join(recs)
 
 
+def text_fixture():
+    """text_real.npz: the reference's real text fixtures written by samtools,
+    bcftools, NCBI and UCSC (testdata/README.md): reads.sam cut at a line end
+    after 120 KB, calls.vcf, cytoband.bed, lambda.gff3, lambda.gtf whole."""
+    out = {}
+    for name in ("reads.sam", "calls.vcf", "cytoband.bed", "lambda.gff3", "lambda.gtf"):
+        b = (TESTDATA / name).read_bytes()
+        if name == "reads.sam":
+            b = b[: b.index(b"\n", 120_000) + 1]
+        out[name.replace(".", "_")] = np.frombuffer(b, np.uint8)
+    np.savez_compressed(HERE / "text_real.npz", **out)
+    print("text_real", (HERE / "text_real.npz").stat().st_size)
+
+
 def main():
+    text_fixture()
     raw = np.frombuffer(cases(), np.uint8)
     np.savez_compressed(HERE / "fields_cases.npz", bgzf=synth.bgzf(raw, packing="full", levels=(6, 6)))
 

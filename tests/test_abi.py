@@ -13,7 +13,7 @@ import pytest
 from oracle import oracle
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("fields_"))  # record-field inputs have their own tests
+CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("fields_", "text_")))  # record-field and text inputs have their own tests
 
 
 @pytest.fixture(scope="module")

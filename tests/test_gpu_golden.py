@@ -13,7 +13,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("fields_"))  # record-field inputs have their own tests
+CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("fields_", "text_")))  # record-field and text inputs have their own tests
 BAM_CASES = [c for c in CASES if c.startswith("bam_")]
 REF_COLS = ["ref_id", "pos", "flags", "mapq", "seq_len", "mate_ref_id", "mate_pos", "tlen", "cigar_start",
             "sequence_start", "quality_start", "aux_start", "record_end"]
