@@ -21,6 +21,7 @@
 // bind() runs the stages once eagerly to size every buffer, then captures the
 // stage sequence as a CUDA graph; run() replays it.
 
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -381,6 +382,22 @@ __global__ void k_check_counts(EngineDevState *st, u64 rec_cap, u64 aux_cap)
     if (st->totals[0] != rec_cap || (u64)st->n_aux != aux_cap) st->capacity_err = 1;
 }
 
+// The error words of the per-group inflate launches of a pipelined host run:
+// member indices there are relative to the group; the first failing member in
+// file order wins, as in the single launch.
+__global__ void k_merge_group_errors(const u64 *errs, const u64 *first, u32 groups, EngineDevState *st)
+{
+    if (threadIdx.x != 0) return;
+    u64 best = ~0ull;
+    for (u32 g = 0; g < groups; ++g) {
+        const u64 w = errs[g];
+        if (w == ~0ull) continue;
+        const u64 v = ((first[g] + (w >> 8)) << 8) | (w & 0xffull);
+        if (v < best) best = v;
+    }
+    st->block_err = best;
+}
+
 } // namespace
 
 // ===========================================================================
@@ -437,6 +454,18 @@ struct frt_engine {
     frt_fasta_compactor *fasta = nullptr;
     int decode_rc = FRT_OK;
     frt_error decode_err{};
+    // host-buffer runs with the upload overlapped (run_host_pipelined)
+    struct HostPipe {
+        cudaStream_t copy = nullptr, side = nullptr;
+        cudaEvent_t plan = nullptr;
+        std::vector<cudaEvent_t> up, done;
+        uint8_t *staging = nullptr; // pinned plan
+        size_t staging_bytes = 0;
+        u64 *d_count = nullptr;     // members per group
+        u64 *d_errs = nullptr;      // per-group error words
+        u64 *d_first = nullptr;     // first member of each group
+        u32 *d_heads = nullptr;     // per-group queue heads
+    } pipe;
 };
 
 namespace {
@@ -710,6 +739,19 @@ extern "C" void frt_engine_destroy(frt_engine *e)
     if (!e) return;
     DeviceGuardLite g(e->device);
     free_all(e);
+    {
+        auto &pp = e->pipe;
+        if (pp.copy) cudaStreamSynchronize(pp.copy);
+        if (pp.side) cudaStreamSynchronize(pp.side);
+        for (cudaEvent_t ev : pp.up) cudaEventDestroy(ev);
+        for (cudaEvent_t ev : pp.done) cudaEventDestroy(ev);
+        if (pp.plan) cudaEventDestroy(pp.plan);
+        if (pp.copy) cudaStreamDestroy(pp.copy);
+        if (pp.side) cudaStreamDestroy(pp.side);
+        if (pp.staging) cudaFreeHost(pp.staging);
+        for (void *q : {(void *)pp.d_count, (void *)pp.d_errs, (void *)pp.d_first, (void *)pp.d_heads})
+            if (q) cudaFree(q);
+    }
     frt_bam_decoder_destroy(e->bam_dec);
     frt_fastq_scanner_destroy(e->fastq);
     frt_bcf_scanner_destroy(e->bcf);
@@ -1199,6 +1241,159 @@ extern "C" int frt_engine_finish(frt_engine *e, frt_engine_stats *stats, frt_err
     return rc;
 }
 
+namespace {
+
+constexpr int kPipeSlices = 8; // upload slices, and at most this many inflate groups
+
+// A host-buffer run of one bound BAM with the upload overlapped: the file goes
+// to the device in slices on a copy stream while the host walks the member
+// headers (the plan the device front would compute: member spans, trailers,
+// output offsets); each group of members whose bytes have all arrived is
+// inflated by its own launch of the persistent kernel (longest member first
+// within the group), alternating two streams so a launch fills the tail of the
+// one before; the record stages then run on the engine stream.  Returns 1 when
+// the host plan does not match the bound file (the caller then runs the
+// single-launch path on the uploaded bytes), else an frt_status.
+int run_host_pipelined(frt_engine *e, const uint8_t *host, size_t len, frt_error *err)
+{
+    auto &pp = e->pipe;
+    cudaError_t ce;
+    if (!pp.copy) {
+        if ((ce = cudaStreamCreateWithFlags(&pp.copy, cudaStreamNonBlocking)) != cudaSuccess ||
+            (ce = cudaStreamCreateWithFlags(&pp.side, cudaStreamNonBlocking)) != cudaSuccess ||
+            (ce = cudaEventCreateWithFlags(&pp.plan, cudaEventDisableTiming)) != cudaSuccess)
+            return cuda_fail(err, ce, "creating the upload streams");
+        pp.up.resize(kPipeSlices);
+        pp.done.resize(kPipeSlices);
+        for (int k = 0; k < kPipeSlices; ++k)
+            if ((ce = cudaEventCreateWithFlags(&pp.up[k], cudaEventDisableTiming)) != cudaSuccess ||
+                (ce = cudaEventCreateWithFlags(&pp.done[k], cudaEventDisableTiming)) != cudaSuccess)
+                return cuda_fail(err, ce, "creating the upload events");
+        if ((ce = cudaMalloc(&pp.d_count, 8 * kPipeSlices)) != cudaSuccess ||
+            (ce = cudaMalloc(&pp.d_errs, 8 * kPipeSlices)) != cudaSuccess ||
+            (ce = cudaMalloc(&pp.d_first, 8 * kPipeSlices)) != cudaSuccess ||
+            (ce = cudaMalloc(&pp.d_heads, 4 * kPipeSlices)) != cudaSuccess)
+            return cuda_fail(err, ce, "allocating the group state");
+    }
+    // the previous run's work on the side stream is done before its buffers are reused
+    if ((ce = cudaStreamWaitEvent(pp.copy, pp.plan, 0)) != cudaSuccess) return cuda_fail(err, ce, "ordering uploads");
+    u64 slice_end[kPipeSlices];
+    for (int k = 0; k < kPipeSlices; ++k) {
+        const u64 a = (u64)len * k / kPipeSlices, b = (u64)len * (k + 1) / kPipeSlices;
+        slice_end[k] = b;
+        if (b > a && (ce = cudaMemcpyAsync((void *)(e->in + a), host + a, b - a, cudaMemcpyHostToDevice, pp.copy)) !=
+                         cudaSuccess)
+            return cuda_fail(err, ce, "uploading the file");
+        if ((ce = cudaEventRecord(pp.up[k], pp.copy)) != cudaSuccess) return cuda_fail(err, ce, "uploading the file");
+    }
+    // the plan, on the host, while the slices travel
+    std::vector<frt_span> spans;
+    size_t consumed = 0;
+    frt_error scratch{};
+    if (discover(host, len, 0, spans, &consumed, &scratch) != FRT_OK || consumed != len || spans.size() != e->n_cap)
+        return 1;
+    const u64 n = spans.size();
+    u64 total = 0;
+    for (const auto &sp : spans) total += sp.isize;
+    if (total > e->out_cap) return 1;
+    const size_t need = n * (8 + 4 + 4 + 4 + 8 + 4) + 8 * (n + 1) + sizeof(EngineDevState) + 8 * 4 * kPipeSlices + 64;
+    if (need > pp.staging_bytes) {
+        if (pp.staging) cudaFreeHost(pp.staging);
+        pp.staging = nullptr;
+        if ((ce = cudaHostAlloc(&pp.staging, need, cudaHostAllocDefault)) != cudaSuccess)
+            return cuda_fail(err, ce, "allocating the plan staging");
+        pp.staging_bytes = need;
+    }
+    uint8_t *at = pp.staging;
+    auto take = [&](size_t bytes) {
+        uint8_t *q = at;
+        at += (bytes + 7) & ~(size_t)7;
+        return q;
+    };
+    u64 *h_in_off = (u64 *)take(8 * n), *h_coff = (u64 *)take(8 * n), *h_out_off = (u64 *)take(8 * (n + 1));
+    u32 *h_in_len = (u32 *)take(4 * n), *h_isize = (u32 *)take(4 * n), *h_crc = (u32 *)take(4 * n);
+    u32 *h_order = (u32 *)take(4 * n);
+    EngineDevState *h_st = (EngineDevState *)take(sizeof(EngineDevState));
+    u64 *h_count = (u64 *)take(8 * kPipeSlices), *h_first = (u64 *)take(8 * kPipeSlices);
+    u64 acc = 0;
+    for (u64 m = 0; m < n; ++m) {
+        h_in_off[m] = spans[m].payload_start;
+        h_in_len[m] = (u32)spans[m].payload_len;
+        h_isize[m] = spans[m].isize;
+        h_crc[m] = spans[m].crc32;
+        h_coff[m] = spans[m].compressed_offset;
+        h_out_off[m] = acc;
+        acc += spans[m].isize;
+    }
+    h_out_off[n] = acc;
+    // groups: members whose last byte lies in slice k or before, not yet taken
+    u64 first[kPipeSlices + 1], m0 = 0;
+    int groups = 0;
+    for (int k = 0; k < kPipeSlices; ++k) {
+        u64 m1 = m0;
+        while (m1 < n && spans[m1].payload_start + spans[m1].payload_len + 8 <= slice_end[k]) ++m1;
+        first[k] = m0;
+        h_first[k] = m0;
+        h_count[k] = m1 - m0;
+        // longest first within the group, as the single launch's queue
+        std::vector<u32> idx(m1 - m0);
+        for (u64 q = 0; q < m1 - m0; ++q) idx[q] = (u32)q;
+        std::stable_sort(idx.begin(), idx.end(), [&](u32 a, u32 b) {
+            return spans[m0 + a].payload_len > spans[m0 + b].payload_len;
+        });
+        std::copy(idx.begin(), idx.end(), h_order + m0);
+        m0 = m1;
+        groups = k + 1;
+    }
+    if (m0 != n) return 1;
+    first[kPipeSlices] = n;
+    memset(h_st, 0, sizeof(EngineDevState));
+    h_st->block_err = ~0ull;
+    h_st->n_members = n;
+    h_st->inflated_total = acc;
+    cudaStream_t s = e->stream;
+    struct Copy {
+        void *dst;
+        const void *src;
+        size_t bytes;
+    } copies[] = {{e->in_off, h_in_off, 8 * n},   {e->coffset, h_coff, 8 * n},  {e->out_off, h_out_off, 8 * (n + 1)},
+                  {e->in_len, h_in_len, 4 * n},   {e->isize, h_isize, 4 * n},   {e->crc_expect, h_crc, 4 * n},
+                  {e->order, h_order, 4 * n},     {e->st, h_st, sizeof(EngineDevState)},
+                  {pp.d_count, h_count, 8 * kPipeSlices}, {pp.d_first, h_first, 8 * kPipeSlices}};
+    for (const Copy &c : copies)
+        if ((ce = cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return cuda_fail(err, ce, "uploading the plan");
+    if ((ce = cudaMemsetAsync(pp.d_errs, 0xff, 8 * kPipeSlices, s)) != cudaSuccess ||
+        (ce = cudaMemsetAsync(pp.d_heads, 0, 4 * kPipeSlices, s)) != cudaSuccess ||
+        (ce = cudaEventRecord(pp.plan, s)) != cudaSuccess)
+        return cuda_fail(err, ce, "uploading the plan");
+    for (int k = 0; k < groups; ++k) {
+        cudaStream_t sg = (k & 1) ? pp.side : s;
+        if ((ce = cudaStreamWaitEvent(sg, pp.up[k], 0)) != cudaSuccess ||
+            (ce = cudaStreamWaitEvent(sg, pp.plan, 0)) != cudaSuccess)
+            return cuda_fail(err, ce, "ordering the inflate");
+        const u64 f = first[k];
+        if (first[k + 1] > f &&
+            (ce = frt_launch_inflate_persistent(e->in, e->in_off + f, e->in_len + f, e->out, e->out_off + f,
+                                                e->isize + f, e->crc_expect + f, e->status + f, e->produced + f,
+                                                e->crc + f, e->order + f, pp.d_count + k, first[k + 1] - f,
+                                                e->out_cap, pp.d_heads + k, (u32)e->grid,
+                                                (unsigned long long *)(pp.d_errs + k), e->tuning, sg)) != cudaSuccess)
+            return cuda_fail(err, ce, "launching the inflate");
+        if ((ce = cudaEventRecord(pp.done[k], sg)) != cudaSuccess) return cuda_fail(err, ce, "ordering the inflate");
+    }
+    for (int k = 0; k < groups; ++k)
+        if ((k & 1) && (ce = cudaStreamWaitEvent(s, pp.done[k], 0)) != cudaSuccess)
+            return cuda_fail(err, ce, "joining the inflate");
+    // the next run's uploads wait for everything that reads this run's staging
+    k_merge_group_errors<<<1, 32, 0, s>>>(pp.d_errs, pp.d_first, (u32)groups, e->st);
+    if ((ce = enqueue_records(e, true)) != cudaSuccess) return cuda_fail(err, ce, "launching the record stages");
+    if ((ce = cudaEventRecord(pp.plan, s)) != cudaSuccess) return cuda_fail(err, ce, "ordering the run");
+    return FRT_OK;
+}
+
+} // namespace
+
 extern "C" int frt_engine_run_host(frt_engine *e, const uint8_t *host, size_t len, frt_engine_stats *stats,
                                    frt_error *err)
 {
@@ -1208,8 +1403,19 @@ extern "C" int frt_engine_run_host(frt_engine *e, const uint8_t *host, size_t le
                   "bind a device buffer of this length first; run_host refills it from host memory");
         return FRT_ERR_INVALID_ARGUMENT;
     }
-    cudaError_t ce = cudaMemcpyAsync((void *)e->in, host, len, cudaMemcpyHostToDevice, e->stream);
-    if (ce != cudaSuccess) return cuda_fail(err, ce, "uploading the file");
+    if (!e->multi) {
+        int rc = run_host_pipelined(e, host, len, err);
+        if (rc == FRT_OK) return frt_engine_finish(e, stats, err);
+        if (rc != 1) return rc;
+        // the host plan differs from the bound file's: the bytes are (being)
+        // uploaded on the copy stream; run the single launch after them
+        cudaError_t ce = cudaEventRecord(e->pipe.up[kPipeSlices - 1], e->pipe.copy);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(e->stream, e->pipe.up[kPipeSlices - 1], 0);
+        if (ce != cudaSuccess) return cuda_fail(err, ce, "ordering after the upload");
+    } else {
+        cudaError_t ce = cudaMemcpyAsync((void *)e->in, host, len, cudaMemcpyHostToDevice, e->stream);
+        if (ce != cudaSuccess) return cuda_fail(err, ce, "uploading the file");
+    }
     int rc = frt_engine_run(e, err);
     if (rc) return rc;
     return frt_engine_finish(e, stats, err);
