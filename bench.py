@@ -58,10 +58,13 @@ WORKLOADS = {
 # (c) bgzipped FASTA, decoded by their scanners after one inflate of all members.
 MIXED = {
     "mixed_formats": dict(bcf_sites=2_000_000, bcf_samples=500, fastq_reads=10_000_000, fasta_bases=3_100_000_000,
+                          vcf_sites=20_000, vcf_samples=2504,
                           desc="one persistent inflate over (a) BCF 2M sites x 500 samples over 24 contigs, "
                                "(b) bgzipped FASTQ 10M x 150 bp, (c) bgzipped FASTA 3.1 Gb (60-column lines, "
-                               "soft-masked runs, N runs); each then decoded by its scanner"),
+                               "soft-masked runs, N runs); each then decoded by its scanner. Text framing is "
+                               "timed beside it on a bgzipped VCF of 20k sites x 2,504 phased genotypes"),
     "mixed_formats_small": dict(bcf_sites=200_000, bcf_samples=500, fastq_reads=1_000_000, fasta_bases=310_000_000,
+                                vcf_sites=2_000, vcf_samples=2504,
                                 desc="the mixed-format workload at one tenth size (profiling size)"),
 }
 
@@ -527,6 +530,49 @@ def generate_mixed(name: str):
     return files
 
 
+def text_framing(args, frt, w, peak):
+    """TextScanner over a bgzipped VCF inflated on the device: the scan's wall
+    time per batch (its read-backs make it host-synchronous), the HBM
+    fraction of its algorithmic bytes (the text read once, the five columns
+    written) and the oracle's numpy restatement on the same bytes."""
+    import numpy as np
+    import torch
+
+    from fritillaria_gb300 import synth
+
+    raw, bgz = synth.vcf_text(w["vcf_sites"], w["vcf_samples"], seed=64)
+    spans, _ = frt.discover_blocks(bgz)
+    batch = frt.CudaCodec(0).inflate_batch_device(bgz, spans)
+    scanner = frt.TextScanner(0)
+    for _ in range(3):
+        out = scanner.scan(batch, 0, frt.Dialect.VCF)
+    torch.cuda.synchronize()
+    reps = 20
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out = scanner.scan(batch, 0, frt.Dialect.VCF)
+    torch.cuda.synchronize()
+    ms = 1e3 * (time.perf_counter() - t0) / reps
+    col_bytes = sum(out.column_ptr(k)[1] for k in out._cols)
+    algo = raw.size + col_bytes
+    res = {"text_bytes": int(raw.size), "compressed_bytes": int(bgz.size), "records": len(out),
+           "header_lines": int(out.scan_info()[0]), "tabs": int(out.column_ptr("tabs")[1] // 8),
+           "column_bytes": int(col_bytes), "scan_ms": round(ms, 3),
+           "scan_gbs": round(raw.size / (ms / 1e3) / 1e9, 2),
+           "hbm_frac": round(algo / (ms / 1e3) / 1e9 / peak, 4),
+           "form": "wall time per TextScanner.scan on a resident inflated batch, 20 scans after 3 warm-ups"}
+    if not args.no_cpu:
+        from oracle import text
+
+        t0 = time.perf_counter()
+        want = text.device_scan(raw, 0, text.VCF)
+        secs = time.perf_counter() - t0
+        assert len(out) == want["record_offsets"].size and np.array_equal(out.column("tabs"), want["tabs"])
+        res["cpu_baseline"] = {"value": round(raw.size / secs / 1e9, 3), "unit": "GB/s", "cores": 1, "kind": "port",
+                               "sample": "the whole VCF text through oracle/text.py device_scan (numpy)"}
+    return res
+
+
 def run_mixed(args, rank, world, local):
     import numpy as np
     import torch
@@ -653,6 +699,7 @@ def run_mixed(args, rank, world, local):
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "text_framing": text_framing(args, frt, w, peak),
             "gpu_launches": eng.launches_per_run() * args.steps,
             "clocks": clocks.summary(),
             "wall_s": round(wall, 3),

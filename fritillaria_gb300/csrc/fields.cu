@@ -17,8 +17,10 @@
 //                     cigar_raw, sequence_packed, qualities, aux_raw
 //                     (record.rs:222-270), so the inflated batch can be dropped.
 //
-// Lengths are turned into offsets by a device exclusive scan; the copies are a
-// warp per record with consecutive lanes on consecutive bytes.
+// The payload copies take three launches: per-CTA byte counts, a scan of
+// those counts, and one copy in which each CTA scans its records' lengths,
+// writes their offsets into the result and stages every record's bytes in
+// shared memory with 16-byte loads before consecutive lanes write them out.
 
 #include <cstring>
 #include <vector>
@@ -32,41 +34,64 @@ namespace {
 
 constexpr u32 kScanBlock = 1024;
 
-// In-place exclusive scan of a[0, n) per 1024-element block; block totals to part.
-__global__ void __launch_bounds__(kScanBlock) k_scan_block(u64 *a, u64 n, u64 *part)
+// The payload copies.  compact fills five payloads -- the name without its
+// NUL, CIGAR, packed sequence, qualities, aux -- from each record's bytes after
+// its 36 fixed ones; unpack expands the packed sequence to one byte a base.
+enum CopyMode { COPY_COMPACT = 0, COPY_BASES = 1 };
+template <int MODE> __host__ __device__ constexpr int kinds() { return MODE == COPY_COMPACT ? 5 : 1; }
+constexpr u32 kRoundRecords = 256; // records per round: one a thread, 32 a warp
+constexpr u32 kRounds = 4;
+constexpr u32 kBlockRecords = kRoundRecords * kRounds;
+
+// A record's copy: its source bytes [src, src + cut[5]) and, relative to src,
+// compact's payload bounds -- name [0, cut[0]), CIGAR [cut[1], cut[2]),
+// sequence [cut[2], cut[3]), qualities [cut[3], cut[4]), aux [cut[4], cut[5])
+// -- or, for unpack, the packed sequence with cut[0] = l_seq bases.
+struct Span {
+    u64 src;
+    u32 cut[6];
+    u8 *dst[5];
+};
+
+struct CopyOut {
+    u64 *off[5];
+    u8 *data[5];
+};
+
+__device__ __forceinline__ u64 record_span(const RecordView &v, u64 i, int mode, u32 cut[6])
 {
-    __shared__ u64 warps[32];
-    const u64 i = (u64)blockIdx.x * kScanBlock + threadIdx.x;
-    const u32 lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
-    const u64 x = i < n ? a[i] : 0ull;
-    u64 s = x;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const u64 y = __shfl_up_sync(FRT_FULL_MASK, s, d);
-        if ((int)lane >= d) s += y;
+    const u8 *p = v.buf + v.record_offsets[i];
+    if (mode == COPY_BASES) {
+        const u32 l = v.seq_len[i];
+        cut[0] = l;
+        cut[1] = cut[2] = cut[3] = cut[4] = 0;
+        cut[5] = (l + 1u) >> 1;
+        return (u64)(p + v.sequence_start[i]);
     }
-    if (lane == 31u) warps[w] = s;
-    __syncthreads();
-    if (w == 0) {
-        u64 t = warps[lane];
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const u64 y = __shfl_up_sync(FRT_FULL_MASK, t, d);
-            if ((int)lane >= d) t += y;
-        }
-        warps[lane] = t;
-    }
-    __syncthreads();
-    const u64 before = w ? warps[w - 1] : 0ull;
-    if (i < n) a[i] = before + s - x;
-    if (threadIdx.x == kScanBlock - 1) part[blockIdx.x] = before + s;
+    const u32 nl = v.name_len[i];
+    cut[0] = nl && p[36u + nl - 1u] == 0 ? nl - 1u : nl; // Record::name strips the NUL
+    cut[1] = v.cigar_start[i] - 36u;
+    cut[2] = v.sequence_start[i] - 36u;
+    cut[3] = v.quality_start[i] - 36u;
+    cut[4] = v.aux_start[i] - 36u;
+    cut[5] = v.record_end[i] - 36u;
+    return (u64)(p + 36);
 }
 
-// Exclusive scan of the nb block totals by one block, 1024 at a time.
-__global__ void __launch_bounds__(kScanBlock) k_scan_parts(u64 *part, u64 nb)
+template <int MODE> __device__ __forceinline__ u32 payload_len(const u32 cut[6], int k)
+{
+    if (MODE == COPY_BASES || k == 0) return cut[0];
+    return cut[k + 1] - cut[k];
+}
+
+// Exclusive scan of each kind's block totals, one CTA a kind, 1024 at a time:
+// part[k * stride + b] for b < nb, the kind's total to part[k * stride + nb]
+// and to totals[k].
+__global__ void __launch_bounds__(kScanBlock) k_scan_parts(u64 *part, u64 nb, u64 stride, u64 *totals)
 {
     __shared__ u64 warps[32];
     __shared__ u64 carry;
+    part += blockIdx.x * stride;
     const u32 lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
@@ -98,59 +123,41 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_parts(u64 *part, u64 nb)
         if (threadIdx.x == kScanBlock - 1) carry = c + before + s;
         __syncthreads();
     }
-}
-
-__global__ void k_scan_add(u64 *a, u64 n, const u64 *part)
-{
-    const u64 i = (u64)blockIdx.x * kScanBlock + threadIdx.x;
-    if (i < n) a[i] += part[blockIdx.x];
-}
-
-// What each payload of a record spans, relative to the record start.
-enum Payload { P_NAME = 0, P_CIGAR = 1, P_SEQ = 2, P_QUAL = 3, P_AUX = 4, P_BASES = 5 };
-
-__device__ __forceinline__ void payload_range(const RecordView &v, u64 i, int which, u32 *from, u32 *len)
-{
-    const u8 *p = v.buf + v.record_offsets[i];
-    switch (which) {
-    case P_NAME: {
-        const u32 nl = v.name_len[i];
-        *from = 36u;
-        *len = nl && p[36u + nl - 1u] == 0 ? nl - 1u : nl; // Record::name strips the NUL
-        break;
-    }
-    case P_CIGAR: *from = v.cigar_start[i]; *len = v.sequence_start[i] - v.cigar_start[i]; break;
-    case P_SEQ: *from = v.sequence_start[i]; *len = v.quality_start[i] - v.sequence_start[i]; break;
-    case P_QUAL: *from = v.quality_start[i]; *len = v.aux_start[i] - v.quality_start[i]; break;
-    case P_AUX: *from = v.aux_start[i]; *len = v.record_end[i] - v.aux_start[i]; break;
-    default: *from = v.sequence_start[i]; *len = v.seq_len[i]; break; // bases: one byte each
+    if (threadIdx.x == 0) {
+        part[nb] = carry;
+        totals[blockIdx.x] = carry;
     }
 }
 
-// lens[i] = the payload's length for i < n, lens[n] = 0 (the scan makes it the total).
-__global__ void k_payload_lengths(RecordView v, int which, u64 *lens)
+// Each CTA's payload bytes per kind, over its kBlockRecords records.
+template <int MODE> __global__ void __launch_bounds__(kRoundRecords) k_fields_count(RecordView v, u64 *part, u64 stride)
 {
-    const u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i > v.n) return;
-    if (i == v.n) {
-        lens[i] = 0;
-        return;
+    constexpr int K = kinds<MODE>();
+    __shared__ u64 wsum[K][kRoundRecords / 32];
+    const u32 lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    u64 s[K] = {};
+    const u64 b0 = (u64)blockIdx.x * kBlockRecords;
+    for (u32 q = 0; q < kRounds; ++q) {
+        const u64 i = b0 + q * kRoundRecords + threadIdx.x;
+        if (i < v.n) {
+            u32 cut[6];
+            record_span(v, i, MODE, cut);
+#pragma unroll
+            for (int k = 0; k < K; ++k) s[k] += payload_len<MODE>(cut, k);
+        }
     }
-    u32 from, len;
-    payload_range(v, i, which, &from, &len);
-    lens[i] = len;
-}
-
-__global__ void k_copy_payload(RecordView v, int which, const u64 *offs, u8 *out)
-{
-    const u64 r = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (r >= v.n) return;
-    const u32 lane = threadIdx.x & 31u;
-    u32 from, len;
-    payload_range(v, r, which, &from, &len);
-    const u8 *src = v.buf + v.record_offsets[r] + from;
-    u8 *dst = out + offs[r];
-    for (u32 j = lane; j < len; j += 32) dst[j] = src[j];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+#pragma unroll
+        for (int d = 16; d; d >>= 1) s[k] += __shfl_down_sync(FRT_FULL_MASK, s[k], d);
+        if (lane == 0) wsum[k][w] = s[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < (u32)K) {
+        u64 t = 0;
+        for (u32 j = 0; j < kRoundRecords / 32; ++j) t += wsum[threadIdx.x][j];
+        part[threadIdx.x * stride + blockIdx.x] = t;
+    }
 }
 
 // "=ACMGRSVTWYHKDBN"[nib], from two words instead of a table every lane
@@ -163,17 +170,192 @@ __device__ __forceinline__ u8 base_of(u32 nib)
     return (u8)(w >> (8u * (nib & 7u)));
 }
 
-__global__ void k_unpack_bases(RecordView v, const u64 *offs, u8 *out)
+// Writes the record's bytes [lo, hi) to its payloads; in[r] is its byte r.
+template <int MODE> __device__ __forceinline__ void emit(const Span &sp, const u8 *in, u32 lo, u32 hi, u32 lane)
 {
-    const u64 r = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (r >= v.n) return;
-    const u32 lane = threadIdx.x & 31u, l = v.seq_len[r];
-    const u8 *packed = v.buf + v.record_offsets[r] + v.sequence_start[r];
-    u8 *dst = out + offs[r];
-    for (u32 j = lane; 2u * j < l; j += 32) {
-        const u32 b = packed[j];
-        dst[2u * j] = base_of(b >> 4);
-        if (2u * j + 1u < l) dst[2u * j + 1u] = base_of(b & 15u);
+    if (MODE == COPY_BASES) {
+        const u32 l = sp.cut[0];
+        u8 *d = sp.dst[0];
+        if (((uintptr_t)d & 1u) == 0) {
+            for (u32 r = lo + lane; r < hi; r += 32u) {
+                const u32 b = in[r];
+                if (2u * r + 1u < l)
+                    *(unsigned short *)(d + 2u * r) = (unsigned short)(base_of(b >> 4) | ((u32)base_of(b & 15u) << 8));
+                else
+                    d[2u * r] = base_of(b >> 4);
+            }
+        } else {
+            for (u32 r = lo + lane; r < hi; r += 32u) {
+                const u32 b = in[r];
+                d[2u * r] = base_of(b >> 4);
+                if (2u * r + 1u < l) d[2u * r + 1u] = base_of(b & 15u);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const u32 sk = k ? sp.cut[k] : 0u, ek = k ? sp.cut[k + 1] : sp.cut[0];
+            u8 *d = sp.dst[k];
+            for (u32 r = max(sk, lo) + lane; r < min(ek, hi); r += 32u) d[r - sk] = in[r];
+        }
+    }
+}
+
+// A warp's 32 records.  Each turn gathers, into the warp's shared-memory
+// stage, the aligned 16-byte blocks that hold the bytes of as many of the
+// next records as fit in kStageBlocks -- every lane loads up to four blocks,
+// all in flight together, each found by a binary search over the warp's
+// prefix of per-record block counts -- then writes those records' payloads
+// with consecutive lanes on consecutive bytes.  A record larger than a turn
+// goes through in turns of its own.  The inflated buffers start 256-byte
+// aligned and carry at least 16 bytes of padding past their last byte, so
+// every aligned block that holds a record byte lies inside the allocation.
+constexpr u32 kStageBlocks = 128;
+constexpr u32 kStageLoads = kStageBlocks / 32;
+constexpr u32 kBigSpan = 4096; // records with more bytes go to k_fields_copy_big
+
+template <int MODE> __device__ __forceinline__ void copy_spans(const Span *spans, u8 *stage, u32 lane)
+{
+    const Span &mine = spans[lane];
+    const u32 mo = (u32)(mine.src & 15u);
+    const u64 mbase = mine.src - mo;
+    const u32 mlen = mine.cut[5];
+    // blocks of this lane's record, capped past a turn (such a record goes alone)
+    const u32 nbk = mlen ? min((mo + mlen + 15u) >> 4, kStageBlocks + 1u) : 0u;
+    u32 pre = nbk;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const u32 y = __shfl_up_sync(FRT_FULL_MASK, pre, d);
+        if ((int)lane >= d) pre += y;
+    }
+    const u32 excl = pre - nbk;
+    u32 j0 = 0;
+    while (j0 < 32u) {
+        const u32 base = __shfl_sync(FRT_FULL_MASK, excl, j0);
+        const u32 fit = __ballot_sync(FRT_FULL_MASK, lane >= j0 && pre - base <= kStageBlocks);
+        if (!((fit >> j0) & 1u)) { // record j0 alone is larger than a turn
+            const Span &sp = spans[j0];
+            const u32 len = sp.cut[5], o = (u32)(sp.src & 15u);
+            const u8 *a0 = (const u8 *)(sp.src - o);
+            for (u32 cb = 0; cb < len + o; cb += 16u * kStageBlocks) {
+                uint4 v[kStageLoads];
+#pragma unroll
+                for (u32 h = 0; h < kStageLoads; ++h) {
+                    const u32 blk = cb + 16u * (lane + 32u * h);
+                    if (blk < len + o) v[h] = __ldg((const uint4 *)(a0 + blk));
+                }
+#pragma unroll
+                for (u32 h = 0; h < kStageLoads; ++h)
+                    if (cb + 16u * (lane + 32u * h) < len + o) *(uint4 *)(stage + 16u * (lane + 32u * h)) = v[h];
+                __syncwarp();
+                emit<MODE>(sp, stage + o - cb, cb > o ? cb - o : 0u, min(len, cb + 16u * kStageBlocks - o), lane);
+                __syncwarp();
+            }
+            ++j0;
+            continue;
+        }
+        const u32 j1 = 32u - __clz(fit); // one past the last record of this turn
+        const u32 nb = __shfl_sync(FRT_FULL_MASK, pre, j1 - 1u) - base;
+        uint4 v[kStageLoads];
+#pragma unroll
+        for (u32 h = 0; h < kStageLoads; ++h) {
+            const u32 t = lane + 32u * h;
+            // the first record j in [j0, j1) whose blocks end past t
+            u32 lo = j0, hi = j1 - 1u;
+#pragma unroll
+            for (int step = 0; step < 5; ++step) {
+                const u32 mid = (lo + hi) >> 1;
+                if (__shfl_sync(FRT_FULL_MASK, pre, mid) - base > t)
+                    hi = mid;
+                else
+                    lo = mid + 1u;
+            }
+            const u32 j = min(lo, 31u);
+            const u32 first = __shfl_sync(FRT_FULL_MASK, excl, j) - base;
+            const u64 at = __shfl_sync(FRT_FULL_MASK, mbase, j) + 16ull * (t - first);
+            if (t < nb) v[h] = __ldg((const uint4 *)at);
+        }
+#pragma unroll
+        for (u32 h = 0; h < kStageLoads; ++h)
+            if (lane + 32u * h < nb) *(uint4 *)(stage + 16u * (lane + 32u * h)) = v[h];
+        __syncwarp();
+        for (u32 j = j0; j < j1; ++j) {
+            const Span &sp = spans[j];
+            const u32 first = __shfl_sync(FRT_FULL_MASK, excl, j) - base;
+            if (sp.cut[5]) emit<MODE>(sp, stage + 16u * first + (u32)(sp.src & 15u), 0u, sp.cut[5], lane);
+        }
+        __syncwarp();
+        j0 = j1;
+    }
+}
+
+// Per round a thread reads one record's bounds; a CTA scan of the payload
+// lengths, plus the CTA's prefix from k_scan_parts, gives the output offsets,
+// written straight into the result; then each warp copies its 32 records.
+template <int MODE> __global__ void __launch_bounds__(kRoundRecords, 4) k_fields_copy(RecordView v, const u64 *part,
+                                                                                    u64 stride, CopyOut out, u32 *big,
+                                                                                    u32 *big_count, u32 big_cap)
+{
+    constexpr int K = kinds<MODE>();
+    __shared__ Span spans[kRoundRecords];
+    __shared__ __align__(16) u8 stage[kRoundRecords / 32][16 * kStageBlocks];
+    __shared__ u64 wsum[K][kRoundRecords / 32];
+    __shared__ u64 carry[K]; // each kind's bytes before this round
+    const u32 lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const u64 b0 = (u64)blockIdx.x * kBlockRecords;
+    if (threadIdx.x < (u32)K) carry[threadIdx.x] = part[threadIdx.x * stride + blockIdx.x];
+    for (u32 q = 0; q < kRounds; ++q) {
+        const u64 first = b0 + q * kRoundRecords;
+        if (first >= v.n) break;
+        const u64 i = first + threadIdx.x;
+        const bool valid = i < v.n;
+        u32 cut[6] = {0, 0, 0, 0, 0, 0};
+        const u64 src = valid ? record_span(v, i, MODE, cut) : 0ull;
+        u64 len[K], incl[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            len[k] = payload_len<MODE>(cut, k);
+            u64 x = len[k];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const u64 y = __shfl_up_sync(FRT_FULL_MASK, x, d);
+                if ((int)lane >= d) x += y;
+            }
+            incl[k] = x;
+            if (lane == 31u) wsum[k][w] = x;
+        }
+        __syncthreads();
+        Span &sp = spans[threadIdx.x];
+        u64 next_carry = 0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            u64 before = 0, total = 0;
+#pragma unroll
+            for (u32 j = 0; j < kRoundRecords / 32; ++j) {
+                const u64 t = wsum[k][j];
+                before += j < w ? t : 0ull;
+                total += t;
+            }
+            const u64 off = carry[k] + before + incl[k] - len[k];
+            if (valid) {
+                out.off[k][i] = off;
+                if (i == v.n - 1) out.off[k][v.n] = off + len[k];
+            }
+            sp.dst[k] = out.data[k] + off;
+            if (threadIdx.x == (u32)k) next_carry = carry[k] + total;
+        }
+        sp.src = src;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sp.cut[c] = cut[c];
+        if (cut[5] > kBigSpan) { // k_fields_copy_big's, an empty span here
+            const u32 slot = atomicAdd(big_count, 1u);
+            if (slot < big_cap) big[slot] = (u32)i;
+            sp.cut[5] = 0;
+        }
+        __syncthreads();
+        if (threadIdx.x < (u32)K) carry[threadIdx.x] = next_carry; // read again after the round's last barrier
+        copy_spans<MODE>(spans + 32u * w, stage[w], lane);
+        __syncthreads();
     }
 }
 
@@ -252,6 +434,55 @@ __global__ void k_cigar_resolve(RecordView v, u64 *offset, u32 *ops, u8 *status)
     status[i] = st;
 }
 
+// Records whose bytes pass kBigSpan, listed by k_fields_copy: CTAs take one
+// at a time and their warps split its turns, so the work is shared by bytes
+// rather than by records (a few reads of hundreds of kilobytes would
+// otherwise hold one warp each while the rest of the GPU idles).
+template <int MODE> __global__ void __launch_bounds__(kRoundRecords, 4)
+    k_fields_copy_big(RecordView v, const u32 *big, const u32 *big_count, u32 big_cap, u32 *big_next, CopyOut out)
+{
+    constexpr int K = kinds<MODE>();
+    constexpr u32 kTurn = 16u * kStageBlocks;
+    constexpr u32 kWarps = kRoundRecords / 32;
+    __shared__ __align__(16) u8 stage[kWarps][kTurn];
+    __shared__ Span sp_s;
+    __shared__ u32 b_s;
+    const u32 lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    const u32 nbig = min(*big_count, big_cap);
+    for (;;) {
+        if (threadIdx.x == 0) b_s = atomicAdd(big_next, 1u);
+        __syncthreads();
+        const u32 b = b_s;
+        if (b >= nbig) break;
+        if (threadIdx.x == 0) {
+            const u64 i = big[b];
+            sp_s.src = record_span(v, i, MODE, sp_s.cut);
+#pragma unroll
+            for (int k = 0; k < K; ++k) sp_s.dst[k] = out.data[k] + out.off[k][i];
+        }
+        __syncthreads();
+        const Span &sp = sp_s;
+        const u32 len = sp.cut[5], o = (u32)(sp.src & 15u);
+        const u8 *a0 = (const u8 *)(sp.src - o);
+        u8 *st = stage[w];
+        for (u32 cb = kTurn * w; cb < len + o; cb += kTurn * kWarps) {
+            uint4 x[kStageLoads];
+#pragma unroll
+            for (u32 h = 0; h < kStageLoads; ++h) {
+                const u32 blk = cb + 16u * (lane + 32u * h);
+                if (blk < len + o) x[h] = __ldg((const uint4 *)(a0 + blk));
+            }
+#pragma unroll
+            for (u32 h = 0; h < kStageLoads; ++h)
+                if (cb + 16u * (lane + 32u * h) < len + o) *(uint4 *)(st + 16u * (lane + 32u * h)) = x[h];
+            __syncwarp();
+            emit<MODE>(sp, st + o - cb, cb > o ? cb - o : 0u, min(len, cb + kTurn - o), lane);
+            __syncwarp();
+        }
+        __syncthreads(); // sp_s and b_s are rewritten next
+    }
+}
+
 // Work buffers of one call, freed on every return path.
 struct Temp {
     cudaStream_t st;
@@ -272,20 +503,6 @@ struct Temp {
         return rc;
     }
 };
-
-// Exclusive scan of lens[0, n] in place (lens[n] becomes the total).
-int scan_u64(u64 *lens, u64 n1, cudaStream_t st, Temp &tmp, frt_error *err)
-{
-    const u64 nb = (n1 + kScanBlock - 1) / kScanBlock;
-    u64 *part = nullptr;
-    int rc = tmp.get(&part, nb, err);
-    if (rc) return rc;
-    k_scan_block<<<(unsigned)nb, kScanBlock, 0, st>>>(lens, n1, part);
-    k_scan_parts<<<1, kScanBlock, 0, st>>>(part, nb);
-    k_scan_add<<<(unsigned)nb, kScanBlock, 0, st>>>(lens, n1, part);
-    cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? FRT_OK : cuda_fail(err, e, "scanning payload lengths");
-}
 
 const size_t kAuxWidths[FRT_AUXV_COL_COUNT] = {1, 1, 1, 4, 8, 8};
 const size_t kCigarWidths[FRT_CIGAR_COL_COUNT] = {8, 4, 1};
@@ -322,7 +539,7 @@ int frt::fields_run(const RecordView &v, int op, const char *tag, int device, cu
     const size_t *widths = nullptr;
     int n_cols = 0, format = 0;
     size_t col_bytes[16] = {};
-    std::vector<int> payloads; // which payload each (offsets, data) pair holds
+    int kinds = 0, mode = 0; // payloads copied: (offsets, data) column pairs
     switch (op) {
     case FIELDS_AUX_LOOKUP:
         widths = kAuxWidths, n_cols = FRT_AUXV_COL_COUNT, format = FMT_AUX_VALUES;
@@ -334,36 +551,37 @@ int frt::fields_run(const RecordView &v, int op, const char *tag, int device, cu
         break;
     case FIELDS_UNPACK_SEQUENCES:
         widths = kBasesWidths, n_cols = FRT_BASES_COL_COUNT, format = FMT_BASES;
-        payloads = {P_BASES};
+        kinds = 1, mode = COPY_BASES;
         break;
     case FIELDS_COMPACT:
         widths = kCompactWidths, n_cols = FRT_COMPACT_COL_COUNT, format = FMT_COMPACT;
-        payloads = {P_NAME, P_CIGAR, P_SEQ, P_QUAL, P_AUX};
+        kinds = 5, mode = COPY_COMPACT;
         break;
     default:
         set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "unknown record-field operation %d", op);
         return FRT_ERR_INVALID_ARGUMENT;
     }
 
-    // Payload offsets: lengths, scan, totals back to the host to size the result.
-    std::vector<u64 *> offs(payloads.size(), nullptr);
-    std::vector<u64> totals(payloads.size(), 0);
-    if (!payloads.empty()) {
-        const unsigned grid = (unsigned)((n + 1 + 255) / 256);
+    // Payload totals: per-CTA byte counts, their scan, the totals back to the
+    // host to size the result.  The scanned counts stay for the copy.
+    const u64 nb = (n + kBlockRecords - 1) / kBlockRecords, stride = nb + 1;
+    u64 *part = nullptr;
+    u64 totals[5] = {};
+    if (kinds) {
         u64 *d_tot = nullptr;
-        if ((rc = tmp.get(&d_tot, payloads.size(), err))) return rc;
-        for (size_t k = 0; k < payloads.size(); ++k) {
-            if ((rc = tmp.get(&offs[k], n + 1, err))) return rc;
-            k_payload_lengths<<<grid, 256, 0, st>>>(v, payloads[k], offs[k]);
-            if ((rc = scan_u64(offs[k], n + 1, st, tmp, err))) return rc;
-            if ((e = cudaMemcpyAsync(d_tot + k, offs[k] + n, 8, cudaMemcpyDeviceToDevice, st)) != cudaSuccess)
-                return cuda_fail(err, e, "collecting payload totals");
+        if ((rc = tmp.get(&part, kinds * stride, err)) || (rc = tmp.get(&d_tot, kinds, err))) return rc;
+        if (n) {
+            if (mode == COPY_BASES)
+                k_fields_count<COPY_BASES><<<(unsigned)nb, kRoundRecords, 0, st>>>(v, part, stride);
+            else
+                k_fields_count<COPY_COMPACT><<<(unsigned)nb, kRoundRecords, 0, st>>>(v, part, stride);
+            k_scan_parts<<<kinds, kScanBlock, 0, st>>>(part, nb, stride, d_tot);
+            if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(err, e, "counting payload bytes");
+            if ((e = cudaMemcpyAsync(totals, d_tot, 8 * kinds, cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+                (e = cudaStreamSynchronize(st)) != cudaSuccess)
+                return cuda_fail(err, e, "reading payload totals");
         }
-        if ((e = cudaMemcpyAsync(totals.data(), d_tot, 8 * payloads.size(), cudaMemcpyDeviceToHost, st)) !=
-                cudaSuccess ||
-            (e = cudaStreamSynchronize(st)) != cudaSuccess)
-            return cuda_fail(err, e, "reading payload totals");
-        for (size_t k = 0; k < payloads.size(); ++k) {
+        for (int k = 0; k < kinds; ++k) {
             col_bytes[2 * k] = 8 * (n + 1);
             col_bytes[2 * k + 1] = totals[k];
         }
@@ -391,7 +609,7 @@ int frt::fields_run(const RecordView &v, int op, const char *tag, int device, cu
     };
     if (total_bytes && (rc = dev_alloc((void **)&c->cols, total_bytes, st, err))) return fail(rc);
     auto col = [&](int k) { return c->cols + c->col_off[k]; };
-    const unsigned tgrid = (unsigned)((n + 255) / 256), wgrid = (unsigned)((n * 32 + 255) / 256);
+    const unsigned tgrid = (unsigned)((n + 255) / 256);
     if (n) {
         switch (op) {
         case FIELDS_AUX_LOOKUP: {
@@ -403,20 +621,39 @@ int frt::fields_run(const RecordView &v, int op, const char *tag, int device, cu
         case FIELDS_CIGAR_RESOLVED:
             k_cigar_resolve<<<tgrid, 256, 0, st>>>(v, (u64 *)col(0), (u32 *)col(1), col(2));
             break;
-        default:
-            for (size_t k = 0; k < payloads.size(); ++k) {
-                if ((e = cudaMemcpyAsync(col((int)(2 * k)), offs[k], 8 * (n + 1), cudaMemcpyDeviceToDevice, st)) !=
-                    cudaSuccess)
-                    return fail(cuda_fail(err, e, "placing payload offsets"));
-                if (payloads[k] == P_BASES)
-                    k_unpack_bases<<<wgrid, 256, 0, st>>>(v, offs[k], col((int)(2 * k + 1)));
-                else
-                    k_copy_payload<<<wgrid, 256, 0, st>>>(v, payloads[k], offs[k], col((int)(2 * k + 1)));
+        default: {
+            CopyOut o{};
+            for (int k = 0; k < kinds; ++k) {
+                o.off[k] = (u64 *)col(2 * k);
+                o.data[k] = col(2 * k + 1);
+            }
+            // a record past kBigSpan bytes holds more than kBigSpan - 1 payload
+            // bytes (compact drops at most the name's NUL), which bounds the list
+            u64 payload = 0;
+            for (int k = 0; k < kinds; ++k) payload += totals[k];
+            const u64 cap64 = payload / (kBigSpan - 1) + 1;
+            const u32 cap = (u32)(cap64 < n ? cap64 : n);
+            u32 *big = nullptr, *counters = nullptr;
+            int sms = 0;
+            if ((rc = tmp.get(&big, cap, err)) || (rc = tmp.get(&counters, 2, err))) return fail(rc);
+            if ((e = cudaMemsetAsync(counters, 0, 8, st)) != cudaSuccess ||
+                (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
+                return fail(cuda_fail(err, e, "preparing the payload copy"));
+            if (mode == COPY_BASES) {
+                k_fields_copy<COPY_BASES><<<(unsigned)nb, kRoundRecords, 0, st>>>(v, part, stride, o, big, counters, cap);
+                k_fields_copy_big<COPY_BASES><<<(unsigned)sms * 4u, kRoundRecords, 0, st>>>(v, big, counters, cap,
+                                                                                            counters + 1, o);
+            } else {
+                k_fields_copy<COPY_COMPACT><<<(unsigned)nb, kRoundRecords, 0, st>>>(v, part, stride, o, big, counters,
+                                                                                   cap);
+                k_fields_copy_big<COPY_COMPACT><<<(unsigned)sms * 4u, kRoundRecords, 0, st>>>(v, big, counters, cap,
+                                                                                              counters + 1, o);
             }
         }
+        }
     } else {
-        for (size_t k = 0; k < payloads.size(); ++k) // one offset, 0
-            if ((e = cudaMemsetAsync(col((int)(2 * k)), 0, 8, st)) != cudaSuccess)
+        for (int k = 0; k < kinds; ++k) // one offset, 0
+            if ((e = cudaMemsetAsync(col(2 * k), 0, 8, st)) != cudaSuccess)
                 return fail(cuda_fail(err, e, "placing payload offsets"));
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return fail(cuda_fail(err, e, "launching record-field kernels"));

@@ -188,6 +188,62 @@ def fasta(n_contigs: int = 24, total_bases: int = 3_100_000_000, line_width: int
     return raw, bgzf(raw, "full", levels)
 
 
+def raw_vcf_text(n_sites: int, n_samples: int = 2504, n_contigs: int = 24, seed: int = 1) -> np.ndarray:
+    """VCF 4.2 text of phased biallelic genotypes, shaped like a population
+    panel: `##` meta lines, a `#CHROM` line naming every sample, then one line
+    per site -- CHROM, sorted POS, ID, REF, ALT, QUAL, FILTER, INFO (AC, AN,
+    AF, DP), FORMAT GT and a `a|b` genotype per sample, alleles drawn with the
+    site's allele frequency (log-uniform 1e-4..0.5)."""
+    rng = np.random.default_rng(seed)
+    contigs = [f"chr{k + 1}" for k in range(n_contigs)]
+    head = ["##fileformat=VCFv4.2", "##source=fritillaria_gb300.synth"]
+    head += [f"##contig=<ID={c},length={250_000_000 - 7_000_000 * k}>" for k, c in enumerate(contigs)]
+    head += ['##INFO=<ID=AC,Number=A,Type=Integer,Description="Alternate allele count">',
+             '##INFO=<ID=AN,Number=1,Type=Integer,Description="Total allele number">',
+             '##INFO=<ID=AF,Number=A,Type=Float,Description="Alternate allele frequency">',
+             '##INFO=<ID=DP,Number=1,Type=Integer,Description="Combined depth">',
+             '##FORMAT=<ID=GT,Number=1,Type=String,Description="Phased genotype">',
+             "\t".join(["#CHROM", "POS", "ID", "REF", "ALT", "QUAL", "FILTER", "INFO", "FORMAT"]
+                       + [f"S{i:05d}" for i in range(n_samples)])]
+    parts = [np.frombuffer(("\n".join(head) + "\n").encode(), np.uint8)]
+    per = np.bincount(np.sort(rng.integers(0, n_contigs, n_sites)), minlength=n_contigs)
+    af = np.exp(rng.uniform(np.log(1e-4), np.log(0.5), n_sites))
+    bases = "ACGT"
+    chunk = 1024
+    site = 0
+    for k, c in enumerate(contigs):
+        pos = np.sort(rng.choice(200_000_000, int(per[k]), replace=False)) + 1 if per[k] else []
+        for lo in range(0, int(per[k]), chunk):
+            m = min(chunk, int(per[k]) - lo)
+            alt = (rng.random((m, 2 * n_samples)) < af[site:site + m, None]).astype(np.uint8)
+            gt = np.empty((m, n_samples, 4), np.uint8)
+            gt[:, :, 0] = alt[:, 0::2] + ord("0")
+            gt[:, :, 1] = ord("|")
+            gt[:, :, 2] = alt[:, 1::2] + ord("0")
+            gt[:, :, 3] = ord("\t")
+            gt[:, -1, 3] = ord("\n")
+            gt = gt.reshape(m, 4 * n_samples)
+            ac = alt.sum(axis=1)
+            refs = rng.integers(0, 4, m)
+            alts = (refs + rng.integers(1, 4, m)) % 4
+            qual = rng.integers(20, 10_000, m)
+            dp = rng.integers(5_000, 40_000, m)
+            for i in range(m):
+                p = int(pos[lo + i])
+                line = (f"{c}\t{p}\trs{1_000_000 + site + i}\t{bases[refs[i]]}\t{bases[alts[i]]}\t{qual[i]}\tPASS\t"
+                        f"AC={ac[i]};AN={2 * n_samples};AF={ac[i] / (2 * n_samples):.4g};DP={dp[i]}\tGT\t")
+                parts.append(np.frombuffer(line.encode(), np.uint8))
+                parts.append(gt[i])
+            site += m
+    return np.concatenate(parts)
+
+
+def vcf_text(n_sites: int, n_samples: int = 2504, n_contigs: int = 24, seed: int = 1, levels=(6, 6)):
+    """(VCF text, bgzipped VCF text), members packed full as bgzip does."""
+    raw = raw_vcf_text(n_sites, n_samples, n_contigs, seed)
+    return raw, bgzf(raw, "full", levels)
+
+
 # The benchmark configurations.
 CONFIGS = {
     "short_reads_100k": dict(n_records=100_000, n_contigs=1, genome_len=50_000_000, levels=(6, 6)),

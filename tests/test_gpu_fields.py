@@ -108,11 +108,16 @@ def test_htslib_fixture_matches_samtools(gpu):
         assert "".join(f"{op >> 4}{'MIDNSHP=X'[op & 15]}" for op in ops) == texts[i]
 
 
-@pytest.mark.parametrize("kind", ["short", "ultra_long"])
+@pytest.mark.parametrize("kind", ["short", "ultra_long", "ultra_long_many"])
 def test_synthetic_reads(gpu, kind):
     if kind == "short":
         _, bgzf = synth.short_read_bam(6000, seed=8, levels=(1, 6))
         tags = [b"NM", b"MD", b"RG", b"XX"]
+    elif kind == "ultra_long_many":
+        # more records than one copy CTA takes, reads above and below the
+        # length the long-record kernel takes over at, in one batch
+        _, bgzf = synth.ultra_long_bam(1200, n_long_extra=2, seed=9, levels=(1, 1))
+        tags = [b"MM", b"qs"]
     else:
         _, bgzf = synth.ultra_long_bam(30, n_long_extra=1, seed=8)
         tags = [b"MM", b"ML", b"qs", b"ch", b"NM"]

@@ -82,6 +82,17 @@ def test_random_text(gpu, scanner, seed):
             check(gpu, scanner, batch, buf, start, (ord("@"), ord("x")))
 
 
+def test_synthetic_vcf(gpu, scanner):
+    """The benchmark's VCF shape (meta lines, a #CHROM line naming every
+    sample, a phased genotype per sample) at test size."""
+    buf = synth.raw_vcf_text(300, 257, seed=5)
+    codec = gpu.CudaCodec(0)
+    batch = device_batch(gpu, codec, buf)
+    got = check(gpu, scanner, batch, buf, 0, text.VCF)
+    assert len(got) == 300 and got.scan_info()[0] == 32
+    assert np.all(np.diff(got.column("field_starts").astype(np.int64)) == 8 + 257)
+
+
 def test_edges(gpu, scanner):
     codec = gpu.CudaCodec(0)
     for raw in (b"\n", b"\n\n\n", b"@only\theaders\n@more\n", b"x", b"x\ty", b"a\tb\n\nc\t\td\n", b"@h\n@unterminated",

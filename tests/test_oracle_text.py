@@ -89,3 +89,21 @@ def test_cpu_decode_agrees_on_terminated_batches():
     dev, cpu = text.device_scan(buf, 0, text.VCF), text.cpu_decode(buf, 0, text.VCF)
     # the launcher keeps the unterminated last line as a record; the CPU decode carries it
     assert dev["record_offsets"].size == cpu["record_offsets"].size + 1 and dev["tail"] == cpu["tail"]
+
+
+def test_synthetic_vcf_matches_the_reference_kernels():
+    """The benchmark's VCF generator: seeded, a #CHROM line naming every
+    sample, and framed alike by the oracle, the reference's kernels and the
+    reference's CPU decode."""
+    from fritillaria_gb300 import synth
+
+    buf = synth.raw_vcf_text(200, 100, seed=5)
+    assert np.array_equal(buf, synth.raw_vcf_text(200, 100, seed=5))
+    dev = text.device_scan(buf, 0, text.VCF)
+    assert dev["record_offsets"].size == 200 and dev["tabs"].size == 200 * (8 + 100)
+    chrom = bytes(buf[int(dev["header_offsets"][-1]):int(dev["record_offsets"][0]) - 1]).split(b"\t")
+    assert chrom[:9] == [b"#CHROM", b"POS", b"ID", b"REF", b"ALT", b"QUAL", b"FILTER", b"INFO", b"FORMAT"]
+    assert len(chrom) == 109
+    same(dev, text.cpu_decode(buf, 0, text.VCF))
+    ref()
+    same(dev, ref_kernels.text_scan(buf, 0, ord("#"), None))
