@@ -456,7 +456,8 @@ struct frt_engine {
     frt_error decode_err{};
     // host-buffer runs with the upload overlapped (run_host_pipelined)
     struct HostPipe {
-        cudaStream_t copy = nullptr, side = nullptr;
+        cudaStream_t copy = nullptr;
+        std::vector<cudaStream_t> lanes; // one per inflate group
         cudaEvent_t plan = nullptr;
         std::vector<cudaEvent_t> up, done;
         uint8_t *staging = nullptr; // pinned plan
@@ -738,20 +739,20 @@ extern "C" void frt_engine_destroy(frt_engine *e)
 {
     if (!e) return;
     DeviceGuardLite g(e->device);
-    free_all(e);
     {
         auto &pp = e->pipe;
         if (pp.copy) cudaStreamSynchronize(pp.copy);
-        if (pp.side) cudaStreamSynchronize(pp.side);
+        for (cudaStream_t q : pp.lanes) cudaStreamSynchronize(q);
         for (cudaEvent_t ev : pp.up) cudaEventDestroy(ev);
         for (cudaEvent_t ev : pp.done) cudaEventDestroy(ev);
         if (pp.plan) cudaEventDestroy(pp.plan);
         if (pp.copy) cudaStreamDestroy(pp.copy);
-        if (pp.side) cudaStreamDestroy(pp.side);
+        for (cudaStream_t q : pp.lanes) cudaStreamDestroy(q);
         if (pp.staging) cudaFreeHost(pp.staging);
         for (void *q : {(void *)pp.d_count, (void *)pp.d_errs, (void *)pp.d_first, (void *)pp.d_heads})
             if (q) cudaFree(q);
     }
+    free_all(e);
     frt_bam_decoder_destroy(e->bam_dec);
     frt_fastq_scanner_destroy(e->fastq);
     frt_bcf_scanner_destroy(e->bcf);
@@ -1250,8 +1251,9 @@ constexpr int kPipeSlices = 8; // upload slices, and at most this many inflate g
 // headers (the plan the device front would compute: member spans, trailers,
 // output offsets); each group of members whose bytes have all arrived is
 // inflated by its own launch of the persistent kernel (longest member first
-// within the group), alternating two streams so a launch fills the tail of the
-// one before; the record stages then run on the engine stream.  Returns 1 when
+// within the group) on a stream of its own, so each launch's CTAs take the SMs
+// as the ones before retire -- a group of a small file may hold fewer members
+// than the GPU has warps; the record stages then run on the engine stream.  Returns 1 when
 // the host plan does not match the bound file (the caller then runs the
 // single-launch path on the uploaded bytes), else an frt_status.
 int run_host_pipelined(frt_engine *e, const uint8_t *host, size_t len, frt_error *err)
@@ -1260,9 +1262,12 @@ int run_host_pipelined(frt_engine *e, const uint8_t *host, size_t len, frt_error
     cudaError_t ce;
     if (!pp.copy) {
         if ((ce = cudaStreamCreateWithFlags(&pp.copy, cudaStreamNonBlocking)) != cudaSuccess ||
-            (ce = cudaStreamCreateWithFlags(&pp.side, cudaStreamNonBlocking)) != cudaSuccess ||
             (ce = cudaEventCreateWithFlags(&pp.plan, cudaEventDisableTiming)) != cudaSuccess)
             return cuda_fail(err, ce, "creating the upload streams");
+        pp.lanes.assign(kPipeSlices, nullptr);
+        for (int k = 0; k < kPipeSlices; ++k)
+            if ((ce = cudaStreamCreateWithFlags(&pp.lanes[k], cudaStreamNonBlocking)) != cudaSuccess)
+                return cuda_fail(err, ce, "creating the inflate streams");
         pp.up.resize(kPipeSlices);
         pp.done.resize(kPipeSlices);
         for (int k = 0; k < kPipeSlices; ++k)
@@ -1275,28 +1280,31 @@ int run_host_pipelined(frt_engine *e, const uint8_t *host, size_t len, frt_error
             (ce = cudaMalloc(&pp.d_heads, 4 * kPipeSlices)) != cudaSuccess)
             return cuda_fail(err, ce, "allocating the group state");
     }
-    // the previous run's work on the side stream is done before its buffers are reused
+    // the previous run's inflate streams are done before its buffers are reused
     if ((ce = cudaStreamWaitEvent(pp.copy, pp.plan, 0)) != cudaSuccess) return cuda_fail(err, ce, "ordering uploads");
+    // The copy stream carries slice 0, slice 1, plan 0, slice 2, plan 1, ...:
+    // a group's plan follows its own slice with one slice of lookahead, so it
+    // never waits behind the whole file on the copy engine.
+    constexpr int kLookahead = 2;
     u64 slice_end[kPipeSlices];
-    for (int k = 0; k < kPipeSlices; ++k) {
-        const u64 a = (u64)len * k / kPipeSlices, b = (u64)len * (k + 1) / kPipeSlices;
-        slice_end[k] = b;
-        if (b > a && (ce = cudaMemcpyAsync((void *)(e->in + a), host + a, b - a, cudaMemcpyHostToDevice, pp.copy)) !=
-                         cudaSuccess)
-            return cuda_fail(err, ce, "uploading the file");
-        if ((ce = cudaEventRecord(pp.up[k], pp.copy)) != cudaSuccess) return cuda_fail(err, ce, "uploading the file");
-    }
-    // the plan, on the host, while the slices travel
-    std::vector<frt_span> spans;
-    size_t consumed = 0;
-    frt_error scratch{};
-    if (discover(host, len, 0, spans, &consumed, &scratch) != FRT_OK || consumed != len || spans.size() != e->n_cap)
-        return 1;
-    const u64 n = spans.size();
-    u64 total = 0;
-    for (const auto &sp : spans) total += sp.isize;
-    if (total > e->out_cap) return 1;
-    const size_t need = n * (8 + 4 + 4 + 4 + 8 + 4) + 8 * (n + 1) + sizeof(EngineDevState) + 8 * 4 * kPipeSlices + 64;
+    for (int k = 0; k < kPipeSlices; ++k) slice_end[k] = (u64)len * (k + 1) / kPipeSlices;
+    int issued = 0; // slices on the copy stream
+    auto upload_through = [&](int last) -> cudaError_t {
+        for (; issued <= last && issued < kPipeSlices; ++issued) {
+            const u64 a = issued ? slice_end[issued - 1] : 0, b = slice_end[issued];
+            if (b > a) {
+                cudaError_t c = cudaMemcpyAsync((void *)(e->in + a), host + a, b - a, cudaMemcpyHostToDevice, pp.copy);
+                if (c != cudaSuccess) return c;
+            }
+        }
+        return cudaSuccess;
+    };
+    if ((ce = upload_through(kLookahead - 1)) != cudaSuccess) return cuda_fail(err, ce, "uploading the file");
+    // The plan, on the host, one slice at a time while the slices travel: a
+    // group is the members whose blocks end in its slice, and it launches as
+    // soon as its slice is walked and uploaded.
+    const u64 cap = e->n_cap;
+    const size_t need = cap * (8 + 4 + 4 + 4 + 8 + 4) + 8 * (cap + 1) + sizeof(EngineDevState) + 8 * 4 * kPipeSlices + 64;
     if (need > pp.staging_bytes) {
         if (pp.staging) cudaFreeHost(pp.staging);
         pp.staging = nullptr;
@@ -1310,81 +1318,98 @@ int run_host_pipelined(frt_engine *e, const uint8_t *host, size_t len, frt_error
         at += (bytes + 7) & ~(size_t)7;
         return q;
     };
-    u64 *h_in_off = (u64 *)take(8 * n), *h_coff = (u64 *)take(8 * n), *h_out_off = (u64 *)take(8 * (n + 1));
-    u32 *h_in_len = (u32 *)take(4 * n), *h_isize = (u32 *)take(4 * n), *h_crc = (u32 *)take(4 * n);
-    u32 *h_order = (u32 *)take(4 * n);
+    u64 *h_in_off = (u64 *)take(8 * cap), *h_coff = (u64 *)take(8 * cap), *h_out_off = (u64 *)take(8 * (cap + 1));
+    u32 *h_in_len = (u32 *)take(4 * cap), *h_isize = (u32 *)take(4 * cap), *h_crc = (u32 *)take(4 * cap);
+    u32 *h_order = (u32 *)take(4 * cap);
     EngineDevState *h_st = (EngineDevState *)take(sizeof(EngineDevState));
     u64 *h_count = (u64 *)take(8 * kPipeSlices), *h_first = (u64 *)take(8 * kPipeSlices);
-    u64 acc = 0;
-    for (u64 m = 0; m < n; ++m) {
-        h_in_off[m] = spans[m].payload_start;
-        h_in_len[m] = (u32)spans[m].payload_len;
-        h_isize[m] = spans[m].isize;
-        h_crc[m] = spans[m].crc32;
-        h_coff[m] = spans[m].compressed_offset;
-        h_out_off[m] = acc;
-        acc += spans[m].isize;
-    }
-    h_out_off[n] = acc;
-    // groups: members whose last byte lies in slice k or before, not yet taken
-    u64 first[kPipeSlices + 1], m0 = 0;
+    cudaStream_t s = e->stream;
+    if ((ce = cudaMemsetAsync(pp.d_errs, 0xff, 8 * kPipeSlices, s)) != cudaSuccess ||
+        (ce = cudaMemsetAsync(pp.d_heads, 0, 4 * kPipeSlices, s)) != cudaSuccess ||
+        (ce = cudaEventRecord(pp.plan, s)) != cudaSuccess)
+        return cuda_fail(err, ce, "resetting the group state");
     int groups = 0;
+    // on a plan that differs from the bound file's, the groups already
+    // launched finish before the caller's fallback run rewrites their output
+    auto bail = [&]() {
+        for (int k = 0; k < groups; ++k) cudaStreamWaitEvent(s, pp.done[k], 0);
+        return upload_through(kPipeSlices - 1) == cudaSuccess ? 1 : FRT_ERR_CUDA;
+    };
+    std::vector<frt_span> spans;
+    spans.reserve(cap);
+    u64 pos = 0, acc = 0, m0 = 0;
+    std::vector<u32> idx;
     for (int k = 0; k < kPipeSlices; ++k) {
-        u64 m1 = m0;
-        while (m1 < n && spans[m1].payload_start + spans[m1].payload_len + 8 <= slice_end[k]) ++m1;
-        first[k] = m0;
+        size_t consumed = 0;
+        frt_error scratch{};
+        if (slice_end[k] > pos &&
+            discover(host + pos, slice_end[k] - pos, pos, spans, &consumed, &scratch) != FRT_OK)
+            return bail();
+        const u64 m1 = spans.size();
+        if (m1 > cap) return bail();
+        for (u64 m = m0; m < m1; ++m) {
+            h_in_off[m] = pos + spans[m].payload_start; // discover's payload_start is relative to its buffer
+            h_in_len[m] = (u32)spans[m].payload_len;
+            h_isize[m] = spans[m].isize;
+            h_crc[m] = spans[m].crc32;
+            h_coff[m] = spans[m].compressed_offset;
+            h_out_off[m] = acc;
+            acc += spans[m].isize;
+        }
+        pos += consumed;
+        if (acc > e->out_cap) return bail();
         h_first[k] = m0;
         h_count[k] = m1 - m0;
         // longest first within the group, as the single launch's queue
-        std::vector<u32> idx(m1 - m0);
+        idx.resize(m1 - m0);
         for (u64 q = 0; q < m1 - m0; ++q) idx[q] = (u32)q;
         std::stable_sort(idx.begin(), idx.end(), [&](u32 a, u32 b) {
             return spans[m0 + a].payload_len > spans[m0 + b].payload_len;
         });
         std::copy(idx.begin(), idx.end(), h_order + m0);
-        m0 = m1;
+        cudaStream_t sg = pp.lanes[k];
+        struct Copy {
+            void *dst;
+            const void *src;
+            size_t bytes;
+        } copies[] = {{e->in_off + m0, h_in_off + m0, 8 * (m1 - m0)},    {e->coffset + m0, h_coff + m0, 8 * (m1 - m0)},
+                      {e->out_off + m0, h_out_off + m0, 8 * (m1 - m0)},  {e->in_len + m0, h_in_len + m0, 4 * (m1 - m0)},
+                      {e->isize + m0, h_isize + m0, 4 * (m1 - m0)},      {e->crc_expect + m0, h_crc + m0, 4 * (m1 - m0)},
+                      {e->order + m0, h_order + m0, 4 * (m1 - m0)},      {pp.d_count + k, h_count + k, 8},
+                      {pp.d_first + k, h_first + k, 8}};
+        for (const Copy &c : copies)
+            if (c.bytes && (ce = cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyHostToDevice, pp.copy)) != cudaSuccess)
+                return cuda_fail(err, ce, "uploading the plan");
+        // slice k and plan k are on the device once up[k] fires
+        if ((ce = cudaEventRecord(pp.up[k], pp.copy)) != cudaSuccess ||
+            (ce = upload_through(k + kLookahead)) != cudaSuccess)
+            return cuda_fail(err, ce, "uploading the file");
+        if ((ce = cudaStreamWaitEvent(sg, pp.plan, 0)) != cudaSuccess ||
+            (ce = cudaStreamWaitEvent(sg, pp.up[k], 0)) != cudaSuccess)
+            return cuda_fail(err, ce, "ordering the inflate");
+        if (m1 > m0 &&
+            (ce = frt_launch_inflate_persistent(e->in, e->in_off + m0, e->in_len + m0, e->out, e->out_off + m0,
+                                                e->isize + m0, e->crc_expect + m0, e->status + m0, e->produced + m0,
+                                                e->crc + m0, e->order + m0, pp.d_count + k, m1 - m0, e->out_cap,
+                                                pp.d_heads + k, (u32)e->grid, (unsigned long long *)(pp.d_errs + k),
+                                                e->tuning, sg)) != cudaSuccess)
+            return cuda_fail(err, ce, "launching the inflate");
+        if ((ce = cudaEventRecord(pp.done[k], sg)) != cudaSuccess) return cuda_fail(err, ce, "ordering the inflate");
         groups = k + 1;
+        m0 = m1;
     }
-    if (m0 != n) return 1;
-    first[kPipeSlices] = n;
+    if (pos != len || m0 != cap) return bail();
+    const u64 n = m0;
+    h_out_off[n] = acc;
     memset(h_st, 0, sizeof(EngineDevState));
     h_st->block_err = ~0ull;
     h_st->n_members = n;
     h_st->inflated_total = acc;
-    cudaStream_t s = e->stream;
-    struct Copy {
-        void *dst;
-        const void *src;
-        size_t bytes;
-    } copies[] = {{e->in_off, h_in_off, 8 * n},   {e->coffset, h_coff, 8 * n},  {e->out_off, h_out_off, 8 * (n + 1)},
-                  {e->in_len, h_in_len, 4 * n},   {e->isize, h_isize, 4 * n},   {e->crc_expect, h_crc, 4 * n},
-                  {e->order, h_order, 4 * n},     {e->st, h_st, sizeof(EngineDevState)},
-                  {pp.d_count, h_count, 8 * kPipeSlices}, {pp.d_first, h_first, 8 * kPipeSlices}};
-    for (const Copy &c : copies)
-        if ((ce = cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
-            return cuda_fail(err, ce, "uploading the plan");
-    if ((ce = cudaMemsetAsync(pp.d_errs, 0xff, 8 * kPipeSlices, s)) != cudaSuccess ||
-        (ce = cudaMemsetAsync(pp.d_heads, 0, 4 * kPipeSlices, s)) != cudaSuccess ||
-        (ce = cudaEventRecord(pp.plan, s)) != cudaSuccess)
-        return cuda_fail(err, ce, "uploading the plan");
-    for (int k = 0; k < groups; ++k) {
-        cudaStream_t sg = (k & 1) ? pp.side : s;
-        if ((ce = cudaStreamWaitEvent(sg, pp.up[k], 0)) != cudaSuccess ||
-            (ce = cudaStreamWaitEvent(sg, pp.plan, 0)) != cudaSuccess)
-            return cuda_fail(err, ce, "ordering the inflate");
-        const u64 f = first[k];
-        if (first[k + 1] > f &&
-            (ce = frt_launch_inflate_persistent(e->in, e->in_off + f, e->in_len + f, e->out, e->out_off + f,
-                                                e->isize + f, e->crc_expect + f, e->status + f, e->produced + f,
-                                                e->crc + f, e->order + f, pp.d_count + k, first[k + 1] - f,
-                                                e->out_cap, pp.d_heads + k, (u32)e->grid,
-                                                (unsigned long long *)(pp.d_errs + k), e->tuning, sg)) != cudaSuccess)
-            return cuda_fail(err, ce, "launching the inflate");
-        if ((ce = cudaEventRecord(pp.done[k], sg)) != cudaSuccess) return cuda_fail(err, ce, "ordering the inflate");
-    }
     for (int k = 0; k < groups; ++k)
-        if ((k & 1) && (ce = cudaStreamWaitEvent(s, pp.done[k], 0)) != cudaSuccess)
-            return cuda_fail(err, ce, "joining the inflate");
+        if ((ce = cudaStreamWaitEvent(s, pp.done[k], 0)) != cudaSuccess) return cuda_fail(err, ce, "joining the inflate");
+    if ((ce = cudaMemcpyAsync(e->out_off + n, h_out_off + n, 8, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(e->st, h_st, sizeof(EngineDevState), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(err, ce, "uploading the totals");
     // the next run's uploads wait for everything that reads this run's staging
     k_merge_group_errors<<<1, 32, 0, s>>>(pp.d_errs, pp.d_first, (u32)groups, e->st);
     if ((ce = enqueue_records(e, true)) != cudaSuccess) return cuda_fail(err, ce, "launching the record stages");
