@@ -134,21 +134,41 @@ __device__ void spec_member(const u8 *buf, u64 len, const u64 *starts, u32 m, u6
     } else if (ms <= start) {
         e = start;
     } else {
-        for (u64 base = ms; base < me; base += 32) {
-            u64 p = base + lane;
-            bool ok = p < me && plausible(buf, len, p, n_ref);
-            if (ok) {
-                // the next two records must validate as well, wherever they
-                // fall in the batch (a decoy's length usually lands far away)
-                u64 q = p + 4ull + ld_u32le(buf + p);
-                for (int k = 0; k < 2 && ok && q + 36 <= len; ++k) {
-                    ok = plausible(buf, len, q, n_ref);
-                    q += 4ull + ld_u32le(buf + q);
+        // 128 offsets a turn, four a lane.  plausible() needs ref_id in
+        // [-1, n_ref), which random bytes almost never hold, so each lane first
+        // builds its four ref_id words from two aligned word loads and runs the
+        // full test only where that passes.  A word outside [0, len) reads as 0
+        // (the full test then rejects the offset: its header would pass len);
+        // the ref_id words of any offset with a whole header lie inside.
+        const long long A = (long long)(((uintptr_t)(buf + ms) & ~(uintptr_t)3) - (uintptr_t)buf);
+        for (long long base = A; base < (long long)me; base += 128) {
+            const long long wo = base + 4ll * lane + 4ll;
+            const u32 w0 = wo >= 0 && wo + 4 <= (long long)len ? *(const u32 *)(buf + wo) : 0u;
+            const u32 w1 = wo + 4 >= 0 && wo + 8 <= (long long)len ? *(const u32 *)(buf + wo + 4) : 0u;
+            u32 first = 4;
+#pragma unroll
+            for (u32 k = 0; k < 4u; ++k) {
+                const u32 ref = k ? __funnelshift_r(w0, w1, 8u * k) : w0;
+                const long long ps = base + 4ll * lane + k;
+                if (first == 4 && ps >= (long long)ms && ps < (long long)me && ref + 1u <= (u32)n_ref) {
+                    const u64 p = (u64)ps;
+                    bool ok = plausible(buf, len, p, n_ref);
+                    if (ok) {
+                        // the next two records must validate as well, wherever they
+                        // fall in the batch (a decoy's length usually lands far away)
+                        u64 q = p + 4ull + ld_u32le(buf + p);
+                        for (int j = 0; j < 2 && ok && q + 36 <= len; ++j) {
+                            ok = plausible(buf, len, q, n_ref);
+                            q += 4ull + ld_u32le(buf + q);
+                        }
+                    }
+                    if (ok) first = k;
                 }
             }
-            u32 hit = __ballot_sync(FRT_FULL_MASK, ok);
+            const u32 hit = __ballot_sync(FRT_FULL_MASK, first < 4u);
             if (hit) {
-                e = base + (u64)(__ffs(hit) - 1);
+                const u32 src = (u32)(__ffs(hit) - 1);
+                e = (u64)(base + 4ll * src + __shfl_sync(FRT_FULL_MASK, first, src));
                 break;
             }
         }
@@ -324,11 +344,7 @@ __device__ void reconcile_chain(const u8 *buf, u64 len, const u64 *starts, u32 n
             // a member holds records if it was proven with an entry; covered
             // decoys were cleared above; members after a stop hold none
             bool proven = m < stop_at && e != INF64;
-            if (proven) {
-                u64 me = starts[m + 1];
-                (void)me;
-                c = count[m];
-            }
+            if (proven) c = count[m];
             if (!proven && m < n_members) count[m] = 0;
         }
         u32 x = c;
@@ -463,6 +479,28 @@ namespace {
 
 // One aux field at `pos` (aux.rs:301-405): returns the offset just past it,
 // or 0 when malformed.  Fills type/subtype/value offset/count.
+// The first zero byte of rec[q, end), or end.  Long Z strings (MM:Z of an
+// ultra-long read runs to 100 KB) go 32 bytes a step through aligned 16-byte
+// loads; no load reaches past end.
+__device__ __forceinline__ u32 find_nul(const u8 *rec, u32 q, u32 end)
+{
+    for (; q < end && ((uintptr_t)(rec + q) & 15u); ++q)
+        if (rec[q] == 0) return q;
+    for (; q + 32u <= end; q += 32u) {
+        const uint4 a = *(const uint4 *)(rec + q), b = *(const uint4 *)(rec + q + 16u);
+        const u32 m[8] = {__vcmpeq4(a.x, 0u), __vcmpeq4(a.y, 0u), __vcmpeq4(a.z, 0u), __vcmpeq4(a.w, 0u),
+                          __vcmpeq4(b.x, 0u), __vcmpeq4(b.y, 0u), __vcmpeq4(b.z, 0u), __vcmpeq4(b.w, 0u)};
+        if (m[0] | m[1] | m[2] | m[3] | m[4] | m[5] | m[6] | m[7]) {
+#pragma unroll
+            for (u32 k = 0; k < 8u; ++k)
+                if (m[k]) return q + 4u * k + ((u32)(__ffs(m[k]) - 1) >> 3);
+        }
+    }
+    for (; q < end; ++q)
+        if (rec[q] == 0) return q;
+    return end;
+}
+
 __device__ __forceinline__ u32 aux_field(const u8 *rec, u32 pos, u32 end, u32 *w0, u32 *voff, u32 *cnt)
 {
     if (pos + 3 > end) return 0;
@@ -474,8 +512,7 @@ __device__ __forceinline__ u32 aux_field(const u8 *rec, u32 pos, u32 end, u32 *w
     case 's': case 'S': next = v + 2; break;
     case 'i': case 'I': case 'f': next = v + 4; break;
     case 'Z': case 'H': {
-        u32 q = v;
-        while (q < end && rec[q] != 0) ++q;
+        const u32 q = find_nul(rec, v, end);
         if (q >= end) return 0;
         count = q - v;
         if (ty == 'H') {
