@@ -448,6 +448,7 @@ struct frt_engine {
     };
     bool multi = false;
     std::vector<File> files;
+    std::vector<u64> bound_coff, bound_out_off; // the plan the file views were built on
     frt_bam_decoder *bam_dec = nullptr;
     frt_fastq_scanner *fastq = nullptr;
     frt_bcf_scanner *bcf = nullptr;
@@ -994,6 +995,8 @@ extern "C" int frt_engine_bind_files(frt_engine *e, const uint8_t *dev, size_t l
     }
     coff[n] = len;
     e->multi = true;
+    e->bound_coff.assign(coff.begin(), coff.begin() + n);
+    e->bound_out_off = out_off;
     // decoders on the engine's stream
     if (!e->bam_dec && (rc = frt_bam_decoder_create(e->device, s, &e->bam_dec, err))) return rc;
     if (!e->fastq && (rc = frt_fastq_scanner_create(e->device, s, &e->fastq, err))) return rc;
@@ -1358,6 +1361,9 @@ int run_host_pipelined(frt_engine *e, const uint8_t *host, size_t len, frt_error
         }
         pos += consumed;
         if (acc > e->out_cap) return bail();
+        if (e->multi) // the per-file views hold the bound plan's offsets
+            for (u64 m = m0; m < m1; ++m)
+                if (h_coff[m] != e->bound_coff[m] || h_out_off[m] != e->bound_out_off[m]) return bail();
         h_first[k] = m0;
         h_count[k] = m1 - m0;
         // longest first within the group, as the single launch's queue
@@ -1398,7 +1404,7 @@ int run_host_pipelined(frt_engine *e, const uint8_t *host, size_t len, frt_error
         groups = k + 1;
         m0 = m1;
     }
-    if (pos != len || m0 != cap) return bail();
+    if (pos != len || m0 != cap || (e->multi && acc != e->bound_out_off[cap])) return bail();
     const u64 n = m0;
     h_out_off[n] = acc;
     memset(h_st, 0, sizeof(EngineDevState));
@@ -1412,7 +1418,8 @@ int run_host_pipelined(frt_engine *e, const uint8_t *host, size_t len, frt_error
         return cuda_fail(err, ce, "uploading the totals");
     // the next run's uploads wait for everything that reads this run's staging
     k_merge_group_errors<<<1, 32, 0, s>>>(pp.d_errs, pp.d_first, (u32)groups, e->st);
-    if ((ce = enqueue_records(e, true)) != cudaSuccess) return cuda_fail(err, ce, "launching the record stages");
+    if (!e->multi && (ce = enqueue_records(e, true)) != cudaSuccess)
+        return cuda_fail(err, ce, "launching the record stages");
     if ((ce = cudaEventRecord(pp.plan, s)) != cudaSuccess) return cuda_fail(err, ce, "ordering the run");
     return FRT_OK;
 }
@@ -1428,20 +1435,25 @@ extern "C" int frt_engine_run_host(frt_engine *e, const uint8_t *host, size_t le
                   "bind a device buffer of this length first; run_host refills it from host memory");
         return FRT_ERR_INVALID_ARGUMENT;
     }
-    if (!e->multi) {
-        int rc = run_host_pipelined(e, host, len, err);
-        if (rc == FRT_OK) return frt_engine_finish(e, stats, err);
-        if (rc != 1) return rc;
-        // the host plan differs from the bound file's: the bytes are (being)
-        // uploaded on the copy stream; run the single launch after them
-        cudaError_t ce = cudaEventRecord(e->pipe.up[kPipeSlices - 1], e->pipe.copy);
-        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(e->stream, e->pipe.up[kPipeSlices - 1], 0);
-        if (ce != cudaSuccess) return cuda_fail(err, ce, "ordering after the upload");
-    } else {
-        cudaError_t ce = cudaMemcpyAsync((void *)e->in, host, len, cudaMemcpyHostToDevice, e->stream);
-        if (ce != cudaSuccess) return cuda_fail(err, ce, "uploading the file");
+    int rc = run_host_pipelined(e, host, len, err);
+    if (rc == FRT_OK) {
+        if (e->multi) { // the inflate's status, then each file's decoder, as run_multi
+            e->decode_rc = inflate_status(e, &e->decode_err);
+            if (!e->decode_rc) e->decode_rc = decode_files(e, &e->decode_err);
+            if (e->decode_rc) {
+                if (err) *err = e->decode_err;
+                return e->decode_rc;
+            }
+        }
+        return frt_engine_finish(e, stats, err);
     }
-    int rc = frt_engine_run(e, err);
+    if (rc != 1) return rc;
+    // the host plan differs from the bound file's: the bytes are (being)
+    // uploaded on the copy stream; run the single launch after them
+    cudaError_t ce = cudaEventRecord(e->pipe.up[kPipeSlices - 1], e->pipe.copy);
+    if (ce == cudaSuccess) ce = cudaStreamWaitEvent(e->stream, e->pipe.up[kPipeSlices - 1], 0);
+    if (ce != cudaSuccess) return cuda_fail(err, ce, "ordering after the upload");
+    rc = frt_engine_run(e, err);
     if (rc) return rc;
     return frt_engine_finish(e, stats, err);
 }

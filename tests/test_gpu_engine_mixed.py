@@ -120,3 +120,38 @@ def test_mixed_reports_the_first_bad_member(gpu):
         eng.run()
         eng.finish()
     assert ei.value.offset == fq_off + second
+
+
+def test_mixed_run_host_overlaps_the_upload_and_matches(gpu):
+    """run_host on several files: the slices go up while the host plans, each
+    group is inflated as it lands, then every file's decoder runs."""
+    torch = pytest.importorskip("torch")
+    files = _files()
+    eng, dev, layout = _bind(gpu, torch, files)
+    blob = np.concatenate([f[2] for f in files])
+    pinned = torch.from_numpy(blob).pin_memory().numpy()
+    for host in (pinned, pinned, np.array(blob)):
+        dev.zero_()  # the run must bring the bytes itself
+        torch.cuda.synchronize()
+        st = eng.run_host(host)
+        assert st.status == 0
+        assert st.inflated_bytes == sum(f[1].size for f in files)
+        _check(gpu, eng, files, layout)
+
+
+def test_mixed_run_host_reports_the_first_bad_member(gpu):
+    torch = pytest.importorskip("torch")
+    files = _files()
+    eng, dev, layout = _bind(gpu, torch, files)
+    blob = np.concatenate([f[2] for f in files])
+    fq_off = layout[2][0]
+    spans, _ = oracle.discover(files[2][2])
+    second = int(spans[1]["compressed_offset"])
+    bad = blob.copy()
+    bad[fq_off + int(spans[1]["payload_start"] + spans[1]["payload_len"])] ^= 0xFF
+    with pytest.raises(gpu.ChecksumMismatch) as ei:
+        eng.run_host(bad)
+    assert ei.value.offset == fq_off + second
+    st = eng.run_host(blob)  # and the good files afterwards are fine
+    assert st.status == 0
+    _check(gpu, eng, files, layout)
