@@ -212,7 +212,8 @@ template <int MODE> __device__ __forceinline__ void emit(const Span &sp, const u
 // every aligned block that holds a record byte lies inside the allocation.
 constexpr u32 kStageBlocks = 128;
 constexpr u32 kStageLoads = kStageBlocks / 32;
-constexpr u32 kBigSpan = 4096; // records with more bytes go to k_fields_copy_big
+constexpr u32 kBigSpan = 4096;  // records with more bytes go to k_fields_copy_big
+constexpr u32 kPiece = 16384;   // a warp's share of such a record at a time (eight turns)
 
 template <int MODE> __device__ __forceinline__ void copy_spans(const Span *spans, u8 *stage, u32 lane)
 {
@@ -293,7 +294,7 @@ template <int MODE> __device__ __forceinline__ void copy_spans(const Span *spans
 // lengths, plus the CTA's prefix from k_scan_parts, gives the output offsets,
 // written straight into the result; then each warp copies its 32 records.
 template <int MODE> __global__ void __launch_bounds__(kRoundRecords, 4) k_fields_copy(RecordView v, const u64 *part,
-                                                                                    u64 stride, CopyOut out, u32 *big,
+                                                                                    u64 stride, CopyOut out, u64 *big,
                                                                                     u32 *big_count, u32 big_cap)
 {
     constexpr int K = kinds<MODE>();
@@ -348,8 +349,9 @@ template <int MODE> __global__ void __launch_bounds__(kRoundRecords, 4) k_fields
 #pragma unroll
         for (int c = 0; c < 6; ++c) sp.cut[c] = cut[c];
         if (cut[5] > kBigSpan) { // k_fields_copy_big's, an empty span here
-            const u32 slot = atomicAdd(big_count, 1u);
-            if (slot < big_cap) big[slot] = (u32)i;
+            const u32 np = ((u32)(src & 15u) + cut[5] + kPiece - 1u) / kPiece;
+            const u32 slot = atomicAdd(big_count, np);
+            for (u32 j = 0; j < np && slot + j < big_cap; ++j) big[slot + j] = ((u64)i << 20) | j;
             sp.cut[5] = 0;
         }
         __syncthreads();
@@ -434,38 +436,36 @@ __global__ void k_cigar_resolve(RecordView v, u64 *offset, u32 *ops, u8 *status)
     status[i] = st;
 }
 
-// Records whose bytes pass kBigSpan, listed by k_fields_copy: CTAs take one
-// at a time and their warps split its turns, so the work is shared by bytes
-// rather than by records (a few reads of hundreds of kilobytes would
-// otherwise hold one warp each while the rest of the GPU idles).
+// Records whose bytes pass kBigSpan, listed by k_fields_copy as pieces of
+// kPiece bytes (record index << 20 | piece): each warp takes one piece at a
+// time and copies its turns, so the work is shared out by bytes and no warp
+// waits on another (a few reads of hundreds of kilobytes would otherwise hold
+// one warp each while the rest of the GPU idles).
 template <int MODE> __global__ void __launch_bounds__(kRoundRecords, 4)
-    k_fields_copy_big(RecordView v, const u32 *big, const u32 *big_count, u32 big_cap, u32 *big_next, CopyOut out)
+    k_fields_copy_big(RecordView v, const u64 *big, const u32 *big_count, u32 big_cap, u32 *big_next, CopyOut out)
 {
     constexpr int K = kinds<MODE>();
     constexpr u32 kTurn = 16u * kStageBlocks;
-    constexpr u32 kWarps = kRoundRecords / 32;
-    __shared__ __align__(16) u8 stage[kWarps][kTurn];
-    __shared__ Span sp_s;
-    __shared__ u32 b_s;
+    __shared__ __align__(16) u8 stage[kRoundRecords / 32][kTurn];
     const u32 lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
-    const u32 nbig = min(*big_count, big_cap);
+    const u32 npieces = min(*big_count, big_cap);
+    u8 *st = stage[w];
     for (;;) {
-        if (threadIdx.x == 0) b_s = atomicAdd(big_next, 1u);
-        __syncthreads();
-        const u32 b = b_s;
-        if (b >= nbig) break;
-        if (threadIdx.x == 0) {
-            const u64 i = big[b];
-            sp_s.src = record_span(v, i, MODE, sp_s.cut);
+        u32 b = 0;
+        if (lane == 0) b = atomicAdd(big_next, 1u);
+        b = __shfl_sync(FRT_FULL_MASK, b, 0);
+        if (b >= npieces) break;
+        const u64 item = big[b];
+        const u64 i = item >> 20;
+        const u32 piece = (u32)(item & 0xfffffu);
+        Span sp;
+        sp.src = record_span(v, i, MODE, sp.cut);
 #pragma unroll
-            for (int k = 0; k < K; ++k) sp_s.dst[k] = out.data[k] + out.off[k][i];
-        }
-        __syncthreads();
-        const Span &sp = sp_s;
+        for (int k = 0; k < K; ++k) sp.dst[k] = out.data[k] + out.off[k][i];
         const u32 len = sp.cut[5], o = (u32)(sp.src & 15u);
         const u8 *a0 = (const u8 *)(sp.src - o);
-        u8 *st = stage[w];
-        for (u32 cb = kTurn * w; cb < len + o; cb += kTurn * kWarps) {
+        const u32 stop = min(len + o, (piece + 1u) * kPiece);
+        for (u32 cb = piece * kPiece; cb < stop; cb += kTurn) {
             uint4 x[kStageLoads];
 #pragma unroll
             for (u32 h = 0; h < kStageLoads; ++h) {
@@ -479,7 +479,6 @@ template <int MODE> __global__ void __launch_bounds__(kRoundRecords, 4)
             emit<MODE>(sp, st + o - cb, cb > o ? cb - o : 0u, min(len, cb + kTurn - o), lane);
             __syncwarp();
         }
-        __syncthreads(); // sp_s and b_s are rewritten next
     }
 }
 
@@ -627,13 +626,16 @@ int frt::fields_run(const RecordView &v, int op, const char *tag, int device, cu
                 o.off[k] = (u64 *)col(2 * k);
                 o.data[k] = col(2 * k + 1);
             }
-            // a record past kBigSpan bytes holds more than kBigSpan - 1 payload
-            // bytes (compact drops at most the name's NUL), which bounds the list
+            // A record past kBigSpan bytes holds at least kBigSpan payload bytes
+            // (compact drops at most the name's NUL, so span <= payload + 1)
+            // and splits into at most span / kPiece + 2 pieces: the list holds
+            // at most payload / kPiece + 3 * records of them.
             u64 payload = 0;
             for (int k = 0; k < kinds; ++k) payload += totals[k];
-            const u64 cap64 = payload / (kBigSpan - 1) + 1;
-            const u32 cap = (u32)(cap64 < n ? cap64 : n);
-            u32 *big = nullptr, *counters = nullptr;
+            const u64 records = payload / kBigSpan + 1, cap64 = payload / kPiece + 3 * records + 2;
+            const u32 cap = (u32)(cap64 < 0xffffffffull ? cap64 : 0xffffffffull);
+            u64 *big = nullptr;
+            u32 *counters = nullptr;
             int sms = 0;
             if ((rc = tmp.get(&big, cap, err)) || (rc = tmp.get(&counters, 2, err))) return fail(rc);
             if ((e = cudaMemsetAsync(counters, 0, 8, st)) != cudaSuccess ||
