@@ -171,24 +171,26 @@ __device__ __forceinline__ u8 base_of(u32 nib)
 }
 
 // Writes the record's bytes [lo, hi) to its payloads; in[r] is its byte r.
-template <int MODE> __device__ __forceinline__ void emit(const Span &sp, const u8 *in, u32 lo, u32 hi, u32 lane)
+// pairs[b] holds the two bases of packed byte b, the high nibble's first.
+template <int MODE>
+__device__ __forceinline__ void emit(const Span &sp, const u8 *in, u32 lo, u32 hi, u32 lane, const u16 *pairs)
 {
     if (MODE == COPY_BASES) {
         const u32 l = sp.cut[0];
         u8 *d = sp.dst[0];
         if (((uintptr_t)d & 1u) == 0) {
             for (u32 r = lo + lane; r < hi; r += 32u) {
-                const u32 b = in[r];
+                const u32 v = pairs[in[r]];
                 if (2u * r + 1u < l)
-                    *(unsigned short *)(d + 2u * r) = (unsigned short)(base_of(b >> 4) | ((u32)base_of(b & 15u) << 8));
+                    *(u16 *)(d + 2u * r) = (u16)v;
                 else
-                    d[2u * r] = base_of(b >> 4);
+                    d[2u * r] = (u8)v;
             }
         } else {
             for (u32 r = lo + lane; r < hi; r += 32u) {
-                const u32 b = in[r];
-                d[2u * r] = base_of(b >> 4);
-                if (2u * r + 1u < l) d[2u * r + 1u] = base_of(b & 15u);
+                const u32 v = pairs[in[r]];
+                d[2u * r] = (u8)v;
+                if (2u * r + 1u < l) d[2u * r + 1u] = (u8)(v >> 8);
             }
         }
     } else {
@@ -215,7 +217,8 @@ constexpr u32 kStageLoads = kStageBlocks / 32;
 constexpr u32 kBigSpan = 4096;  // records with more bytes go to k_fields_copy_big
 constexpr u32 kPiece = 16384;   // a warp's share of such a record at a time (eight turns)
 
-template <int MODE> __device__ __forceinline__ void copy_spans(const Span *spans, u8 *stage, u32 lane)
+template <int MODE>
+__device__ __forceinline__ void copy_spans(const Span *spans, u8 *stage, u32 lane, const u16 *pairs)
 {
     const Span &mine = spans[lane];
     const u32 mo = (u32)(mine.src & 15u);
@@ -249,7 +252,7 @@ template <int MODE> __device__ __forceinline__ void copy_spans(const Span *spans
                 for (u32 h = 0; h < kStageLoads; ++h)
                     if (cb + 16u * (lane + 32u * h) < len + o) *(uint4 *)(stage + 16u * (lane + 32u * h)) = v[h];
                 __syncwarp();
-                emit<MODE>(sp, stage + o - cb, cb > o ? cb - o : 0u, min(len, cb + 16u * kStageBlocks - o), lane);
+                emit<MODE>(sp, stage + o - cb, cb > o ? cb - o : 0u, min(len, cb + 16u * kStageBlocks - o), lane, pairs);
                 __syncwarp();
             }
             ++j0;
@@ -283,7 +286,7 @@ template <int MODE> __device__ __forceinline__ void copy_spans(const Span *spans
         for (u32 j = j0; j < j1; ++j) {
             const Span &sp = spans[j];
             const u32 first = __shfl_sync(FRT_FULL_MASK, excl, j) - base;
-            if (sp.cut[5]) emit<MODE>(sp, stage + 16u * first + (u32)(sp.src & 15u), 0u, sp.cut[5], lane);
+            if (sp.cut[5]) emit<MODE>(sp, stage + 16u * first + (u32)(sp.src & 15u), 0u, sp.cut[5], lane, pairs);
         }
         __syncwarp();
         j0 = j1;
@@ -302,7 +305,10 @@ template <int MODE> __global__ void __launch_bounds__(kRoundRecords, 4) k_fields
     __shared__ __align__(16) u8 stage[kRoundRecords / 32][16 * kStageBlocks];
     __shared__ u64 wsum[K][kRoundRecords / 32];
     __shared__ u64 carry[K]; // each kind's bytes before this round
+    __shared__ u16 pairs[MODE == COPY_BASES ? 256 : 1];
     const u32 lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    if (MODE == COPY_BASES)
+        for (u32 b = threadIdx.x; b < 256u; b += blockDim.x) pairs[b] = (u16)(base_of(b >> 4) | ((u32)base_of(b & 15u) << 8));
     const u64 b0 = (u64)blockIdx.x * kBlockRecords;
     if (threadIdx.x < (u32)K) carry[threadIdx.x] = part[threadIdx.x * stride + blockIdx.x];
     for (u32 q = 0; q < kRounds; ++q) {
@@ -356,7 +362,7 @@ template <int MODE> __global__ void __launch_bounds__(kRoundRecords, 4) k_fields
         }
         __syncthreads();
         if (threadIdx.x < (u32)K) carry[threadIdx.x] = next_carry; // read again after the round's last barrier
-        copy_spans<MODE>(spans + 32u * w, stage[w], lane);
+        copy_spans<MODE>(spans + 32u * w, stage[w], lane, pairs);
         __syncthreads();
     }
 }
@@ -447,7 +453,12 @@ template <int MODE> __global__ void __launch_bounds__(kRoundRecords, 4)
     constexpr int K = kinds<MODE>();
     constexpr u32 kTurn = 16u * kStageBlocks;
     __shared__ __align__(16) u8 stage[kRoundRecords / 32][kTurn];
+    __shared__ u16 pairs[MODE == COPY_BASES ? 256 : 1];
     const u32 lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+    if (MODE == COPY_BASES) {
+        for (u32 b = threadIdx.x; b < 256u; b += blockDim.x) pairs[b] = (u16)(base_of(b >> 4) | ((u32)base_of(b & 15u) << 8));
+        __syncthreads();
+    }
     const u32 npieces = min(*big_count, big_cap);
     u8 *st = stage[w];
     for (;;) {
@@ -476,7 +487,7 @@ template <int MODE> __global__ void __launch_bounds__(kRoundRecords, 4)
             for (u32 h = 0; h < kStageLoads; ++h)
                 if (cb + 16u * (lane + 32u * h) < len + o) *(uint4 *)(st + 16u * (lane + 32u * h)) = x[h];
             __syncwarp();
-            emit<MODE>(sp, st + o - cb, cb > o ? cb - o : 0u, min(len, cb + kTurn - o), lane);
+            emit<MODE>(sp, st + o - cb, cb > o ? cb - o : 0u, min(len, cb + kTurn - o), lane, pairs);
             __syncwarp();
         }
     }
