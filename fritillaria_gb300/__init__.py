@@ -307,6 +307,11 @@ def lib():
         "frt_text_scanner_create": (C.c_int, [C.c_int, _P, _P, _P]),
         "frt_text_scanner_destroy": (None, [_P]),
         "frt_text_scan": (C.c_int, [_P, _P, C.c_uint64, C.c_int32, C.c_int32, _P, _P]),
+        "frt_vcf_decoder_create": (C.c_int, [C.c_int, _P, _P, _P]),
+        "frt_vcf_decoder_destroy": (None, [_P]),
+        "frt_vcf_set_contigs": (C.c_int, [_P, _P, _P, C.c_size_t, _P]),
+        "frt_vcf_set_contigs_from_header": (C.c_int, [_P, _P, C.c_size_t, _P, _P]),
+        "frt_vcf_decode": (C.c_int, [_P, _P, _P, _P]),
         "frt_bcf_parse_header": (C.c_int, [_P, C.c_size_t, _P, _P, _P, _P]),
         "frt_bcf_scanner_create": (C.c_int, [C.c_int, _P, _P, _P]),
         "frt_bcf_scanner_destroy": (None, [_P]),
@@ -875,6 +880,74 @@ class TextScanner(_Scanner):
         _raise(lib().frt_text_scan(self._h, batch.handle if batch is not None else None, int(start), int(comment),
                                    -1 if secondary is None else int(secondary), C.byref(out), C.byref(err)), err)
         return ColumnBatch(out, TEXT_COLUMNS)
+
+
+VCF_COLUMNS = {"chrom": (0, np.int32), "pos": (1, np.uint64), "bounds": (2, np.uint32), "n_alt": (3, np.uint32),
+               "qual": (4, np.uint32), "flags": (5, np.uint16), "status": (6, np.uint8)}
+VCF_BOUNDS = 9  # ends of CHROM, POS, ID, REF, ALT, QUAL, FILTER, INFO, and of the line
+
+
+class VcfFlag(enum.IntFlag):
+    """FRT_VCF_FLAG_*: missing fields ("."), FILTER PASS, QUAL parsed on the
+    device, the telomere start."""
+    ID_MISSING = 1
+    ALT_MISSING = 2
+    QUAL_MISSING = 4
+    FILTER_MISSING = 8
+    INFO_MISSING = 16
+    SAMPLES_MISSING = 32
+    FILTER_PASS = 64
+    QUAL_PARSED = 128
+    TELOMERE = 256
+
+
+class VcfStatus(enum.IntEnum):
+    OK = 0
+    UNEXPECTED_EOL = 1     # fewer than eight fields (read_record's "unexpected EOL")
+    INVALID_POSITION = 2   # POS is not a usize, or is 0 written other than "0"
+
+
+class VcfColumns(ColumnBatch):
+    """The fixed fields of a text scan's VCF records; `bounds` comes back as
+    (records, VCF_BOUNDS) and `quality()` as float32 (NaN where not parsed)."""
+
+    def column(self, name: str) -> np.ndarray:
+        out = super().column(name)
+        return out.reshape(-1, VCF_BOUNDS) if name == "bounds" else out
+
+    def quality(self) -> np.ndarray:
+        return self.column("qual").view(np.float32)
+
+
+class VcfDecoder(_Scanner):
+    """Columnar VCF on the device over the text framing -- the step the
+    reference's README names after its text scan (README.md, "What's next"),
+    with the vendored lazy reader's field semantics
+    (crates/fritillaria-vcf/src/io/reader/record.rs:9-118,
+    src/record/fields.rs:20-103).  CHROM becomes an index into the contig
+    dictionary set here."""
+    _create, _destroy = "frt_vcf_decoder_create", "frt_vcf_decoder_destroy"
+
+    def set_contigs(self, names) -> None:
+        bufs = [bytes(n, "ascii") if isinstance(n, str) else bytes(n) for n in names]
+        arr = (C.c_char_p * max(1, len(bufs)))(*bufs)
+        lens = (C.c_size_t * max(1, len(bufs)))(*[len(b) for b in bufs])
+        err = _Err()
+        _raise(lib().frt_vcf_set_contigs(self._h, arr, lens, len(bufs), C.byref(err)), err)
+
+    def set_contigs_from_header(self, text) -> int:
+        """The contigs of a header's "##contig=<ID=...>" lines; returns how many."""
+        b = _u8(text)
+        n = C.c_size_t()
+        err = _Err()
+        _raise(lib().frt_vcf_set_contigs_from_header(self._h, b.ctypes.data if b.size else None, b.size, C.byref(n),
+                                                     C.byref(err)), err)
+        return n.value
+
+    def decode(self, text: ColumnBatch) -> VcfColumns:
+        out, err = _P(), _Err()
+        _raise(lib().frt_vcf_decode(self._h, text._h, C.byref(out), C.byref(err)), err)
+        return VcfColumns(out, VCF_COLUMNS)
 
 
 def parse_bcf_header(data):

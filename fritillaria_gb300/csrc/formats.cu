@@ -1762,3 +1762,412 @@ extern "C" int frt_text_scan(frt_text_scanner *sc, const frt_inflate_batch *b, u
     }
     return columns_finish(c, b, out);
 }
+
+// ---- columnar VCF over the text framing --------------------------------------
+//
+// The fixed fields of every VCF record of a text batch, with the semantics of
+// the vendored lazy reader: read_record (crates/fritillaria-vcf/src/io/reader/
+// record.rs:9-118) takes seven tab-terminated fields, then the INFO field up to
+// a tab or the end of the line, and drops a carriage return before the line
+// feed; the accessors (record/fields.rs:20-103, record.rs:35-79) read "."
+// as missing, "0" as the telomere start, a position with usize::from_str and
+// Position::try_from, the quality with f32::from_str, and the alternate bases
+// split on ','.  The reference's own device path stops at the text framing
+// (its README lists columnar VCF.gz as the next step); this is that step.
+
+namespace {
+
+const size_t kVcfWidths[FRT_VCF_COL_COUNT] = {4, 8, 4 * FRT_VCF_BOUNDS, 4, 4, 2, 1};
+enum { FMT_VCF = 5 };
+
+struct VcfDict {
+    const u32 *slots = nullptr; // index + 1 per slot, 0 empty; open addressing
+    const u32 *name_off = nullptr; // n + 1 offsets into names
+    const u8 *names = nullptr;
+    u32 mask = 0, n = 0;
+};
+
+__host__ __device__ __forceinline__ u32 fnv1a(const u8 *p, u32 n)
+{
+    u32 h = 2166136261u;
+    for (u32 i = 0; i < n; ++i) h = (h ^ p[i]) * 16777619u;
+    return h;
+}
+
+__device__ int vcf_contig(const VcfDict &d, const u8 *p, u32 n)
+{
+    if (!d.n) return -1;
+    for (u32 s = fnv1a(p, n) & d.mask;; s = (s + 1) & d.mask) {
+        const u32 v = d.slots[s];
+        if (!v) return -1;
+        const u32 a = d.name_off[v - 1], b = d.name_off[v];
+        if (b - a != n) continue;
+        u32 i = 0;
+        while (i < n && d.names[a + i] == p[i]) ++i;
+        if (i == n) return (int)(v - 1);
+    }
+}
+
+// usize::from_str: an optional '+', then one or more ASCII digits, no overflow.
+__device__ bool vcf_usize(const u8 *p, u32 n, u64 *out)
+{
+    u32 i = n && p[0] == '+' ? 1u : 0u;
+    if (i == n) return false;
+    u64 v = 0;
+    for (; i < n; ++i) {
+        const u32 c = (u32)p[i] - '0';
+        if (c > 9u) return false;
+        if (v > (~0ull - c) / 10ull) return false;
+        v = v * 10ull + c;
+    }
+    *out = v;
+    return true;
+}
+
+__device__ __forceinline__ bool vcf_is(const u8 *p, u32 n, const char *lit, u32 m)
+{
+    if (n != m) return false;
+    for (u32 i = 0; i < m; ++i)
+        if (p[i] != (u8)lit[i]) return false;
+    return true;
+}
+
+// The quality as f32::from_str would give it, when Clinger's fast path
+// ("How to read floating point numbers accurately", 1990) applies: a decimal
+// of at most 2^24 with a power of ten of at most 10^10 either way, both exact
+// in binary32, so one correctly rounded multiply or divide is the correctly
+// rounded value.  Anything else -- more digits, a larger exponent, inf, NaN or
+// text f32::from_str rejects -- is left unparsed (returns false).
+__device__ bool vcf_qual(const u8 *p, u32 n, float *out)
+{
+    u32 i = 0;
+    bool neg = false;
+    if (i < n && (p[i] == '+' || p[i] == '-')) neg = p[i++] == '-';
+    u64 m = 0;
+    int e10 = 0, digits = 0;
+    bool big = false;
+    for (; i < n && p[i] >= '0' && p[i] <= '9'; ++i, ++digits) {
+        if (m < 100000000000000000ull) m = m * 10ull + (p[i] - '0');
+        else { big = true; ++e10; }
+    }
+    if (i < n && p[i] == '.') {
+        for (++i; i < n && p[i] >= '0' && p[i] <= '9'; ++i, ++digits)
+            if (m < 100000000000000000ull) { m = m * 10ull + (p[i] - '0'); --e10; }
+            else big = true;
+    }
+    if (!digits) return false;
+    if (i < n && (p[i] == 'e' || p[i] == 'E')) {
+        ++i;
+        bool eneg = false;
+        if (i < n && (p[i] == '+' || p[i] == '-')) eneg = p[i++] == '-';
+        if (i == n) return false;
+        int x = 0;
+        for (; i < n && p[i] >= '0' && p[i] <= '9'; ++i)
+            if (x < 100000) x = x * 10 + (p[i] - '0');
+        e10 += eneg ? -x : x;
+    }
+    if (i != n || big) return false;
+    if (m == 0) {
+        *out = neg ? -0.0f : 0.0f;
+        return true;
+    }
+    while (e10 < 0 && m % 10ull == 0) { // trailing zeros of the fraction
+        m /= 10ull;
+        ++e10;
+    }
+    while (e10 > 10 && m * 10ull <= (1ull << 24)) { // a small mantissa absorbs the excess exponent
+        m *= 10ull;
+        --e10;
+    }
+    if (m > (1ull << 24) || e10 > 10 || e10 < -10) return false;
+    const float p10[11] = {1e0f, 1e1f, 1e2f, 1e3f, 1e4f, 1e5f, 1e6f, 1e7f, 1e8f, 1e9f, 1e10f};
+    const float v = (float)m;
+    const float r = e10 >= 0 ? __fmul_rn(v, p10[e10]) : __fdiv_rn(v, p10[-e10]);
+    *out = neg ? -r : r;
+    return true;
+}
+
+__global__ void k_vcf_fields(const u8 *buf, u64 buf_len, const u64 *rec_off, const u64 *rec_end, const u64 *tabs,
+                             const u64 *field_starts, u64 n, VcfDict dict, int *chrom, u64 *pos, u32 *bounds,
+                             u32 *n_alt, u32 *qual, u16 *flags, u8 *status)
+{
+    const u64 r = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const u64 a = rec_off[r];
+    const u8 *p = buf + a;
+    const u32 len = (u32)(rec_end[r] - a);
+    const u64 fs = field_starts[r], nt = field_starts[r + 1] - fs;
+    // read_field and read_line drop a carriage return before a line feed; a
+    // record ends at its line feed, or at the batch end when it has none
+    const bool lf = rec_end[r] < buf_len;
+    const u32 content = lf && len && p[len - 1] == '\r' ? len - 1 : len;
+    u32 e[FRT_VCF_BOUNDS] = {};
+    int cid = -1;
+    u64 v = 0;
+    u32 na = 0, qv = 0x7fc00000u;
+    u16 fl = 0;
+    u8 st = 0;
+    if (nt < 7) {
+        st = FRT_VCF_STATUS_UNEXPECTED_EOL;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 7; ++k) e[k] = (u32)(tabs[fs + k] - a);
+        e[7] = nt >= 8 ? (u32)(tabs[fs + 7] - a) : content;
+        e[8] = content;
+        cid = vcf_contig(dict, p, e[0]);
+        const u8 *f = p + e[0] + 1;
+        u32 fn = e[1] - e[0] - 1;
+        if (vcf_is(f, fn, "0", 1)) {
+            fl |= FRT_VCF_FLAG_TELOMERE;
+        } else if (!vcf_usize(f, fn, &v) || v == 0) {
+            v = 0;
+            st = FRT_VCF_STATUS_INVALID_POSITION;
+        }
+        if (vcf_is(p + e[1] + 1, e[2] - e[1] - 1, ".", 1)) fl |= FRT_VCF_FLAG_ID_MISSING;
+        f = p + e[3] + 1;
+        fn = e[4] - e[3] - 1;
+        if (vcf_is(f, fn, ".", 1)) {
+            fl |= FRT_VCF_FLAG_ALT_MISSING;
+        } else if (fn) {
+            na = 1;
+            for (u32 i = 0; i < fn; ++i) na += f[i] == ',' ? 1u : 0u;
+        }
+        f = p + e[4] + 1;
+        fn = e[5] - e[4] - 1;
+        float q;
+        if (vcf_is(f, fn, ".", 1)) fl |= FRT_VCF_FLAG_QUAL_MISSING;
+        else if (vcf_qual(f, fn, &q)) {
+            fl |= FRT_VCF_FLAG_QUAL_PARSED;
+            qv = __float_as_uint(q);
+        }
+        f = p + e[5] + 1;
+        fn = e[6] - e[5] - 1;
+        if (vcf_is(f, fn, ".", 1)) fl |= FRT_VCF_FLAG_FILTER_MISSING;
+        else if (vcf_is(f, fn, "PASS", 4)) fl |= FRT_VCF_FLAG_FILTER_PASS;
+        if (vcf_is(p + e[6] + 1, e[7] - e[6] - 1, ".", 1)) fl |= FRT_VCF_FLAG_INFO_MISSING;
+        // samples: what follows INFO; missing when empty or its first piece is "."
+        if (nt < 8) {
+            fl |= FRT_VCF_FLAG_SAMPLES_MISSING;
+        } else {
+            const u32 s0 = e[7] + 1, s1 = nt >= 9 ? (u32)(tabs[fs + 8] - a) : content;
+            if (s0 >= content || vcf_is(p + s0, s1 - s0, ".", 1)) fl |= FRT_VCF_FLAG_SAMPLES_MISSING;
+        }
+    }
+    chrom[r] = cid;
+    pos[r] = v;
+#pragma unroll
+    for (int k = 0; k < FRT_VCF_BOUNDS; ++k) bounds[FRT_VCF_BOUNDS * r + k] = e[k];
+    n_alt[r] = na;
+    qual[r] = qv;
+    flags[r] = fl;
+    status[r] = st;
+}
+
+} // namespace
+
+struct frt_vcf_decoder {
+    Scanner s;
+    u32 *slots = nullptr, *name_off = nullptr;
+    u8 *names = nullptr;
+    u32 mask = 0, n = 0;
+};
+
+extern "C" int frt_vcf_decoder_create(int device, void *stream, frt_vcf_decoder **out, frt_error *err)
+{
+    if (!out) return FRT_ERR_INVALID_ARGUMENT;
+    frt_vcf_decoder *d = new frt_vcf_decoder;
+    int rc = scanner_create(device, stream, &d->s, err);
+    if (rc) {
+        delete d;
+        return rc;
+    }
+    *out = d;
+    return FRT_OK;
+}
+
+namespace {
+void vcf_free_dict(frt_vcf_decoder *d)
+{
+    dev_free(d->slots, d->s.stream);
+    dev_free(d->name_off, d->s.stream);
+    dev_free(d->names, d->s.stream);
+    d->slots = d->name_off = nullptr;
+    d->names = nullptr;
+    d->mask = d->n = 0;
+}
+} // namespace
+
+extern "C" void frt_vcf_decoder_destroy(frt_vcf_decoder *d)
+{
+    if (!d) return;
+    {
+        DeviceGuardLite g(d->s.device);
+        vcf_free_dict(d);
+        cudaStreamSynchronize(d->s.stream);
+    }
+    stream_release(d->s.shared);
+    delete d;
+}
+
+// The contig dictionary CHROM is looked up in: names[i] (lens[i] bytes) is
+// contig i.  A name given twice keeps its first index.
+extern "C" int frt_vcf_set_contigs(frt_vcf_decoder *d, const char *const *names, const size_t *lens, size_t n,
+                                   frt_error *err)
+{
+    if (!d || (n && (!names || !lens)) || n >= 0x7fffffffu) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument or too many contigs");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    DeviceGuardLite g(d->s.device);
+    std::lock_guard<std::mutex> lk(d->s.mu);
+    std::vector<u32> off(n + 1, 0);
+    std::vector<u8> blob;
+    for (size_t i = 0; i < n; ++i) {
+        if (!names[i] && lens[i]) {
+            set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "contig %zu has no name", i);
+            return FRT_ERR_INVALID_ARGUMENT;
+        }
+        blob.insert(blob.end(), (const u8 *)names[i], (const u8 *)names[i] + lens[i]);
+        if (blob.size() >= 0xffffffffull) {
+            set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "contig names exceed 4 GiB");
+            return FRT_ERR_INVALID_ARGUMENT;
+        }
+        off[i + 1] = (u32)blob.size();
+    }
+    u32 cap = 16;
+    while (cap < 2 * n) cap <<= 1;
+    std::vector<u32> slots(cap, 0);
+    for (size_t i = 0; i < n; ++i) {
+        const u8 *p = blob.data() + off[i];
+        const u32 len = off[i + 1] - off[i];
+        u32 s = fnv1a(p, len) & (cap - 1);
+        bool dup = false;
+        for (; slots[s]; s = (s + 1) & (cap - 1)) {
+            const u32 j = slots[s] - 1;
+            if (off[j + 1] - off[j] == len && std::memcmp(blob.data() + off[j], p, len) == 0) {
+                dup = true;
+                break;
+            }
+        }
+        if (!dup) slots[s] = (u32)i + 1;
+    }
+    cudaStream_t st = d->s.stream;
+    vcf_free_dict(d);
+    int rc;
+    if ((rc = dev_alloc((void **)&d->slots, 4 * slots.size(), st, err)) ||
+        (rc = dev_alloc((void **)&d->name_off, 4 * off.size(), st, err)) ||
+        (rc = dev_alloc((void **)&d->names, blob.size() + 1, st, err))) {
+        vcf_free_dict(d);
+        return rc;
+    }
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(d->slots, slots.data(), 4 * slots.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d->name_off, off.data(), 4 * off.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+        (blob.size() &&
+         (e = cudaMemcpyAsync(d->names, blob.data(), blob.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess) ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+        vcf_free_dict(d);
+        return cuda_fail(err, e, "uploading the contig dictionary");
+    }
+    d->mask = cap - 1;
+    d->n = (u32)n;
+    return FRT_OK;
+}
+
+// The contigs of a VCF header: the ID of every "##contig=<...>" line, in
+// order (the VCF 4.x meta-information structure; keys are comma-separated
+// inside the angle brackets and the ID value runs to the next ',' or '>').
+extern "C" int frt_vcf_set_contigs_from_header(frt_vcf_decoder *d, const uint8_t *text, size_t len, size_t *n_out,
+                                               frt_error *err)
+{
+    if (!d || (len && !text)) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    static const char kPrefix[] = "##contig=<";
+    const size_t kp = sizeof(kPrefix) - 1;
+    std::vector<const char *> names;
+    std::vector<size_t> lens;
+    size_t i = 0;
+    while (i < len) {
+        size_t eol = i;
+        while (eol < len && text[eol] != '\n') ++eol;
+        if (eol - i > kp && std::memcmp(text + i, kPrefix, kp) == 0) {
+            size_t k = i + kp;
+            while (k < eol) {
+                size_t ke = k;
+                while (ke < eol && text[ke] != '=' && text[ke] != ',' && text[ke] != '>') ++ke;
+                if (ke < eol && text[ke] == '=') {
+                    size_t ve = ke + 1;
+                    bool quoted = ve < eol && text[ve] == '"';
+                    if (quoted) {
+                        ++ve;
+                        while (ve < eol && text[ve] != '"') ++ve;
+                        if (ve < eol) ++ve;
+                    }
+                    while (ve < eol && text[ve] != ',' && text[ve] != '>') ++ve;
+                    if (ke - k == 2 && text[k] == 'I' && text[k + 1] == 'D') {
+                        names.push_back((const char *)text + ke + 1);
+                        lens.push_back(ve - ke - 1);
+                        break;
+                    }
+                    k = ve + 1;
+                } else {
+                    k = ke + 1;
+                }
+            }
+        }
+        i = eol + 1;
+    }
+    if (n_out) *n_out = names.size();
+    return frt_vcf_set_contigs(d, names.data(), lens.data(), names.size(), err);
+}
+
+// Columns of the records of a text scan (frt_text_scan with the VCF dialect);
+// the result holds the scan's batch alive.
+extern "C" int frt_vcf_decode(frt_vcf_decoder *d, const frt_columns *text, frt_columns **out, frt_error *err)
+{
+    if (!d || !text || !out || text->format != FMT_TEXT) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument, or not the result of a text scan");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    Scanner &s = d->s;
+    DeviceGuardLite g(s.device);
+    std::lock_guard<std::mutex> lk(s.mu);
+    if (text->device != s.device) {
+        set_error(err, FRT_ERR_INVALID_DEVICE_BATCH, 0, 0, 0, 0, nullptr, "text columns on device %d, decoder on %d",
+                  text->device, s.device);
+        return FRT_ERR_INVALID_DEVICE_BATCH;
+    }
+    cudaError_t e;
+    if (text->ready && (e = cudaStreamWaitEvent(s.stream, text->ready, 0)) != cudaSuccess)
+        return cuda_fail(err, e, "ordering after the text scan");
+    const u64 n = text->n;
+    frt_columns *c = columns_new(s, FMT_VCF, kVcfWidths, FRT_VCF_COL_COUNT, n);
+    c->tail = text->tail;
+    int rc = columns_alloc(c, err);
+    if (rc) {
+        columns_discard(c);
+        return rc;
+    }
+    if (n) {
+        const frt_columns *t = text;
+        auto tcol = [&](int k) { return (const u64 *)(t->cols + t->col_off[k]); };
+        VcfDict dict;
+        dict.slots = d->slots;
+        dict.name_off = d->name_off;
+        dict.names = d->names;
+        dict.mask = d->mask;
+        dict.n = d->n;
+        k_vcf_fields<<<grid_for(n, 256), 256, 0, s.stream>>>(
+            text->source->data, text->source->len, tcol(FRT_TEXT_COL_RECORD_OFFSETS), tcol(FRT_TEXT_COL_RECORD_ENDS),
+            tcol(FRT_TEXT_COL_TABS), tcol(FRT_TEXT_COL_FIELD_STARTS), n, dict, colp<int>(c, FRT_VCF_COL_CHROM),
+            colp<u64>(c, FRT_VCF_COL_POS), colp<u32>(c, FRT_VCF_COL_BOUNDS), colp<u32>(c, FRT_VCF_COL_N_ALT),
+            colp<u32>(c, FRT_VCF_COL_QUAL), colp<u16>(c, FRT_VCF_COL_FLAGS), colp<u8>(c, FRT_VCF_COL_STATUS));
+        if ((e = cudaGetLastError()) != cudaSuccess) {
+            columns_discard(c);
+            return cuda_fail(err, e, "launching the VCF decode");
+        }
+    }
+    return columns_finish(c, text->source, out);
+}

@@ -352,6 +352,69 @@ void frt_text_scanner_destroy(frt_text_scanner *s);
 int frt_text_scan(frt_text_scanner *s, const frt_inflate_batch *batch, uint64_t start, int32_t comment,
                   int32_t secondary, frt_columns **out, frt_error *err);
 
+/* ---- columnar VCF: the fixed fields of a text scan's records ---------------
+ * The records of frt_text_scan with the VCF dialect (comment '#'), each read
+ * as the vendored lazy reader reads it: read_record
+ * (crates/fritillaria-vcf/src/io/reader/record.rs:9-118: seven tab-terminated
+ * fields, then INFO up to a tab or the end of the line, a carriage return
+ * before the line feed dropped; fewer fields is "unexpected EOL") and the
+ * accessors of src/record/fields.rs:20-103 and src/record.rs:35-79 ("." is
+ * missing, POS "0" the telomere, else usize::from_str then a non-zero
+ * Position; QUAL f32::from_str; ALT split on ','; samples missing when empty
+ * or their first field is "."). The reference's device path ends at the text
+ * framing and its README names columnar VCF.gz as the next step: there is no
+ * reference interface to replace, so these entry points are additions. */
+typedef struct frt_vcf_decoder frt_vcf_decoder;
+enum { FRT_VCF_BOUNDS = 9 };
+typedef enum {
+    FRT_VCF_COL_CHROM = 0,  /* i32: CHROM's index in the contig dictionary, -1 when absent */
+    FRT_VCF_COL_POS = 1,    /* u64: the 1-based start; 0 for the telomere and for an invalid POS */
+    FRT_VCF_COL_BOUNDS = 2, /* u32 x FRT_VCF_BOUNDS a record, from the record's first byte: the ends of
+                               CHROM, POS, ID, REF, ALT, QUAL, FILTER and INFO, then of the line
+                               (carriage return dropped); field k > 0 starts one past the end of
+                               field k - 1, the samples one past INFO's end when a tab follows it */
+    FRT_VCF_COL_N_ALT = 3,  /* u32: alternate alleles (0 when ALT is "." or empty) */
+    FRT_VCF_COL_QUAL = 4,   /* u32: the f32 bits of QUAL when FRT_VCF_FLAG_QUAL_PARSED, else a NaN */
+    FRT_VCF_COL_FLAGS = 5,  /* u16: FRT_VCF_FLAG_* */
+    FRT_VCF_COL_STATUS = 6, /* u8: FRT_VCF_STATUS_* */
+    FRT_VCF_COL_COUNT = 7
+} frt_vcf_column;
+enum {
+    FRT_VCF_FLAG_ID_MISSING = 1,
+    FRT_VCF_FLAG_ALT_MISSING = 2,
+    FRT_VCF_FLAG_QUAL_MISSING = 4,
+    FRT_VCF_FLAG_FILTER_MISSING = 8,
+    FRT_VCF_FLAG_INFO_MISSING = 16,
+    FRT_VCF_FLAG_SAMPLES_MISSING = 32,
+    FRT_VCF_FLAG_FILTER_PASS = 64,
+    /* QUAL parsed on the device: decimals of at most 2^24 with a power of ten
+       of at most 10^10 either way (Clinger's fast path, exact).  A QUAL that
+       is neither missing nor parsed (longer decimals, inf, NaN, or text that
+       f32::from_str rejects) is left to the caller, by its bounds. */
+    FRT_VCF_FLAG_QUAL_PARSED = 128,
+    FRT_VCF_FLAG_TELOMERE = 256
+};
+enum {
+    FRT_VCF_STATUS_OK = 0,
+    FRT_VCF_STATUS_UNEXPECTED_EOL = 1,    /* fewer than eight fields: the record's other columns are 0 */
+    FRT_VCF_STATUS_INVALID_POSITION = 2   /* POS is not a usize, or is 0 written other than "0" */
+};
+
+int frt_vcf_decoder_create(int device, void *stream, frt_vcf_decoder **out, frt_error *err);
+void frt_vcf_decoder_destroy(frt_vcf_decoder *d);
+/* The contig dictionary: names[i] (lens[i] bytes) is contig i; a repeated
+ * name keeps its first index.  Replaces any earlier dictionary. */
+int frt_vcf_set_contigs(frt_vcf_decoder *d, const char *const *names, const size_t *lens, size_t n,
+                        frt_error *err);
+/* The dictionary from a VCF header's text: the ID of each "##contig=<...>"
+ * line, in order; *n_contigs = how many. */
+int frt_vcf_set_contigs_from_header(frt_vcf_decoder *d, const uint8_t *text, size_t len, size_t *n_contigs,
+                                    frt_error *err);
+/* Columns FRT_VCF_COL_* of the records of `text` (an frt_text_scan result);
+ * frt_columns_len and frt_columns_tail are the scan's; the result holds the
+ * scan's batch alive. */
+int frt_vcf_decode(frt_vcf_decoder *d, const frt_columns *text, frt_columns **out, frt_error *err);
+
 /* ---- record fields: opt-in device kernels over decoded BAM records ---------
  * The reference reads these on the host, record by record: Record::aux_get
  * (crates/fritillaria-bam/src/columnar/record.rs:286-294, over the Fields
