@@ -567,6 +567,17 @@ def text_framing(args, frt, w, peak):
     torch.cuda.synchronize()
     vcf_ms = 1e3 * (time.perf_counter() - t0) / reps
     vcf_ok = int((cols.column("status") == 0).sum())
+    gt = dec.genotypes(out)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        gt = dec.genotypes(out)
+    torch.cuda.synchronize()
+    gt_ms = 1e3 * (time.perf_counter() - t0) / reps
+    n_calls = int(out.column_ptr("tabs")[1] // 8) - 8 * len(out)
+    called = int(((gt.column("calls") >> 28) == 0).sum()) - 8 * len(out)  # tabs before FORMAT hold 0
+    # per call: the sample's bytes read (about 4) and its u32 written; per record its tabs read
+    gt_algo = raw.size + 4 * n_calls + 8 * n_calls
     res = {"text_bytes": int(raw.size), "compressed_bytes": int(bgz.size), "records": len(out),
            "header_lines": int(out.scan_info()[0]), "tabs": int(out.column_ptr("tabs")[1] // 8),
            "column_bytes": int(col_bytes), "scan_ms": round(ms, 3),
@@ -576,7 +587,13 @@ def text_framing(args, frt, w, peak):
            "vcf_decode": {"ms": round(vcf_ms, 4), "records_ok": vcf_ok, "contigs": n_contigs,
                           "records_per_s": round(len(out) / (vcf_ms / 1e3)),
                           "form": "wall time per VcfDecoder.decode over the scan's columns (CHROM index, POS, "
-                                  "field bounds, ALT count, QUAL, flags, status)"}}
+                                  "field bounds, ALT count, QUAL, flags, status)"},
+           "genotypes": {"ms": round(gt_ms, 4), "calls": n_calls, "called": called,
+                         "calls_per_s": round(n_calls / (gt_ms / 1e3)),
+                         "hbm_frac": round(gt_algo / (gt_ms / 1e3) / 1e9 / peak, 4),
+                         "algorithmic_bytes": gt_algo,
+                         "form": "wall time per VcfDecoder.genotypes: every sample's GT as a packed u32 "
+                                 "(algorithmic bytes: the text read, the 8-byte tabs read, a u32 per call)"}}
     if not args.no_cpu:
         from oracle import text
 

@@ -312,6 +312,7 @@ def lib():
         "frt_vcf_set_contigs": (C.c_int, [_P, _P, _P, C.c_size_t, _P]),
         "frt_vcf_set_contigs_from_header": (C.c_int, [_P, _P, C.c_size_t, _P, _P]),
         "frt_vcf_decode": (C.c_int, [_P, _P, _P, _P]),
+        "frt_vcf_genotypes": (C.c_int, [_P, _P, _P, _P]),
         "frt_bcf_parse_header": (C.c_int, [_P, C.c_size_t, _P, _P, _P, _P]),
         "frt_bcf_scanner_create": (C.c_int, [C.c_int, _P, _P, _P]),
         "frt_bcf_scanner_destroy": (None, [_P]),
@@ -948,6 +949,48 @@ class VcfDecoder(_Scanner):
         out, err = _P(), _Err()
         _raise(lib().frt_vcf_decode(self._h, text._h, C.byref(out), C.byref(err)), err)
         return VcfColumns(out, VCF_COLUMNS)
+
+    def genotypes(self, text: ColumnBatch) -> "VcfGenotypes":
+        """Every sample's GT (value/genotype/iter.rs), one call per tab."""
+        out, err = _P(), _Err()
+        _raise(lib().frt_vcf_genotypes(self._h, text._h, C.byref(out), C.byref(err)), err)
+        return VcfGenotypes(out, VCF_GT_COLUMNS)
+
+
+VCF_GT_COLUMNS = {"calls": (0, np.uint32), "key": (1, np.int32)}
+
+
+class GtStatus(enum.IntEnum):
+    """FRT_VCF_GT_*: bits 28-31 of a call."""
+    CALLED = 0
+    MISSING = 1        # the value is "."
+    NONE = 2           # no value: no GT key, a shorter or empty sample, no samples
+    INVALID = 3        # the reader's error
+    UNREPRESENTED = 4  # valid but more than two alleles, or an index above 4093
+
+
+class VcfGenotypes(ColumnBatch):
+    """Every sample's GT: `calls` has one u32 per tab of the text scan, the
+    call of the sample that tab opens; `unpack()` splits calls into status,
+    ploidy, phasing and allele indices (-1 for ".")."""
+
+    @staticmethod
+    def unpack(calls: np.ndarray) -> dict:
+        c = calls.astype(np.uint32)
+        return {"status": (c >> 28).astype(np.uint8), "ploidy": ((c >> 26) & 3).astype(np.uint8),
+                "phased": np.stack([(c >> 24) & 1, (c >> 25) & 1], -1).astype(np.uint8),
+                "alleles": np.stack([(c & 0xFFF).astype(np.int32) - 1, ((c >> 12) & 0xFFF).astype(np.int32) - 1], -1)}
+
+    def matrix(self, text: ColumnBatch) -> np.ndarray:
+        """The calls as (records, samples), when every record has as many samples."""
+        fs = text.column("field_starts").astype(np.int64)
+        if len(fs) < 2:
+            return np.zeros((0, 0), np.uint32)
+        ns = np.diff(fs) - 8
+        if (ns != ns[0]).any() or ns[0] < 0:
+            raise ValueError("records have different numbers of samples")
+        calls = self.column("calls")
+        return calls[(fs[:-1, None] + 8 + np.arange(ns[0])[None, :])]
 
 
 def parse_bcf_header(data):

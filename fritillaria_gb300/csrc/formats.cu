@@ -1778,7 +1778,8 @@ extern "C" int frt_text_scan(frt_text_scanner *sc, const frt_inflate_batch *b, u
 namespace {
 
 const size_t kVcfWidths[FRT_VCF_COL_COUNT] = {4, 8, 4 * FRT_VCF_BOUNDS, 4, 4, 2, 1};
-enum { FMT_VCF = 5 };
+const size_t kVcfGtWidths[FRT_VCF_GT_COL_COUNT] = {4, 4};
+enum { FMT_VCF = 5, FMT_VCF_GT = 6 };
 
 struct VcfDict {
     const u32 *slots = nullptr; // index + 1 per slot, 0 empty; open addressing
@@ -1961,6 +1962,112 @@ __global__ void k_vcf_fields(const u8 *buf, u64 buf_len, const u64 *rec_off, con
     qual[r] = qv;
     flags[r] = fl;
     status[r] = st;
+}
+
+// One sample's GT value (crates/fritillaria-vcf/src/record/samples/series/
+// value.rs:17-30 and value/genotype/iter.rs): "." is missing; otherwise the
+// alleles split before each '|' or '/', the first one's phasing explicit when
+// it opens with one, else unphased when a '/' follows anywhere and phased
+// when none does; each position "." or usize::from_str; an empty value is an
+// error.  Packed as FRT_VCF_GT_*.
+__device__ u32 vcf_gt_code(const u8 *p, u32 n)
+{
+    if (n == 1 && p[0] == '.') return (u32)FRT_VCF_GT_MISSING << 28;
+    if (n == 0) return (u32)FRT_VCF_GT_INVALID << 28;
+    u32 codes[2] = {0, 0}, phased[2] = {0, 0}, ploidy = 0;
+    u32 i = 0;
+    while (i < n) {
+        // the allele: [i, j) with the next separator searched from i + 1
+        u32 j = i + 1;
+        while (j < n && p[j] != '|' && p[j] != '/') ++j;
+        u32 a = i, ph;
+        if (p[a] == '|' || p[a] == '/') {
+            ph = p[a] == '|';
+            ++a;
+        } else { // only the first allele can lack a separator
+            ph = 1;
+            for (u32 k = j; k < n; ++k)
+                if (p[k] == '/') ph = 0;
+        }
+        u32 code;
+        if (j - a == 1 && p[a] == '.') {
+            code = 0;
+        } else {
+            u64 v;
+            if (!vcf_usize(p + a, j - a, &v)) return (u32)FRT_VCF_GT_INVALID << 28;
+            if (v >= 4095ull) code = 0x1000u; // valid but wider than 12 bits
+            else code = (u32)v + 1u;
+        }
+        if (ploidy < 2) {
+            codes[ploidy] = code;
+            phased[ploidy] = ph;
+        }
+        ++ploidy;
+        i = j;
+    }
+    // the whole value was walked, so an invalid allele anywhere is reported first
+    if (ploidy > 2 || codes[0] == 0x1000u || codes[1] == 0x1000u) return (u32)FRT_VCF_GT_UNREPRESENTED << 28;
+    return (ploidy << 26) | (phased[1] << 25) | (phased[0] << 24) | (codes[1] << 12) | codes[0];
+}
+
+// Every sample's GT, a warp per record with lanes over its samples.  calls[t]
+// is the call of the sample that tab t opens (tabs 8 on of each record); the
+// first eight tabs of a record get 0.  key[r] = GT's index among the FORMAT
+// keys, -1 when the record has no samples or no GT key.
+__global__ void k_vcf_gt(const u8 *buf, u64 buf_len, const u64 *rec_off, const u64 *rec_end, const u64 *tabs,
+                         const u64 *field_starts, u64 n, u32 *calls, int *key)
+{
+    const u64 r = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const u32 lane = threadIdx.x & 31u;
+    if (r >= n) return;
+    const u64 a = rec_off[r];
+    const u8 *p = buf + a;
+    const u32 len = (u32)(rec_end[r] - a);
+    const u64 fs = field_starts[r], nt = field_starts[r + 1] - fs;
+    const u32 content = rec_end[r] < buf_len && len && p[len - 1] == '\r' ? len - 1 : len;
+    for (u64 t = lane; t < nt && t < 8ull; t += 32) calls[fs + t] = 0;
+    if (nt < 8) {
+        if (lane == 0) key[r] = -1;
+        return;
+    }
+    // FORMAT: [tab 7 + 1, tab 8 or the end); samples are missing when there
+    // is nothing after INFO or FORMAT is "."
+    const u32 f0 = (u32)(tabs[fs + 7] - a) + 1u, f1 = nt >= 9 ? (u32)(tabs[fs + 8] - a) : content;
+    int g = -1;
+    if (f0 < content && !(f1 - f0 == 1 && p[f0] == '.')) {
+        int k = 0;
+        for (u32 q = f0; q <= f1; ++k) {
+            u32 e = q;
+            while (e < f1 && p[e] != ':') ++e;
+            if (e - q == 2 && p[q] == 'G' && p[q + 1] == 'T') {
+                g = k;
+                break;
+            }
+            q = e + 1;
+        }
+    }
+    if (lane == 0) key[r] = g;
+    for (u64 j = lane; j + 8 < nt; j += 32) {
+        u32 code = (u32)FRT_VCF_GT_NONE << 28;
+        if (g >= 0) {
+            const u32 s0 = (u32)(tabs[fs + 8 + j] - a) + 1u;
+            const u32 s1 = j + 9 < nt ? (u32)(tabs[fs + 9 + j] - a) : content;
+            if (s0 < s1) { // an empty sample has no values
+                u32 q = s0;
+                int k = 0;
+                for (; k < g && q <= s1; ++k) {
+                    while (q < s1 && p[q] != ':') ++q;
+                    ++q;
+                }
+                if (q <= s1) {
+                    u32 e = q;
+                    while (e < s1 && p[e] != ':') ++e;
+                    code = vcf_gt_code(p + q, e - q);
+                }
+            }
+        }
+        calls[fs + 8 + j] = code;
+    }
 }
 
 } // namespace
@@ -2167,6 +2274,56 @@ extern "C" int frt_vcf_decode(frt_vcf_decoder *d, const frt_columns *text, frt_c
         if ((e = cudaGetLastError()) != cudaSuccess) {
             columns_discard(c);
             return cuda_fail(err, e, "launching the VCF decode");
+        }
+    }
+    return columns_finish(c, text->source, out);
+}
+
+// Every sample's GT of the records of `text` (an frt_text_scan result):
+// column FRT_VCF_GT_COL_CALLS has one u32 per tab of the scan, the call of
+// the sample that tab opens; FRT_VCF_GT_COL_KEY one i32 per record.
+extern "C" int frt_vcf_genotypes(frt_vcf_decoder *d, const frt_columns *text, frt_columns **out, frt_error *err)
+{
+    if (!d || !text || !out || text->format != FMT_TEXT) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument, or not the result of a text scan");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
+    Scanner &s = d->s;
+    DeviceGuardLite g(s.device);
+    std::lock_guard<std::mutex> lk(s.mu);
+    if (text->device != s.device) {
+        set_error(err, FRT_ERR_INVALID_DEVICE_BATCH, 0, 0, 0, 0, nullptr, "text columns on device %d, decoder on %d",
+                  text->device, s.device);
+        return FRT_ERR_INVALID_DEVICE_BATCH;
+    }
+    cudaError_t e;
+    if (text->ready && (e = cudaStreamWaitEvent(s.stream, text->ready, 0)) != cudaSuccess)
+        return cuda_fail(err, e, "ordering after the text scan");
+    const u64 n = text->n, n_tabs = text->total;
+    frt_columns *c = columns_new(s, FMT_VCF_GT, kVcfGtWidths, FRT_VCF_GT_COL_COUNT, n);
+    c->tail = text->tail;
+    c->total = n_tabs;
+    c->col_bytes[FRT_VCF_GT_COL_CALLS] = 4 * n_tabs;
+    size_t off = 0;
+    for (int k = 0; k < FRT_VCF_GT_COL_COUNT; ++k) {
+        c->col_off[k] = off;
+        off += (c->col_bytes[k] + 255) & ~(size_t)255;
+    }
+    int rc = columns_alloc(c, err);
+    if (rc) {
+        columns_discard(c);
+        return rc;
+    }
+    if (n) {
+        const frt_columns *t = text;
+        auto tcol = [&](int k) { return (const u64 *)(t->cols + t->col_off[k]); };
+        k_vcf_gt<<<grid_for(n * 32, 256), 256, 0, s.stream>>>(
+            text->source->data, text->source->len, tcol(FRT_TEXT_COL_RECORD_OFFSETS), tcol(FRT_TEXT_COL_RECORD_ENDS),
+            tcol(FRT_TEXT_COL_TABS), tcol(FRT_TEXT_COL_FIELD_STARTS), n, colp<u32>(c, FRT_VCF_GT_COL_CALLS),
+            colp<int>(c, FRT_VCF_GT_COL_KEY));
+        if ((e = cudaGetLastError()) != cudaSuccess) {
+            columns_discard(c);
+            return cuda_fail(err, e, "launching the genotype decode");
         }
     }
     return columns_finish(c, text->source, out);

@@ -415,6 +415,31 @@ int frt_vcf_set_contigs_from_header(frt_vcf_decoder *d, const uint8_t *text, siz
  * scan's batch alive. */
 int frt_vcf_decode(frt_vcf_decoder *d, const frt_columns *text, frt_columns **out, frt_error *err);
 
+/* Genotypes: every sample's GT value (crates/fritillaria-vcf/src/record/
+ * samples/series/value.rs:17-30, value/genotype/iter.rs), found at GT's
+ * position among the FORMAT keys (src/record/samples/sample.rs: keys zipped
+ * with the sample's ':'-separated values).  One u32 per tab of the text scan:
+ * the call of the sample that tab opens (from each record's ninth tab on; the
+ * first eight tabs of a record get 0), so sample j of record i is at
+ * TABS index FIELD_STARTS[i] + 8 + j.  A call packs FRT_VCF_GT_STATUS in bits
+ * 28-31 and, when that is FRT_VCF_GT_CALLED, the ploidy (1 or 2) in bits
+ * 26-27, the second and first alleles' phasing (1 phased) in bits 25 and 24,
+ * and the second and first alleles' index + 1 (0 for ".") in bits 12-23 and
+ * 0-11. */
+typedef enum {
+    FRT_VCF_GT_COL_CALLS = 0, /* u32 per tab of the scan */
+    FRT_VCF_GT_COL_KEY = 1,   /* i32 per record: GT's index among the FORMAT keys; -1 none or no samples */
+    FRT_VCF_GT_COL_COUNT = 2
+} frt_vcf_gt_column;
+enum {
+    FRT_VCF_GT_CALLED = 0,        /* the alleles below */
+    FRT_VCF_GT_MISSING = 1,       /* the value is "." */
+    FRT_VCF_GT_NONE = 2,          /* no value: no GT key, a shorter or empty sample, or no samples */
+    FRT_VCF_GT_INVALID = 3,       /* the reader's error: an empty value or an allele neither "." nor a usize */
+    FRT_VCF_GT_UNREPRESENTED = 4  /* valid, but more than two alleles or an index above 4093: read its text */
+};
+int frt_vcf_genotypes(frt_vcf_decoder *d, const frt_columns *text, frt_columns **out, frt_error *err);
+
 /* ---- record fields: opt-in device kernels over decoded BAM records ---------
  * The reference reads these on the host, record by record: Record::aux_get
  * (crates/fritillaria-bam/src/columnar/record.rs:286-294, over the Fields

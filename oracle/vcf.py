@@ -256,3 +256,83 @@ def decode(buf, scan: dict, contigs=()) -> dict:
         out["flags"][r] = fl
         out["status"][r] = st
     return out
+
+
+GT_CALLED, GT_MISSING, GT_NONE, GT_INVALID, GT_UNREPRESENTED = 0, 1, 2, 3, 4
+
+
+def alleles(v: bytes):
+    """Genotype::iter over a GT value (value/genotype/iter.rs): [(position or
+    None, phased)], or None where the iterator yields an error."""
+    if not v:
+        return None  # UnexpectedEof
+    out, i = [], 0
+    while i < len(v):
+        j = i + 1  # next_allele searches from the second byte
+        while j < len(v) and v[j] not in b"|/":
+            j += 1
+        a = i
+        if v[a] in b"|/":  # explicit phasing (every allele after the first has one)
+            ph, a = v[a] == 124, a + 1
+        else:              # is_implicitly_unphased over what follows
+            ph = b"/" not in v[j:]
+        pos = v[a:j]
+        if pos == b".":
+            x = None
+        else:
+            x = usize(pos)
+            if x is None:
+                return None
+        out.append((x, ph))
+        i = j
+    return out
+
+
+def gt_code(v: bytes) -> int:
+    """One GT value packed as the device packs it: "." is missing
+    (src/record/samples/series/value.rs:26-27), else alleles()."""
+    if v == b".":
+        return GT_MISSING << 28
+    al = alleles(v)
+    if al is None:
+        return GT_INVALID << 28
+    if len(al) > 2 or any(x is not None and x >= 4095 for x, _ in al):
+        return GT_UNREPRESENTED << 28
+    code = [0 if x is None else x + 1 for x, _ in al] + [0]
+    ph = [int(p) for _, p in al] + [0]
+    return (len(al) << 26) | (ph[1] << 25) | (ph[0] << 24) | (code[1] << 12) | code[0]
+
+
+def genotypes(buf, scan: dict):
+    """(calls per tab, GT key index per record) for a text scan's records: the
+    samples follow FORMAT (src/record/fields.rs:86-103 for when they are
+    missing), each value is found at GT's position among the FORMAT keys
+    (src/record/samples/sample.rs: keys zipped with the ':'-pieces of a
+    non-empty sample)."""
+    buf = bytes(np.asarray(buf, np.uint8))
+    offs, ends = scan["record_offsets"], scan["record_ends"]
+    tabs, fs = scan["tabs"], scan["field_starts"]
+    calls = np.zeros(len(tabs), np.uint32)
+    key = np.full(len(offs), -1, np.int32)
+    for r in range(len(offs)):
+        a, b = int(offs[r]), int(ends[r])
+        line = buf[a:b]
+        t = [int(x) - a for x in tabs[int(fs[r]):int(fs[r + 1])]]
+        if len(t) < 8:
+            continue
+        content = len(line) - 1 if b < len(buf) and line.endswith(b"\r") else len(line)
+        fmt = line[t[7] + 1:(t[8] if len(t) >= 9 else content)]
+        g = -1
+        if t[7] + 1 < content and fmt != b".":
+            keys = fmt.split(b":")
+            g = keys.index(b"GT") if b"GT" in keys else -1
+        key[r] = g
+        for j in range(len(t) - 8):
+            code = GT_NONE << 28
+            if g >= 0:
+                s = line[t[8 + j] + 1:(t[9 + j] if 9 + j < len(t) else content)]
+                pieces = s.split(b":") if s else []
+                if g < len(pieces):
+                    code = gt_code(pieces[g])
+            calls[int(fs[r]) + 8 + j] = code
+    return calls, key

@@ -34,11 +34,16 @@ def run(gpu, raw: bytes, contigs=None, header=None):
     elif contigs is not None:
         dec.set_contigs(contigs)
     got = dec.decode(tx)
-    want = vcf.decode(buf, text.device_scan(buf, 0, text.VCF), contigs or ())
+    scan = text.device_scan(buf, 0, text.VCF)
+    want = vcf.decode(buf, scan, contigs or ())
     assert len(got) == len(want["pos"]) == len(tx)
     assert got.tail() == tx.tail()
     for k in COLS:
         assert np.array_equal(got.column(k), want[k]), k
+    gt = dec.genotypes(tx)
+    calls, key = vcf.genotypes(buf, scan)
+    assert np.array_equal(gt.column("calls"), calls) and np.array_equal(gt.column("key"), key)
+    got.gt, got.text = gt, tx
     return got
 
 
@@ -55,6 +60,14 @@ def test_synthetic_population_vcf(gpu):
     header = b"\n".join(l for l in raw.split(b"\n") if l.startswith(b"#"))
     got = run(gpu, raw, header=header)
     assert len(got) == 600 and (got.column("flags") & gpu.VcfFlag.FILTER_PASS).all()
+    m = got.gt.matrix(got.text)
+    assert m.shape == (600, 97)
+    u = gpu.VcfGenotypes.unpack(m)
+    assert (u["status"] == 0).all() and (u["ploidy"] == 2).all() and (u["phased"] == 1).all()
+    # the generator's genotypes, read back from the text
+    lines = [l for l in raw.split(b"\n") if l and not l.startswith(b"#")]
+    want = np.array([[[int(g[0:1]), int(g[2:3])] for g in l.split(b"\t")[9:]] for l in lines])
+    assert np.array_equal(u["alleles"], want)
 
 
 EDGE = [b".\t1\t.\tN\t.\t.\t.\t.",
@@ -124,3 +137,14 @@ def test_dictionary_changes_and_errors(gpu):
     fq = gpu.FastqScanner(0).decode(None, 0)  # columns, but not a text scan's
     with pytest.raises(gpu.InvalidArgument):
         dec.decode(fq)
+
+
+def test_genotype_spellings(gpu):
+    gts = [b"0|0", b"0/1", b"|0/1", b"|1/2|3", b"./.", b".|.", b".", b"", b"1", b"/1", b"0|", b"+1|2", b"-1|2",
+           b"4094|0", b"4095|0", b"12|7", b"0/.", b"0|1|2", b"a|b", b"0:1", b"01|00"]
+    samples = b"\t".join(g + b":9" for g in gts)
+    raw = (b"chr1\t1\t.\tA\tC\t.\t.\t.\tGT:DP\t" + samples + b"\n"
+           b"chr1\t2\t.\tA\tC\t.\t.\t.\tDP:GT\t" + b"\t".join(b"9:" + g for g in gts) + b"\n"
+           b"chr1\t3\t.\tA\tC\t.\t.\t.\tGT\t\t.\t0|1\r\n"
+           b"chr1\t4\t.\tA\tC\t.\t.\t.\tGT\t0/1\r")
+    run(gpu, raw, contigs=[b"chr1"])

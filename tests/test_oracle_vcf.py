@@ -128,3 +128,40 @@ def test_fields_and_missing_markers():
     assert f[2] & vcf.ALT_MISSING and f[2] & vcf.SAMPLES_MISSING  # nothing after INFO's tab
     assert not f[3] & vcf.SAMPLES_MISSING
     assert got["bounds"][4][8] == len(lines[4]) and not f[4] & vcf.INFO_MISSING  # INFO is ".\r"
+
+
+def test_genotype_iterator_vectors():
+    """value/genotype/iter.rs test_next: each value's (position, phasing) list."""
+    assert vcf.alleles(b"0|0") == [(0, True), (0, True)]
+    assert vcf.alleles(b"0/1") == [(0, False), (1, False)]
+    assert vcf.alleles(b"|0/1") == [(0, True), (1, False)]
+    assert vcf.alleles(b"|1/2|3") == [(1, True), (2, False), (3, True)]
+    assert vcf.alleles(b"./.") == [(None, False), (None, False)]
+    assert vcf.alleles(b"") is None  # UnexpectedEof
+    # test_is_implicitly_unphased / test_next_allele, through the first allele
+    assert vcf.alleles(b"0") == [(0, True)]
+    assert vcf.alleles(b"/0") == [(0, False)]
+
+
+def test_genotype_packing_and_lookup():
+    code = vcf.gt_code
+    assert code(b"0|1") == (2 << 26) | (1 << 25) | (1 << 24) | (2 << 12) | 1
+    assert code(b"./.") == 2 << 26
+    assert code(b".") == vcf.GT_MISSING << 28 and code(b"") == vcf.GT_INVALID << 28
+    assert code(b"0|") == vcf.GT_INVALID << 28 and code(b"-1|0") == vcf.GT_INVALID << 28
+    assert code(b"0|1|2") == vcf.GT_UNREPRESENTED << 28 and code(b"4095|0") == vcf.GT_UNREPRESENTED << 28
+    assert code(b"4094|0") & 0xFFF == 4095
+    lines = [b"c\t1\t.\tA\tC\t.\t.\t.\tGT:DP\t0|1:5\t./.:.\t1:3",
+             b"c\t2\t.\tA\tC\t.\t.\t.\tDP:GT\t5:0/1\t7\t\t.:.",
+             b"c\t3\t.\tA\tC\t.\t.\t.\tDP\t5",
+             b"c\t4\t.\tA\tC\t.\t.\t.\t.\t0|1",
+             b"c\t5\t.\tA\tC\t.\t.\t."]
+    buf = np.frombuffer(b"\n".join(lines) + b"\n", np.uint8)
+    scan = text.device_scan(buf, 0, text.VCF)
+    calls, key = vcf.genotypes(buf, scan)
+    assert list(key) == [0, 1, -1, -1, -1]
+    fs = scan["field_starts"].astype(int)
+    row = lambda r: [int(c) for c in calls[fs[r] + 8:fs[r + 1]]]  # noqa: E731
+    assert row(0) == [code(b"0|1"), code(b"./."), code(b"1")]
+    assert row(1) == [code(b"0/1"), vcf.GT_NONE << 28, vcf.GT_NONE << 28, vcf.GT_MISSING << 28]
+    assert row(2) == [vcf.GT_NONE << 28] and row(3) == [vcf.GT_NONE << 28] and row(4) == []
