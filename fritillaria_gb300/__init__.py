@@ -313,6 +313,22 @@ def lib():
         "frt_vcf_set_contigs_from_header": (C.c_int, [_P, _P, C.c_size_t, _P, _P]),
         "frt_vcf_decode": (C.c_int, [_P, _P, _P, _P]),
         "frt_vcf_genotypes": (C.c_int, [_P, _P, _P, _P]),
+        "frt_compressor_create": (C.c_int, [C.c_int, _P, _P, _P]),
+        "frt_compressor_destroy": (None, [_P]),
+        "frt_compressor_name": (C.c_char_p, [_P]),
+        "frt_compressor_device_ordinal": (C.c_int, [_P]),
+        "frt_choose_framing": (C.c_int, [C.c_size_t, C.c_size_t]),
+        "frt_framed_size": (C.c_size_t, [C.c_size_t, C.c_size_t]),
+        "frt_compress_bound": (C.c_size_t, [C.c_size_t]),
+        "frt_compress_batch_device": (C.c_int, [_P, _P, C.c_size_t, _P, C.c_size_t, _P, C.c_size_t, _P, _P, _P]),
+        "frt_bgzf_writer_open": (C.c_int, [_P, _P, _P, _P, _P]),
+        "frt_bgzf_writer_set_chunks_per_batch": (None, [_P, C.c_size_t]),
+        "frt_bgzf_writer_set_payload_size": (None, [_P, C.c_size_t]),
+        "frt_bgzf_writer_write_batch": (C.c_int, [_P, _P, C.c_size_t, _P, C.c_size_t, _P]),
+        "frt_bgzf_writer_write_device": (C.c_int, [_P, _P, C.c_size_t, _P]),
+        "frt_bgzf_writer_finish": (C.c_int, [_P, _P]),
+        "frt_bgzf_writer_stats": (None, [_P, _P, _P, _P, _P]),
+        "frt_bgzf_writer_destroy": (None, [_P]),
         "frt_bcf_parse_header": (C.c_int, [_P, C.c_size_t, _P, _P, _P, _P]),
         "frt_bcf_scanner_create": (C.c_int, [C.c_int, _P, _P, _P]),
         "frt_bcf_scanner_destroy": (None, [_P]),
@@ -991,6 +1007,135 @@ class VcfGenotypes(ColumnBatch):
             raise ValueError("records have different numbers of samples")
         calls = self.column("calls")
         return calls[(fs[:-1, None] + 8 + np.arange(ns[0])[None, :])]
+
+
+# ---------------------------------------------------------------------------
+# the write side
+# ---------------------------------------------------------------------------
+MAX_COMPRESSIBLE_PAYLOAD = 65505  # crates/fritillaria-core/src/compress.rs:51-65
+DEFAULT_PAYLOAD_SIZE = 0xFF00     # crates/fritillaria-bgzf/src/write.rs:19
+EOF_BLOCK = bytes([0x1F, 0x8B, 8, 4, 0, 0, 0, 0, 0, 0xFF, 6, 0, 0x42, 0x43, 2, 0, 0x1B, 0, 3, 0, 0, 0, 0, 0, 0, 0, 0, 0])
+
+
+class Framing(enum.IntEnum):
+    """How a block's payload is encoded (compress.rs:82-98)."""
+    DEFLATED = 0
+    STORED = 1
+    EMPTY = 2
+
+
+def choose_framing(payload_len: int, deflate_len: int) -> Framing:
+    """choose_framing (compress.rs:115-128)."""
+    return Framing(lib().frt_choose_framing(payload_len, deflate_len))
+
+
+def framed_size(payload_len: int, deflate_len: int) -> int:
+    """framed_size (compress.rs:134-142)."""
+    return lib().frt_framed_size(payload_len, deflate_len)
+
+
+class CompressedBatch:
+    """Framed BGZF blocks back to back (compress.rs:157-226): block i is
+    data[offsets[i]:offsets[i + 1]]; no EOF block."""
+
+    def __init__(self, data: np.ndarray, offsets: np.ndarray):
+        self.data, self.offsets = data, offsets
+
+    def __len__(self):
+        return len(self.offsets) - 1
+
+    def block(self, i: int) -> np.ndarray:
+        return self.data[int(self.offsets[i]):int(self.offsets[i + 1])]
+
+    def byte_len(self) -> int:
+        return int(self.data.size)
+
+
+class DeviceCompressor:
+    """DeviceBlockCompressor (crates/fritillaria-core/src/device.rs:326-372) on
+    the GB300: each range of device bytes becomes one BGZF block, inflating back
+    to it exactly."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        h, err = _P(), _Err()
+        _raise(lib().frt_compressor_create(device, stream, C.byref(h), C.byref(err)), err)
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.frt_compressor_destroy(h)
+            self._h = None
+
+    def name(self) -> str:
+        return lib().frt_compressor_name(self._h).decode()
+
+    def device_ordinal(self) -> int:
+        return lib().frt_compressor_device_ordinal(self._h)
+
+    def compress_batch_device(self, data_ptr: int, data_len: int, bounds) -> CompressedBatch:
+        b = np.ascontiguousarray(bounds, dtype=np.uint64)
+        n = max(0, b.size - 1)
+        out = np.empty(max(1, lib().frt_compress_bound(n)), np.uint8)
+        offs = np.zeros(n + 1, np.uint64)
+        got, err = C.c_size_t(), _Err()
+        _raise(lib().frt_compress_batch_device(self._h, data_ptr, data_len, b.ctypes.data, b.size, out.ctypes.data,
+                                               out.size, offs.ctypes.data, C.byref(got), C.byref(err)), err)
+        return CompressedBatch(out[:got.value].copy(), offs)
+
+
+_WRITE_FN = C.CFUNCTYPE(C.c_int64, C.c_void_p, C.c_void_p, C.c_size_t)
+
+
+class DeviceBgzfWriter:
+    """DeviceBgzfWriter (crates/fritillaria-bgzf/src/device_write.rs): device
+    bytes compressed a batch of chunks at a time into `sink` (anything with
+    write(bytes)); finish() appends the EOF block."""
+
+    def __init__(self, sink, compressor: DeviceCompressor, chunks_per_batch: int | None = None,
+                 payload_size: int | None = None):
+        self._sink, self._compressor = sink, compressor
+
+        def _write(_ctx, buf, n):
+            try:
+                self._sink.write(C.string_at(buf, n))
+                return n
+            except Exception:  # the library reports the refusal as Io
+                return -1
+
+        self._cb = _WRITE_FN(_write)
+        h, err = _P(), _Err()
+        _raise(lib().frt_bgzf_writer_open(self._cb, None, compressor._h, C.byref(h), C.byref(err)), err)
+        self._h = h
+        if chunks_per_batch is not None:
+            lib().frt_bgzf_writer_set_chunks_per_batch(h, chunks_per_batch)
+        if payload_size is not None:
+            lib().frt_bgzf_writer_set_payload_size(h, payload_size)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.frt_bgzf_writer_destroy(h)
+            self._h = None
+
+    def write_batch(self, data_ptr: int, data_len: int, bounds) -> None:
+        b = np.ascontiguousarray(bounds, dtype=np.uint64)
+        err = _Err()
+        _raise(lib().frt_bgzf_writer_write_batch(self._h, data_ptr, data_len, b.ctypes.data if b.size else None,
+                                                 b.size, C.byref(err)), err)
+
+    def write_device(self, data_ptr: int, data_len: int) -> None:
+        err = _Err()
+        _raise(lib().frt_bgzf_writer_write_device(self._h, data_ptr, data_len, C.byref(err)), err)
+
+    def finish(self) -> None:
+        err = _Err()
+        _raise(lib().frt_bgzf_writer_finish(self._h, C.byref(err)), err)
+
+    def stats(self) -> dict:
+        v = [C.c_uint64() for _ in range(4)]
+        lib().frt_bgzf_writer_stats(self._h, *[C.byref(x) for x in v])
+        return dict(zip(("blocks", "batches", "compressed_bytes", "uncompressed_bytes"), (x.value for x in v)))
 
 
 def parse_bcf_header(data):

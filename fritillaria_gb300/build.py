@@ -24,7 +24,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
                      f"-I{INCLUDE}", "-diag-suppress", "550"]
 
 CUDA_SOURCES = ["inflate.cu", "bam.cu", "runtime.cu", "decoder.cu", "engine.cu", "formats.cu", "noalloc.cu", "bai.cpp", "tune.cpp", "fields.cu",
-                "serve.cu"]
+                "serve.cu", "deflate.cu"]
 LIB = PKG / "libfrt_gb300.so"
 SYNTH_LIB = PKG / "libfrt_synth.so"
 

@@ -730,6 +730,60 @@ int frt_engine_time_stages(frt_engine *e, float *ms, int repeats, frt_error *err
 /* Kernel launches per run (kernel nodes of the captured graph). */
 uint64_t frt_engine_launches(const frt_engine *e);
 
+/* ---- the write side: BGZF compression of device bytes ----------------------
+ * DeviceBlockCompressor (crates/fritillaria-core/src/device.rs:326-372) and
+ * DeviceBgzfWriter (crates/fritillaria-bgzf/src/device_write.rs).  The
+ * reference compresses with nvCOMP; this library uses its own device deflate
+ * (greedy LZ77 over a 32 KiB window, fixed Huffman codes).  Contract, as
+ * there: one framed block per chunk, chunks of at most 65,505 bytes
+ * (MAX_COMPRESSIBLE_PAYLOAD), no EOF block in a batch, and inflating the output
+ * gives back the input block for block -- not byte identity with any other
+ * compressor.  The framing of each block is chosen by choose_framing
+ * (crates/fritillaria-core/src/compress.rs:115-128). */
+typedef struct frt_compressor frt_compressor;
+typedef struct frt_bgzf_writer frt_bgzf_writer;
+/* A byte sink: returns the bytes it took (> 0), or <= 0 on error. */
+typedef int64_t (*frt_write_fn)(void *ctx, const uint8_t *buf, size_t len);
+
+int frt_compressor_create(int device, void *stream, frt_compressor **out, frt_error *err);
+void frt_compressor_destroy(frt_compressor *c);
+const char *frt_compressor_name(const frt_compressor *c);
+int frt_compressor_device_ordinal(const frt_compressor *c);
+/* choose_framing: 0 deflated, 1 stored, 2 the empty block; framed_size
+ * (compress.rs:134-142): header + body + trailer bytes of that choice. */
+int frt_choose_framing(size_t payload_len, size_t deflate_len);
+size_t frt_framed_size(size_t payload_len, size_t deflate_len);
+/* Bytes that always hold the framed blocks of n chunks (64 KiB each). */
+size_t frt_compress_bound(size_t n_chunks);
+/* compress_batch_device: each range bounds[i]..bounds[i + 1] (n_bounds - 1
+ * ranges, rising, within data_len, at most 65,505 bytes) of the device bytes
+ * becomes one block; the blocks go to host `out` back to back, block i at
+ * out_offsets[i]..out_offsets[i + 1]; *out_len = their total.  The ranges
+ * need not cover the buffer.  A bad range is FRT_ERR_MALFORMED. */
+int frt_compress_batch_device(frt_compressor *c, const uint8_t *data, size_t data_len, const uint64_t *bounds,
+                              size_t n_bounds, uint8_t *out, size_t out_cap, uint64_t *out_offsets, size_t *out_len,
+                              frt_error *err);
+
+/* DeviceBgzfWriter::new(inner, compressor): blocks go to `write`.  The
+ * compressor must outlive the writer. */
+int frt_bgzf_writer_open(frt_write_fn write, void *ctx, frt_compressor *c, frt_bgzf_writer **out, frt_error *err);
+/* with_chunks_per_batch (at least 1; 1024 by default) and with_payload_size
+ * (clamped to 1..65,505; 65,280 by default, DEFAULT_PAYLOAD_SIZE). */
+void frt_bgzf_writer_set_chunks_per_batch(frt_bgzf_writer *w, size_t chunks);
+void frt_bgzf_writer_set_payload_size(frt_bgzf_writer *w, size_t size);
+/* write_batch (device_write.rs:106-141): the chunks bounds[i]..bounds[i + 1]
+ * of the device bytes; bounds must hold at least one entry and end within
+ * `len` (else FRT_ERR_MALFORMED). */
+int frt_bgzf_writer_write_batch(frt_bgzf_writer *w, const uint8_t *data, size_t len, const uint64_t *bounds,
+                                size_t n_bounds, frt_error *err);
+/* The device bytes cut into payload-size chunks. */
+int frt_bgzf_writer_write_device(frt_bgzf_writer *w, const uint8_t *data, size_t len, frt_error *err);
+/* Appends the 28-byte EOF block (crates/fritillaria-bgzf/src/block.rs:40-43), once. */
+int frt_bgzf_writer_finish(frt_bgzf_writer *w, frt_error *err);
+void frt_bgzf_writer_stats(const frt_bgzf_writer *w, uint64_t *blocks, uint64_t *batches, uint64_t *compressed,
+                           uint64_t *uncompressed);
+void frt_bgzf_writer_destroy(frt_bgzf_writer *w);
+
 #ifdef __cplusplus
 }
 #endif
