@@ -96,6 +96,7 @@ def parse_args():
     p.add_argument("--no-plain", action="store_true", help="skip the per-batch comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--no-fields", action="store_true", help="skip timing the record-field kernels")
+    p.add_argument("--no-write", action="store_true", help="skip timing the BGZF compressor")
     p.add_argument("--tuning-cache", default=str(TUNING_CACHE),
                    help="JSON cache of inflate tunings (read, and written on a miss)")
     p.add_argument("--retune", action="store_true", help="time the inflate tunings again even on a cache hit")
@@ -375,6 +376,59 @@ def record_fields(eng, records: int, peak: float) -> dict:
     return out
 
 
+def write_side(frt, eng, bgzf, no_cpu: bool) -> dict:
+    """The write side over the engine's inflated bytes: DeviceCompressor
+    (the reference's DeviceBlockCompressor contract) in 65,280-byte chunks,
+    16,384 chunks a call into pinned host memory, wall time of the calls; and
+    zlib on the host cores over a sample of the same chunks."""
+    import concurrent.futures
+    import zlib
+
+    import numpy as np
+    import torch
+
+    ptr, n = eng.inflated_ptr()
+    comp = frt.DeviceCompressor(0)
+    bounds = np.append(np.arange(0, n, frt.DEFAULT_PAYLOAD_SIZE, dtype=np.uint64), np.uint64(n))
+    per = 16384
+    pinned = torch.empty(per * 65536, dtype=torch.uint8).pin_memory().numpy()
+    comp.compress_batch_device(ptr, n, bounds[:1025], out=pinned)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    total = 0
+    for s0 in range(0, len(bounds) - 1, per):
+        total += comp.compress_batch_device(ptr, n, bounds[s0:s0 + per + 1], out=pinned).byte_len()
+    secs = time.perf_counter() - t0
+    out = {"input_bytes": int(n), "output_bytes": int(total), "ratio": round(n / total, 3), "ms": round(1e3 * secs, 2),
+           "gbs": round(n / secs / 1e9, 2), "blocks": int(len(bounds) - 1),
+           "form": "DeviceCompressor.compress_batch_device over the engine's inflated bytes, 65,280-byte chunks, "
+                   "16,384 chunks a call, framed blocks copied to pinned host memory, wall time"}
+    if not no_cpu:
+        # the same bytes on the host: the file's first members, inflated by zlib
+        spans, _ = frt.discover_blocks(bgzf[: 600 * 65536])
+        parts, size = [], 0
+        for sp in spans:
+            a = int(sp["payload_start"])
+            parts.append(zlib.decompress(bytes(bgzf[a:a + int(sp["payload_len"])]), -15))
+            size += len(parts[-1])
+            if size >= 512 * 65280:
+                break
+        host = np.frombuffer(b"".join(parts), np.uint8)[: 512 * 65280]
+        chunks = [host[i:i + 65280].tobytes() for i in range(0, host.size, 65280)]
+        threads = os.cpu_count() or 1
+        res = {}
+        for level in (1, 6):
+            with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+                t0 = time.perf_counter()
+                sizes = list(ex.map(lambda c: len(zlib.compress(c, level)), chunks))
+                dt = time.perf_counter() - t0
+            res[f"zlib{level}"] = {"gbs": round(host.size / dt / 1e9, 3), "ratio": round(host.size / sum(sizes), 3)}
+        out["cpu_baseline"] = {"kind": "port", "cores": threads, "levels": res,
+                               "sample": f"{len(chunks)} chunks of 65,280 bytes of the same inflated BAM, zlib "
+                                         f"(Python's, releasing the GIL) on a pool of {threads} threads"}
+    return out
+
+
 def run_ours(args, rank, world, local):
     import numpy as np
     import torch
@@ -471,6 +525,7 @@ def run_ours(args, rank, world, local):
            "d2h_bytes_per_step": 128, "ms_per_step": round(1e3 * e2e_s, 3), "step_ms": steps_ms}
 
     fields = record_fields(eng, st.records, peak) if rank == 0 and not args.no_fields else None
+    write = write_side(frt, eng, bgzf, args.no_cpu) if rank == 0 and not args.no_write else None
 
     plain = None
     if not args.no_plain:
@@ -503,6 +558,7 @@ def run_ours(args, rank, world, local):
             "e2e": e2e,
             "plain": plain,
             "record_fields": fields,
+            "write_side": write,
             "gpu_launches": eng.launches_per_run() * args.steps,
             "clocks": clocks.summary(),
             "wall_s": round(wall, 3),

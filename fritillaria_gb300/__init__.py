@@ -1073,15 +1073,20 @@ class DeviceCompressor:
     def device_ordinal(self) -> int:
         return lib().frt_compressor_device_ordinal(self._h)
 
-    def compress_batch_device(self, data_ptr: int, data_len: int, bounds) -> CompressedBatch:
+    def compress_batch_device(self, data_ptr: int, data_len: int, bounds, out: np.ndarray | None = None
+                              ) -> CompressedBatch:
+        """The blocks of bounds[i]..bounds[i + 1]; into `out` (a uint8 host
+        array, pinned for a fast copy back) when given, as a view of it."""
         b = np.ascontiguousarray(bounds, dtype=np.uint64)
         n = max(0, b.size - 1)
-        out = np.empty(max(1, lib().frt_compress_bound(n)), np.uint8)
+        own = out is None
+        if own:
+            out = np.empty(max(1, lib().frt_compress_bound(n)), np.uint8)
         offs = np.zeros(n + 1, np.uint64)
         got, err = C.c_size_t(), _Err()
         _raise(lib().frt_compress_batch_device(self._h, data_ptr, data_len, b.ctypes.data, b.size, out.ctypes.data,
                                                out.size, offs.ctypes.data, C.byref(got), C.byref(err)), err)
-        return CompressedBatch(out[:got.value].copy(), offs)
+        return CompressedBatch(out[:got.value].copy() if own else out[:got.value], offs)
 
 
 _WRITE_FN = C.CFUNCTYPE(C.c_int64, C.c_void_p, C.c_void_p, C.c_size_t)

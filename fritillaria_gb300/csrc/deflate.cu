@@ -19,9 +19,12 @@
 //     the next 32 positions, the first lane whose candidate matches ends a run
 //     of literals, the warp extends that match 32 bytes a compare, and every
 //     position passed is entered in the table (atomicMax: the latest wins);
-//   * fixed Huffman codes (RFC 1951 3.2.6) in one final block, the lanes'
-//     codes packed into a shared-memory ring of words with a warp scan of
-//     their bit lengths and flushed to the chunk's slot 64 words at a time.
+//   * the parse runs twice, identically: first counting its symbols, from
+//     which lane 0 builds length-limited Huffman codes (RFC 1951 3.2.7) and
+//     keeps them when they beat the fixed codes (3.2.6) header included; then
+//     emitting one final block with the winner, the lanes' codes packed into
+//     a shared-memory ring of words with a warp scan of their bit lengths and
+//     flushed to the chunk's slot 64 words at a time.
 // A stream longer than a BGZF block can carry stops early; the host then
 // stores the chunk, as choose_framing does.
 
@@ -66,9 +69,18 @@ constexpr ByteCrc make_byte_crc()
 __device__ const ByteCrc g_bcrc = make_byte_crc();
 
 struct WarpState {
-    u32 table[1u << kHashBits]; // position + 1 of the latest occurrence of each prefix hash, 0 none
+    // the hash table: the last position + 1 of each prefix hash (0 none);
+    // between the passes, the Huffman builder's scratch
+    u32 table[1u << kHashBits];
     u32 ring[kRing];
+    u32 lf[286], df[30]; // literal/length and distance symbol counts of the parse
+    u16 lcode[286], dcode[30], ccode[19]; // codes, reversed as they are packed
+    u8 llen[286], dlen[30], clen[19];
+    u16 items[320]; // the code lengths, run-length coded: symbol | extra value << 5
+    u32 cf[19];     // counts of the code-length code's symbols
+    u32 n_items, hlit, hdist, hclen, dynamic;
 };
+static_assert(sizeof(u32) * (1u << kHashBits) >= 4u * (512 + 1024) + 2u * 1024, "the builder's scratch fits");
 
 __device__ __forceinline__ u32 prefix_hash(u32 b0, u32 b1, u32 b2)
 {
@@ -78,7 +90,7 @@ __device__ __forceinline__ u32 prefix_hash(u32 b0, u32 b1, u32 b2)
 // A Huffman code as it is packed: the code reversed (deflate sends Huffman
 // codes most significant bit first into a stream filled from the least
 // significant bit), in the low bits.
-__device__ __forceinline__ u32 rev(u32 code, u32 len) { return __brev(code) >> (32u - len); }
+__device__ __forceinline__ u32 rev(u32 code, u32 len) { return len ? __brev(code) >> (32u - len) : 0u; }
 
 // Fixed literal/length code of symbol s (RFC 1951 3.2.6): (packed bits, length).
 __device__ __forceinline__ void fixed_lit(u32 s, u32 *v, u32 *n)
@@ -89,49 +101,37 @@ __device__ __forceinline__ void fixed_lit(u32 s, u32 *v, u32 *n)
     else *v = rev(0xC0u + (s - 280u), 8), *n = 8;
 }
 
-// A match of length L (3..258) at distance d (1..32768) as one packed group:
-// length code, its extra bits, distance code (5 fixed bits), its extra bits
-// (RFC 1951 3.2.5), at most 8 + 5 + 5 + 13 = 31 bits.
-__device__ __forceinline__ void match_code(u32 L, u32 d, u32 *v, u32 *n)
+// The length symbol of a match length (3..258) with its extra bits (RFC 1951 3.2.5).
+__device__ __forceinline__ void len_sym(u32 L, u32 *sym, u32 *ex, u32 *nb)
 {
-    u32 sym, lex = 0, lnb = 0;
     if (L == 258) {
-        sym = 285;
+        *sym = 285, *ex = 0, *nb = 0;
     } else if (L <= 10) {
-        sym = 254u + L;
+        *sym = 254u + L, *ex = 0, *nb = 0;
     } else {
-        const u32 x = L - 3u, k = 31u - __clz(x); // x >= 8: k >= 3
-        const u32 hi = (x >> (k - 2u)) & 3u;
-        sym = 257u + 4u * (k - 1u) + hi;
-        lnb = k - 2u;
-        lex = L - (3u + ((4u | hi) << lnb));
+        const u32 x = L - 3u, k = 31u - __clz(x), hi = (x >> (k - 2u)) & 3u;
+        *sym = 257u + 4u * (k - 1u) + hi;
+        *nb = k - 2u;
+        *ex = L - (3u + ((4u | hi) << (k - 2u)));
     }
-    u32 lv, ln;
-    fixed_lit(sym, &lv, &ln);
-    u32 dsym, dex = 0, dnb = 0;
-    const u32 y = d - 1u;
-    if (y < 4u) {
-        dsym = y;
-    } else {
-        const u32 k = 31u - __clz(y); // >= 2
-        const u32 hi = (y >> (k - 1u)) & 1u;
-        dsym = 2u * k + hi;
-        dnb = k - 1u;
-        dex = d - (1u + ((2u | hi) << dnb));
-    }
-    u32 v0 = lv, n0 = ln;
-    v0 |= lex << n0;
-    n0 += lnb;
-    v0 |= rev(dsym, 5) << n0;
-    n0 += 5;
-    v0 |= dex << n0;
-    n0 += dnb;
-    *v = v0;
-    *n = n0;
 }
 
-// Adds each lane's (v, n) at bit `bitpos` + the bits of the lanes below it;
-// returns the new bit position (warp-uniform).
+// The distance symbol of a distance (1..32768) with its extra bits.
+__device__ __forceinline__ void dist_sym(u32 d, u32 *sym, u32 *ex, u32 *nb)
+{
+    const u32 y = d - 1u;
+    if (y < 4u) {
+        *sym = y, *ex = 0, *nb = 0;
+    } else {
+        const u32 k = 31u - __clz(y), hi = (y >> (k - 1u)) & 1u;
+        *sym = 2u * k + hi;
+        *nb = k - 1u;
+        *ex = d - (1u + ((2u | hi) << (k - 1u)));
+    }
+}
+
+// Adds each lane's (v, n), n <= 31, at bit `bitpos` + the bits of the lanes
+// below it; returns the new bit position (warp-uniform).
 __device__ __forceinline__ u32 pack(WarpState *ws, u32 bitpos, u32 v, u32 n, u32 lane)
 {
     u32 x = n;
@@ -162,6 +162,278 @@ __device__ __forceinline__ void flush(WarpState *ws, u32 *slot, u32 from, u32 to
 
 __device__ __forceinline__ u32 byte_at(const u8 *p, u32 i, u32 len) { return i < len ? p[i] : 0u; }
 
+enum PassMode { COUNT = 0, EMIT_FIXED = 1, EMIT_DYNAMIC = 2 };
+
+// One pass of the greedy parse over the chunk (the same parse every time: the
+// table starts empty and atomicMax makes its contents order-free).  COUNT
+// tallies the symbols; the EMIT modes pack their codes, a match as two groups
+// (length, distance) of at most 20 and 28 bits.  Returns false when the
+// stream outgrows a BGZF block.
+template <int MODE>
+__device__ bool lz_pass(WarpState *ws, const u8 *p, u32 len, u32 lane, u32 *slot, u32 &bitpos, u32 &flushed)
+{
+    for (u32 i = lane; i < (1u << kHashBits); i += 32u) ws->table[i] = 0;
+    __syncwarp();
+    u32 pos = 0;
+    while (pos < len) {
+        const u32 q = pos + lane;
+        const u32 b0 = byte_at(p, q, len), b1 = byte_at(p, q + 1u, len), b2 = byte_at(p, q + 2u, len);
+        const bool has3 = q + 3u <= len;
+        const u32 h = prefix_hash(b0, b1, b2);
+        const u32 e = has3 ? ws->table[h] : 0u;
+        bool ok = false;
+        u32 c = 0;
+        if (e) {
+            c = e - 1u;
+            ok = q - c <= kWindow && p[c] == b0 && p[c + 1u] == b1 && p[c + 2u] == b2;
+        }
+        const u32 hits = __ballot_sync(FRT_FULL_MASK, ok);
+        const u32 k = hits ? (u32)__ffs(hits) - 1u : 32u;
+        const u32 nlit = min(k, len - pos);
+        u32 L = 0, dist = 0;
+        if (k < 32u) {
+            const u32 m = pos + k, cm = __shfl_sync(FRT_FULL_MASK, c, k);
+            const u32 cap = min(258u, len - m);
+            L = 3u;
+            while (L < cap) {
+                const u32 i = L + lane;
+                const bool diff = i >= cap || p[cm + i] != p[m + i];
+                const u32 db = __ballot_sync(FRT_FULL_MASK, diff);
+                if (db) {
+                    L += (u32)__ffs(db) - 1u;
+                    break;
+                }
+                L += 32u;
+            }
+            L = min(L, cap);
+            dist = m - cm;
+        }
+        u32 ls = 0, lex = 0, lnb = 0, ds = 0, dex = 0, dnb = 0;
+        if (lane == k && L) {
+            len_sym(L, &ls, &lex, &lnb);
+            dist_sym(dist, &ds, &dex, &dnb);
+        }
+        if (MODE == COUNT) {
+            if (lane < nlit) atomicAdd(&ws->lf[b0], 1u);
+            if (lane == k && L) {
+                atomicAdd(&ws->lf[ls], 1u);
+                atomicAdd(&ws->df[ds], 1u);
+            }
+        } else {
+            u32 v = 0, nb = 0, v2 = 0, nb2 = 0;
+            if (lane < nlit) {
+                if (MODE == EMIT_FIXED) fixed_lit(b0, &v, &nb);
+                else v = ws->lcode[b0], nb = ws->llen[b0];
+            } else if (lane == k && L) {
+                if (MODE == EMIT_FIXED) {
+                    fixed_lit(ls, &v, &nb);
+                    v2 = rev(ds, 5), nb2 = 5;
+                } else {
+                    v = ws->lcode[ls], nb = ws->llen[ls];
+                    v2 = ws->dcode[ds], nb2 = ws->dlen[ds];
+                }
+                v |= lex << nb;
+                nb += lnb;
+                v2 |= dex << nb2;
+                nb2 += dnb;
+            }
+            bitpos = pack(ws, bitpos, v, nb, lane);
+            if (k < 32u && L) bitpos = pack(ws, bitpos, v2, nb2, lane);
+        }
+        if (lane < nlit && has3) atomicMax(&ws->table[h], q + 1u);
+        const u32 adv = nlit + L;
+        for (u32 j = nlit + lane; j < adv; j += 32u) {
+            const u32 r = pos + j;
+            if (r + 3u <= len) atomicMax(&ws->table[prefix_hash(p[r], p[r + 1u], p[r + 2u])], r + 1u);
+        }
+        __syncwarp();
+        pos += adv;
+        if (MODE != COUNT) {
+            if ((bitpos >> 3) > kMaxDeflate) return false;
+            const u32 done = bitpos >> 5;
+            if (done - flushed >= kFlush) {
+                flush(ws, slot, flushed, flushed + kFlush, lane);
+                flushed += kFlush;
+            }
+        }
+    }
+    return true;
+}
+
+// Code lengths of a Huffman code for freq[0, n), at most maxlen bits: the
+// used symbols (at least two; the lowest unused ones get a count of 1) sorted
+// by (count, symbol) with a warp bitonic sort, a two-queue Huffman merge,
+// the lengths past maxlen folded in by the Kraft sum (each excess leaf moves
+// one shorter code a level down), and the shortest codes to the most frequent
+// symbols.  Scratch: keys[512], wt[1024], parent[1024] (u16).
+__device__ void huff_lengths(u32 *freq, u32 n, u32 maxlen, u8 *lens, u32 *keys, u32 *wt, u16 *parent, u32 lane)
+{
+    if (lane == 0) {
+        u32 used = 0;
+        for (u32 s = 0; s < n; ++s) used += freq[s] ? 1u : 0u;
+        for (u32 s = 0; s < n && used < 2u; ++s)
+            if (!freq[s]) freq[s] = 1u, ++used;
+    }
+    __syncwarp();
+    for (u32 i = lane; i < 512u; i += 32u) keys[i] = i < n && freq[i] ? (freq[i] << 9) | i : 0xffffffffu;
+    for (u32 i = lane; i < n; i += 32u) lens[i] = 0;
+    __syncwarp();
+    for (u32 size = 2; size <= 512u; size <<= 1)
+        for (u32 stride = size >> 1; stride; stride >>= 1) {
+            for (u32 t = lane; t < 256u; t += 32u) {
+                const u32 i = 2u * t - (t & (stride - 1u)), j = i + stride;
+                const bool up = (i & size) == 0;
+                const u32 a = keys[i], b = keys[j];
+                if ((a > b) == up) keys[i] = b, keys[j] = a;
+            }
+            __syncwarp();
+        }
+    if (lane == 0) {
+        u32 m = 0;
+        while (m < 512u && keys[m] != 0xffffffffu) ++m;
+        for (u32 i = 0; i < m; ++i) wt[i] = keys[i] >> 9;
+        u32 li = 0, ii = m, nxt = m;
+        while (nxt < 2u * m - 1u) {
+            u32 pick[2];
+            for (int t = 0; t < 2; ++t) {
+                if (li < m && (ii >= nxt || wt[li] <= wt[ii])) pick[t] = li++;
+                else pick[t] = ii++;
+            }
+            wt[nxt] = wt[pick[0]] + wt[pick[1]];
+            parent[pick[0]] = parent[pick[1]] = (u16)nxt;
+            ++nxt;
+        }
+        // depths, root first; wt[] now holds them
+        wt[2u * m - 2u] = 0;
+        for (int i = (int)(2u * m) - 3; i >= 0; --i) wt[i] = wt[parent[i]] + 1u;
+        u32 cnt[16] = {};
+        for (u32 i = 0; i < m; ++i) ++cnt[min(wt[i], maxlen)];
+        u32 total = 0;
+        for (u32 L = 1; L <= maxlen; ++L) total += cnt[L] << (maxlen - L);
+        while (total > (1u << maxlen)) {
+            --cnt[maxlen];
+            for (u32 L = maxlen - 1u; L > 0; --L)
+                if (cnt[L]) {
+                    --cnt[L];
+                    cnt[L + 1u] += 2u;
+                    break;
+                }
+            --total;
+        }
+        u32 k = m; // keys[m - 1] is the most frequent
+        for (u32 L = 1; L <= maxlen; ++L)
+            for (u32 c = 0; c < cnt[L]; ++c) lens[keys[--k] & 511u] = (u8)L;
+    }
+    __syncwarp();
+}
+
+// Canonical codes of lens[0, n) (RFC 1951 3.2.2), reversed for packing.
+__device__ void canonical(const u8 *lens, u32 n, u16 *codes)
+{
+    u32 bl[16] = {}, next[16];
+    for (u32 s = 0; s < n; ++s) ++bl[lens[s]];
+    bl[0] = 0;
+    u32 code = 0;
+    for (u32 b = 1; b < 16; ++b) {
+        code = (code + bl[b - 1]) << 1;
+        next[b] = code;
+    }
+    for (u32 s = 0; s < n; ++s)
+        if (lens[s]) codes[s] = (u16)rev(next[lens[s]]++, lens[s]);
+}
+
+__device__ const u8 kClOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+
+__device__ __forceinline__ u32 fixed_len(u32 s) { return s < 144 ? 8u : s < 256 ? 9u : s < 280 ? 7u : 8u; }
+__device__ __forceinline__ u32 cl_extra(u32 sym) { return sym == 16 ? 2u : sym == 17 ? 3u : sym == 18 ? 7u : 0u; }
+
+// The dynamic trees from the counts (lf[256] counts the end of block), and
+// whether they beat the fixed codes, their header included (the extra bits
+// of lengths and distances are the same either way).
+__device__ void build_trees(WarpState *ws, u32 lane)
+{
+    u32 *keys = ws->table, *wt = ws->table + 512;
+    u16 *parent = (u16 *)(ws->table + 1536);
+    huff_lengths(ws->lf, 286, 15, ws->llen, keys, wt, parent, lane);
+    huff_lengths(ws->df, 30, 15, ws->dlen, keys, wt, parent, lane);
+    if (lane == 0) {
+        u32 hlit = 286;
+        while (hlit > 257 && !ws->llen[hlit - 1]) --hlit;
+        u32 hdist = 30;
+        while (hdist > 1 && !ws->dlen[hdist - 1]) --hdist;
+        // run-length code the lengths (RFC 1951 3.2.7): 16 repeats the previous
+        // length 3-6 times, 17 and 18 are runs of 3-10 and 11-138 zeros
+        const u32 total = hlit + hdist;
+        u32 n = 0, i = 0;
+        while (i < total) {
+            const u32 v = i < hlit ? ws->llen[i] : ws->dlen[i - hlit];
+            u32 j = i;
+            while (j < total && (j < hlit ? ws->llen[j] : ws->dlen[j - hlit]) == v) ++j;
+            u32 run = j - i;
+            if (v == 0) {
+                while (run >= 11) {
+                    const u32 r = min(run, 138u);
+                    ws->items[n++] = (u16)(18u | ((r - 11u) << 5));
+                    run -= r;
+                }
+                if (run >= 3) {
+                    ws->items[n++] = (u16)(17u | ((run - 3u) << 5));
+                    run = 0;
+                }
+                while (run--) ws->items[n++] = 0;
+            } else {
+                ws->items[n++] = (u16)v;
+                --run;
+                while (run >= 3) {
+                    const u32 r = min(run, 6u);
+                    ws->items[n++] = (u16)(16u | ((r - 3u) << 5));
+                    run -= r;
+                }
+                while (run--) ws->items[n++] = (u16)v;
+            }
+            i = j;
+        }
+        ws->n_items = n;
+        ws->hlit = hlit;
+        ws->hdist = hdist;
+        for (u32 t = 0; t < 19; ++t) ws->cf[t] = 0;
+        for (u32 t = 0; t < n; ++t) ++ws->cf[ws->items[t] & 31u];
+    }
+    __syncwarp();
+    huff_lengths(ws->cf, 19, 7, ws->clen, keys, wt, parent, lane);
+    if (lane == 0) {
+        u32 hclen = 19;
+        while (hclen > 4 && !ws->clen[kClOrder[hclen - 1]]) --hclen;
+        ws->hclen = hclen;
+        canonical(ws->llen, 286, ws->lcode);
+        canonical(ws->dlen, 30, ws->dcode);
+        canonical(ws->clen, 19, ws->ccode);
+        u64 dyn = 17u + 3u * hclen, fix = 3;
+        for (u32 t = 0; t < ws->n_items; ++t) {
+            const u32 sym = ws->items[t] & 31u;
+            dyn += ws->clen[sym] + cl_extra(sym);
+        }
+        for (u32 sy = 0; sy < 286; ++sy) {
+            dyn += (u64)ws->lf[sy] * ws->llen[sy];
+            fix += (u64)ws->lf[sy] * fixed_len(sy);
+        }
+        for (u32 d = 0; d < 30; ++d) {
+            dyn += (u64)ws->df[d] * ws->dlen[d];
+            fix += (u64)ws->df[d] * 5u;
+        }
+        ws->dynamic = dyn < fix ? 1u : 0u;
+    }
+    __syncwarp();
+}
+
+__device__ __forceinline__ void flush_some(WarpState *ws, u32 *slot, u32 bitpos, u32 &flushed, u32 lane)
+{
+    if ((bitpos >> 5) - flushed >= kFlush) {
+        flush(ws, slot, flushed, flushed + kFlush, lane);
+        flushed += kFlush;
+    }
+}
+
 __global__ void __launch_bounds__(32 * kWarpsPerCta) k_deflate_chunks(const u8 *data, const u64 *bounds, u32 n,
                                                                       u8 *slots, u32 *deflate_len, u32 *crcs)
 {
@@ -187,79 +459,46 @@ __global__ void __launch_bounds__(32 * kWarpsPerCta) k_deflate_chunks(const u8 *
         if (lane == 0) deflate_len[chunk] = 0;
         return;
     }
-
-    for (u32 i = lane; i < (1u << kHashBits); i += 32u) ws->table[i] = 0;
     for (u32 i = lane; i < kRing; i += 32u) ws->ring[i] = 0;
+    for (u32 i = lane; i < 286u; i += 32u) ws->lf[i] = 0;
+    if (lane < 30u) ws->df[lane] = 0;
     __syncwarp();
     u32 *slot = (u32 *)(slots + (size_t)chunk * kSlot);
-    u32 bitpos = pack(ws, 0, 3u, lane == 0 ? 3u : 0u, lane); // BFINAL 1, BTYPE 01 (fixed codes)
-    u32 flushed = 0; // ring words already in the slot
-    u32 pos = 0;
-    bool too_big = false;
-    while (pos < len) {
-        // candidates for positions pos + lane
-        const u32 q = pos + lane;
-        const u32 b0 = byte_at(p, q, len), b1 = byte_at(p, q + 1u, len), b2 = byte_at(p, q + 2u, len);
-        const bool has3 = q + 3u <= len;
-        const u32 h = prefix_hash(b0, b1, b2);
-        const u32 e = has3 ? ws->table[h] : 0u;
-        bool ok = false;
-        u32 c = 0;
-        if (e) {
-            c = e - 1u;
-            ok = q - c <= kWindow && p[c] == b0 && p[c + 1u] == b1 && p[c + 2u] == b2;
-        }
-        const u32 hits = __ballot_sync(FRT_FULL_MASK, ok);
-        const u32 k = hits ? (u32)__ffs(hits) - 1u : 32u;
-        const u32 nlit = min(k, len - pos);
-        // the match, if one ends the run: extend it 32 bytes a compare
-        u32 L = 0, dist = 0;
-        if (k < 32u) {
-            const u32 m = pos + k, cm = __shfl_sync(FRT_FULL_MASK, c, k);
-            const u32 cap = min(258u, len - m);
-            L = 3u;
-            while (L < cap) {
-                const u32 i = L + lane;
-                const bool diff = i >= cap || p[cm + i] != p[m + i];
-                const u32 db = __ballot_sync(FRT_FULL_MASK, diff);
-                if (db) {
-                    L += (u32)__ffs(db) - 1u;
-                    break;
-                }
-                L += 32u;
+    u32 bitpos = 0, flushed = 0;
+    lz_pass<COUNT>(ws, p, len, lane, slot, bitpos, flushed); // the counts only
+    if (lane == 0) ws->lf[256] += 1u;                          // the end of block
+    __syncwarp();
+    build_trees(ws, lane);
+    const bool dyn = ws->dynamic != 0;
+    bitpos = 0;
+    if (!dyn) {
+        bitpos = pack(ws, 0, 3u, lane == 0 ? 3u : 0u, lane); // BFINAL 1, BTYPE 01
+    } else {
+        // BFINAL 1, BTYPE 10, HLIT, HDIST, HCLEN; the code-length code's lengths
+        // in their permuted order; the run-length coded lengths
+        const u32 h = 1u | (2u << 1) | ((ws->hlit - 257u) << 3) | ((ws->hdist - 1u) << 8) | ((ws->hclen - 4u) << 13);
+        bitpos = pack(ws, 0, lane == 0 ? h : 0u, lane == 0 ? 17u : 0u, lane);
+        bitpos = pack(ws, bitpos, lane < ws->hclen ? ws->clen[kClOrder[lane]] : 0u, lane < ws->hclen ? 3u : 0u, lane);
+        for (u32 base = 0; base < ws->n_items; base += 32u) {
+            const u32 i = base + lane;
+            u32 v = 0, nb = 0;
+            if (i < ws->n_items) {
+                const u32 it = ws->items[i], sym = it & 31u;
+                v = ws->ccode[sym] | ((it >> 5) << ws->clen[sym]);
+                nb = ws->clen[sym] + cl_extra(sym);
             }
-            L = min(L, cap);
-            dist = m - cm;
-        }
-        // codes: lanes below k their literal, lane k the match
-        u32 v = 0, nb = 0;
-        if (lane < nlit) fixed_lit(b0, &v, &nb);
-        else if (lane == k && L) match_code(L, dist, &v, &nb);
-        bitpos = pack(ws, bitpos, v, nb, lane);
-        // enter the positions passed: the literals', then the match's
-        if (lane < nlit && has3) atomicMax(&ws->table[h], q + 1u);
-        const u32 adv = nlit + L;
-        for (u32 j = nlit + lane; j < adv; j += 32u) {
-            const u32 r = pos + j;
-            if (r + 3u <= len) atomicMax(&ws->table[prefix_hash(p[r], p[r + 1u], p[r + 2u])], r + 1u);
-        }
-        __syncwarp();
-        pos += adv;
-        if ((bitpos >> 3) > kMaxDeflate) {
-            too_big = true;
-            break;
-        }
-        const u32 done = bitpos >> 5;
-        if (done - flushed >= kFlush) {
-            flush(ws, slot, flushed, flushed + kFlush, lane);
-            flushed += kFlush;
+            bitpos = pack(ws, bitpos, v, nb, lane);
+            flush_some(ws, slot, bitpos, flushed, lane);
         }
     }
-    if (!too_big) {
-        bitpos = pack(ws, bitpos, 0u, lane == 0 ? 7u : 0u, lane); // end of block: symbol 256, 7 zero bits
-        too_big = ((bitpos + 7u) >> 3) > kMaxDeflate;
+    bool ok = dyn ? lz_pass<EMIT_DYNAMIC>(ws, p, len, lane, slot, bitpos, flushed)
+                  : lz_pass<EMIT_FIXED>(ws, p, len, lane, slot, bitpos, flushed);
+    if (ok) {
+        const u32 v = dyn ? ws->lcode[256] : 0u, nb = dyn ? ws->llen[256] : 7u; // the end of block
+        bitpos = pack(ws, bitpos, lane == 0 ? v : 0u, lane == 0 ? nb : 0u, lane);
+        ok = ((bitpos + 7u) >> 3) <= kMaxDeflate;
     }
-    if (too_big) {
+    if (!ok) {
         if (lane == 0) deflate_len[chunk] = kTooBig;
         return;
     }
