@@ -1,5 +1,5 @@
 """TEST INFRASTRUCTURE ONLY.  A restatement of the reference's BAI region
-resolution and region filter, the checker for the library's BAI query and
+resolution and region filter, the oracle for the library's BAI query and
 its region-serving path:
 
   * parse: the BAI layout (SAM specification 5.2; crates/fritillaria-bam/src/

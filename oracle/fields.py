@@ -1,4 +1,4 @@
-"""Record fields, restated on the CPU -- test infrastructure: the checker for
+"""Record fields, restated on the CPU -- test infrastructure: the oracle for
 the device record-field kernels, never called by the product.
 
 Follows the reference's host accessors for one BAM record:

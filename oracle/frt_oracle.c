@@ -3,7 +3,7 @@
  *
  * A CPU restatement of the reference's algorithm for the BGZF -> device
  * columns path.  Each function names the reference file:line it follows.
- * Nothing in the product path calls this file; it is the checker.
+ * Nothing in the product path calls this file; it is the oracle the tests compare against.
  */
 #define _GNU_SOURCE
 #include "frt_oracle.h"

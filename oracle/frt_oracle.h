@@ -2,7 +2,7 @@
  * TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of the reference's CPU path for BGZF -> inflate ->
- * CRC/ISIZE verify -> BAM record scan -> columns, used as the checker for the
+ * CRC/ISIZE verify -> BAM record scan -> columns, used as the oracle for the
  * CUDA implementation in fritillaria_gb300.  Only tests, the smoke entry point
  * and the CPU-baseline leg of the benchmark may load it; the product never
  * calls into it.

@@ -4,7 +4,7 @@
  * Plain-C restatement of the reference's device path for the three other
  * formats that ride on the same BGZF container: bgzipped FASTQ (record scan and
  * line-bound columns), BCF (site-core scan and columns) and FASTA (newline
- * compaction of a whole reference).  The checker for the CUDA implementation in
+ * compaction of a whole reference).  The oracle for the CUDA implementation in
  * fritillaria_gb300; the product never calls into it.
  *
  * Where the reference's CPU functions and its device launchers differ on

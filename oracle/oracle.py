@@ -2,7 +2,7 @@
 and to the reference's own kernels compiled as host code (``_ref/``).
 
 Only tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` import this module.  It is the checker, never the product."""
+``bench.py`` import this module.  It is the oracle the tests compare against, never the product."""
 
 from __future__ import annotations
 

@@ -1,5 +1,5 @@
 """Tab-delimited text framing, restated on the CPU -- test infrastructure: the
-checker for the device text scanner, never called by the product.
+oracle for the device text scanner, never called by the product.
 
 Two restatements, because the reference's CPU decode and its device launcher
 differ on a batch whose last line has no newline:

@@ -1,4 +1,4 @@
-"""Columnar VCF restated on the CPU -- test infrastructure: the checker for the
+"""Columnar VCF restated on the CPU -- test infrastructure: the oracle for the
 device VCF decoder, never called by the product.
 
 Each record of a text scan (oracle/text.py device_scan, VCF dialect) is read

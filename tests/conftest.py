@@ -16,7 +16,7 @@ def pytest_configure(config):
 @pytest.fixture(scope="session")
 def gpu():
     """The native library on cuda:0.  A GPU test that cannot get it fails: on a
-    GPU machine a skip would hide a broken build."""
+    machine with a GB300 a skip would hide a broken build."""
     import fritillaria_gb300 as frt
 
     frt.lib()
