@@ -2010,14 +2010,19 @@ __device__ u32 vcf_gt_code(const u8 *p, u32 n)
     return (ploidy << 26) | (phased[1] << 25) | (phased[0] << 24) | (codes[1] << 12) | codes[0];
 }
 
-// Every sample's GT, a warp per record with lanes over its samples.  calls[t]
-// is the call of the sample that tab t opens (tabs 8 on of each record); the
-// first eight tabs of a record get 0.  key[r] = GT's index among the FORMAT
-// keys, -1 when the record has no samples or no GT key.
+// Every sample's GT, 2^wl warps per record with their lanes over its
+// samples (a population VCF holds thousands a record, so one warp a record
+// leaves most of the GPU idle on a few thousand records).  Each warp finds
+// the GT key itself.  calls[t] is the call of the sample that tab t opens
+// (tabs 8 on of each record); the first eight tabs of a record get 0.
+// key[r] = GT's index among the FORMAT keys, -1 when the record has no
+// samples or no GT key.
 __global__ void k_vcf_gt(const u8 *buf, u64 buf_len, const u64 *rec_off, const u64 *rec_end, const u64 *tabs,
-                         const u64 *field_starts, u64 n, u32 *calls, int *key)
+                         const u64 *field_starts, u64 n, u32 wl, u32 *calls, int *key)
 {
-    const u64 r = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const u64 gw = ((u64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const u64 r = gw >> wl;
+    const u32 sub = (u32)(gw & ((1ull << wl) - 1ull));
     const u32 lane = threadIdx.x & 31u;
     if (r >= n) return;
     const u64 a = rec_off[r];
@@ -2025,9 +2030,10 @@ __global__ void k_vcf_gt(const u8 *buf, u64 buf_len, const u64 *rec_off, const u
     const u32 len = (u32)(rec_end[r] - a);
     const u64 fs = field_starts[r], nt = field_starts[r + 1] - fs;
     const u32 content = rec_end[r] < buf_len && len && p[len - 1] == '\r' ? len - 1 : len;
-    for (u64 t = lane; t < nt && t < 8ull; t += 32) calls[fs + t] = 0;
+    if (sub == 0)
+        for (u64 t = lane; t < nt && t < 8ull; t += 32) calls[fs + t] = 0;
     if (nt < 8) {
-        if (lane == 0) key[r] = -1;
+        if (sub == 0 && lane == 0) key[r] = -1;
         return;
     }
     // FORMAT: [tab 7 + 1, tab 8 or the end); samples are missing when there
@@ -2046,8 +2052,8 @@ __global__ void k_vcf_gt(const u8 *buf, u64 buf_len, const u64 *rec_off, const u
             q = e + 1;
         }
     }
-    if (lane == 0) key[r] = g;
-    for (u64 j = lane; j + 8 < nt; j += 32) {
+    if (sub == 0 && lane == 0) key[r] = g;
+    for (u64 j = 32u * sub + lane; j + 8 < nt; j += 32ull << wl) {
         u32 code = (u32)FRT_VCF_GT_NONE << 28;
         if (g >= 0) {
             const u32 s0 = (u32)(tabs[fs + 8 + j] - a) + 1u;
@@ -2317,9 +2323,14 @@ extern "C" int frt_vcf_genotypes(frt_vcf_decoder *d, const frt_columns *text, fr
     if (n) {
         const frt_columns *t = text;
         auto tcol = [&](int k) { return (const u64 *)(t->cols + t->col_off[k]); };
-        k_vcf_gt<<<grid_for(n * 32, 256), 256, 0, s.stream>>>(
+        // warps per record: a power of two that gives a lane at most eight
+        // of the average record's samples, up to 16
+        const u64 samples = n_tabs / n > 8 ? n_tabs / n - 8 : 0;
+        u32 wl = 0;
+        while (wl < 4 && (256ull << wl) < samples) ++wl;
+        k_vcf_gt<<<grid_for((n << wl) * 32, 256), 256, 0, s.stream>>>(
             text->source->data, text->source->len, tcol(FRT_TEXT_COL_RECORD_OFFSETS), tcol(FRT_TEXT_COL_RECORD_ENDS),
-            tcol(FRT_TEXT_COL_TABS), tcol(FRT_TEXT_COL_FIELD_STARTS), n, colp<u32>(c, FRT_VCF_GT_COL_CALLS),
+            tcol(FRT_TEXT_COL_TABS), tcol(FRT_TEXT_COL_FIELD_STARTS), n, wl, colp<u32>(c, FRT_VCF_GT_COL_CALLS),
             colp<int>(c, FRT_VCF_GT_COL_KEY));
         if ((e = cudaGetLastError()) != cudaSuccess) {
             columns_discard(c);

@@ -70,6 +70,23 @@ def test_synthetic_population_vcf(gpu):
     assert np.array_equal(u["alleles"], want)
 
 
+def test_wide_records_take_several_warps(gpu):
+    """1,200 samples a record: the genotype kernel spreads each record over
+    eight warps; short records and lines without samples mixed in after them
+    keep their own counts."""
+    raw = bytes(synth.raw_vcf_text(40, 1200, seed=5))
+    raw += (b"chr1\t5\t.\tA\tC\t.\tPASS\t.\tGT:DP\t0|1:3\t1/1:2\n"
+            b"chr1\t6\t.\tA\tC\t.\tPASS\n"
+            b"chr2\t7\t.\tA\tC\t.\tPASS\t.\tDP:GT\t" + b"\t".join(b"4:%d|%d" % (i % 3, i % 2) for i in range(700)) + b"\n")
+    header = b"\n".join(l for l in raw.split(b"\n") if l.startswith(b"#"))
+    got = run(gpu, raw, header=header)
+    assert len(got) == 43
+    fs = got.text.column("field_starts").astype(np.int64)
+    u = gpu.VcfGenotypes.unpack(got.gt.column("calls")[fs[:40, None] + 8 + np.arange(1200)[None, :]])
+    assert u["alleles"].shape == (40, 1200, 2) and (u["status"] == 0).all()
+    assert list(got.gt.column("key")[40:]) == [0, -1, 1]
+
+
 EDGE = [b".\t1\t.\tN\t.\t.\t.\t.",
         b".\t1\t.\tN\t.\t.\t.\t.\r",
         b"chr1\t5\t.\tA\tC\t.\tPASS",
