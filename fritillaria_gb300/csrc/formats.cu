@@ -213,32 +213,79 @@ __global__ void k_tx_place(FqIndex ix, const u32 *is_rec, const u32 *rec_pos, co
     if (is_hdr[k]) hdr_off[hdr_pos[k]] = s;
 }
 
-// A warp per record, consecutive lanes on consecutive bytes.
+// A record's tabs, a warp per record.  The bytes before the record's first
+// 16-byte boundary and after its last go one a lane; the aligned 16-byte
+// blocks between, one a lane with vector loads, 32 blocks a step.  Only
+// blocks wholly inside the record are loaded as vectors.
+struct TabSplit {
+    u64 a, lo, hi, b; // [a, lo) head, [lo, hi) aligned blocks, [hi, b) tail
+    __device__ __forceinline__ TabSplit(const u8 *buf, u64 a_, u64 b_) : a(a_), b(b_)
+    {
+        const u64 base = (u64)(uintptr_t)buf;
+        const u64 up = ((base + a + 15ull) & ~15ull) - base, down = ((base + b) & ~15ull) - base;
+        lo = up < b ? up : b;
+        hi = down > lo ? down : lo;
+    }
+};
+
+// Bit i set when byte i of the block is a tab: __vcmpeq4 marks a byte 0xff,
+// and the multiply gathers the four top bits (7, 15, 23, 31) to bits 28-31
+// (its partial products never overlap, so nothing carries).
+__device__ __forceinline__ u32 tab_bits(uint4 v)
+{
+    auto f = [](u32 w) { return ((__vcmpeq4(w, 0x09090909u) & 0x80808080u) * 0x00204081u) >> 28; };
+    return f(v.x) | (f(v.y) << 4) | (f(v.z) << 8) | (f(v.w) << 12);
+}
+
 __global__ void k_tx_count_tabs(const u8 *buf, const u64 *rec_off, const u64 *rec_end, u32 n, u32 *counts)
 {
     const u32 r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
     if (r >= n) return;
-    const u64 a = rec_off[r], b = rec_end[r];
+    const TabSplit sp(buf, rec_off[r], rec_end[r]);
     u32 c = 0;
-    for (u64 q = a + lane; q < b; q += 32) c += buf[q] == '\t' ? 1u : 0u;
+    if (sp.a + lane < sp.lo) c += buf[sp.a + lane] == '\t' ? 1u : 0u;
+    for (u64 q = sp.lo + 16ull * lane; q < sp.hi; q += 512) c += __popc(tab_bits(*(const uint4 *)(buf + q)));
+    if (sp.hi + lane < sp.b) c += buf[sp.hi + lane] == '\t' ? 1u : 0u;
 #pragma unroll
     for (int d = 16; d; d >>= 1) c += __shfl_down_sync(FRT_FULL_MASK, c, d);
     if (lane == 0) counts[r] = c;
 }
 
+// The same split, writing each tab's offset in order: the lanes' counts are
+// scanned across the warp to place each lane's tabs.
 __global__ void k_tx_emit_tabs(const u8 *buf, const u64 *rec_off, const u64 *rec_end, u32 n, const u32 *tab_base,
                                u64 *tabs)
 {
     const u32 r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
     if (r >= n) return;
-    const u64 a = rec_off[r], b = rec_end[r];
+    const TabSplit sp(buf, rec_off[r], rec_end[r]);
     u32 at = tab_base[r];
-    for (u64 q0 = a; q0 < b; q0 += 32) {
-        const u64 q = q0 + lane;
-        const bool t = q < b && buf[q] == '\t';
+    {
+        const u64 q = sp.a + lane;
+        const bool t = q < sp.lo && buf[q] == '\t';
         const u32 m = __ballot_sync(FRT_FULL_MASK, t);
         if (t) tabs[at + __popc(m & lanemask_lt())] = q;
         at += __popc(m);
+    }
+    for (u64 q0 = sp.lo; q0 < sp.hi; q0 += 512) {
+        const u64 q = q0 + 16ull * lane;
+        u32 bits = q < sp.hi ? tab_bits(*(const uint4 *)(buf + q)) : 0u;
+        const u32 c = __popc(bits);
+        u32 incl = c;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const u32 y = __shfl_up_sync(FRT_FULL_MASK, incl, d);
+            if ((int)lane >= d) incl += y;
+        }
+        u32 w = at + incl - c;
+        for (; bits; bits &= bits - 1u) tabs[w++] = q + (u32)(__ffs(bits) - 1);
+        at += __shfl_sync(FRT_FULL_MASK, incl, 31);
+    }
+    {
+        const u64 q = sp.hi + lane;
+        const bool t = q < sp.b && buf[q] == '\t';
+        const u32 m = __ballot_sync(FRT_FULL_MASK, t);
+        if (t) tabs[at + __popc(m & lanemask_lt())] = q;
     }
 }
 
