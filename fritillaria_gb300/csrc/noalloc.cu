@@ -13,6 +13,11 @@
 // Limits and sharing:
 //   * at most FRT_NOALLOC_MAX_MEMBERS members per call (4 MiB of scratch,
 //     held by every GPU that loads the library until the process exits);
+//   * each member holds at most 65,536 inflated bytes (BGZF's limit, which
+//     sizes the per-member slots of the scratch), the offsets ascend and the
+//     last is at most len; a call that breaks this is rejected with
+//     FRT_ERR_INVALID_ARGUMENT after the scan, which never writes outside
+//     the scratch or the caller's arrays in the meantime;
 //   * every call shares that one array, which keeps the last call's
 //     contents; calls that overlap on the GPU (two streams, two threads)
 //     race on it and must be serialised by the caller;
@@ -67,13 +72,23 @@ int scratch_for(int device, unsigned char **out, frt_error *err)
     return FRT_OK;
 }
 
+// Flags (bad[0] = 1) a member table the scratch cannot hold: a member of
+// more than 65,536 inflated bytes, offsets that descend, or an end past len.
+__global__ void k_check_members(const u64 *starts, u32 n, u64 len, u64 *bad)
+{
+    for (u32 m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+        u64 ms = starts[m], me = starts[m + 1];
+        if (me < ms || me - ms > 65536ull || me > len) *bad = 1ull;
+    }
+}
+
 // Record offsets from the per-member scratch: one warp per member.
 __global__ void k_emit_offsets(const u64 *starts, u32 n, const u32 *count, const u32 *first, const u16 *recs,
                                u64 *out, u64 cap)
 {
     u32 m = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     if (m >= n) return;
-    u32 c = count[m];
+    u32 c = min(count[m], (u32)FRT_SCAN_CAP);
     u64 ms = starts[m];
     const u16 *r = recs + (size_t)m * FRT_SCAN_CAP;
     for (u32 k = lane_id(); k < c; k += 32) {
@@ -100,6 +115,13 @@ extern "C" int frt_bam_scan_noalloc(const uint8_t *data, uint64_t len, const uin
         set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "null argument");
         return FRT_ERR_INVALID_ARGUMENT;
     }
+    if (!record_offsets && record_cap) {
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr,
+                  "record_offsets is null but record_cap is %llu (a null array counts records only with "
+                  "record_cap 0)",
+                  (unsigned long long)record_cap);
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
     int device = 0;
     cudaError_t e = cudaGetDevice(&device);
     if (e != cudaSuccess) return cuda_fail(err, e, "querying the current device");
@@ -119,6 +141,8 @@ extern "C" int frt_bam_scan_noalloc(const uint8_t *data, uint64_t len, const uin
     int bound = n_ref >= 0 ? n_ref : (1 << 24);
     // the previous call's totals must not leak into this one
     if ((e = cudaMemsetAsync(totals, 0, 64, st)) != cudaSuccess) return cuda_fail(err, e, "clearing the totals");
+    k_check_members<<<(n_members + 255) / 256, 256, 0, st>>>(member_offsets, n_members, len, totals + 4);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(err, e, "launching the member check");
     if ((e = frt_launch_bam_spec(data, len, member_offsets, n_members, start, bound, entry, count, land, flags, recs,
                                  st)) != cudaSuccess)
         return cuda_fail(err, e, "launching the record scan");
@@ -130,17 +154,26 @@ extern "C" int frt_bam_scan_noalloc(const uint8_t *data, uint64_t len, const uin
                                                             (u64 *)record_offsets, record_cap);
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(err, e, "launching the offset emit");
     }
-    uint64_t tot[4] = {0, 0, 0, 0};
+    uint64_t tot[5] = {0, 0, 0, 0, 0};
     if ((e = cudaMemcpyAsync(tot, totals, sizeof tot, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         return cuda_fail(err, e, "reading the totals");
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(err, e, "record scan");
+    if (tot[4]) {
+        *n_records = 0;
+        *tail = start;
+        set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr,
+                  "a member holds more than 65,536 inflated bytes, or the member offsets descend or run past "
+                  "len: the scan's per-member scratch holds BGZF members only");
+        return FRT_ERR_INVALID_ARGUMENT;
+    }
     *n_records = tot[0];
     *tail = tot[1];
     if (tot[2]) {
         set_error(err, FRT_ERR_MALFORMED, 0, 0, 0, tot[1], "bam", "malformed record reached from a confirmed boundary");
         return FRT_ERR_MALFORMED;
     }
-    if (tot[0] > record_cap) {
+    // a null array with record_cap 0 asks for the count alone
+    if (record_offsets && tot[0] > record_cap) {
         set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, tot[0], record_cap, 0, nullptr,
                   "the batch holds %llu records but record_offsets has room for %llu",
                   (unsigned long long)tot[0], (unsigned long long)record_cap);

@@ -181,14 +181,18 @@ uint64_t frt_bam_decoder_last_fallbacks(const frt_bam_decoder *d);
  * allocate inside a capture or under a fixed budget, pipelines that
  * preallocate once).  The caller passes the inflated bytes (`data`, `len`),
  * the n_members + 1 member start offsets (device), and `record_offsets`
- * (device, room for `record_cap` entries); the scan's scratch is a fixed
- * device array of the library, so at most FRT_NOALLOC_MAX_MEMBERS members per
- * call (larger batches are rejected with FRT_ERR_INVALID_ARGUMENT).  Results
- * equal frt_bam_decode's record offsets and tail.  All calls share the one
- * scratch array: calls that overlap on the GPU race and must be serialised.
- * The first call on a device looks up the array's address with that device
- * current; make it before any stream capture.  Synchronises `stream` to return
- * n_records and tail. */
+ * (device, room for `record_cap` entries; null only with record_cap 0, which
+ * counts the records); the scan's scratch is a fixed device array of the
+ * library, so at most FRT_NOALLOC_MAX_MEMBERS members per call (larger
+ * batches are rejected with FRT_ERR_INVALID_ARGUMENT), each of at most
+ * 65,536 inflated bytes with ascending offsets ending at or before len (else
+ * FRT_ERR_INVALID_ARGUMENT).  Results equal frt_bam_decode's record offsets
+ * and tail.  All calls share the one scratch array: calls that overlap on the
+ * GPU race and must be serialised.  The first call on a device looks up the
+ * array's address with that device current; make it before any stream
+ * capture.  The address is looked up once per device per process, so after a
+ * cudaDeviceReset reload the library before calling again.  Synchronises
+ * `stream` to return n_records and tail. */
 #define FRT_NOALLOC_MAX_MEMBERS 1024
 int frt_bam_scan_noalloc(const uint8_t *data, uint64_t len, const uint64_t *member_offsets, uint32_t n_members,
                          uint64_t start, int32_t n_ref, uint64_t *record_offsets, uint64_t record_cap,
