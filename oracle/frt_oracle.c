@@ -693,6 +693,114 @@ int orc_baseline_file(const uint8_t *file, size_t len, int format, int threads, 
 }
 
 
+/* Every member of a BGZF file inflated and CRC/ISIZE-checked by the worker
+ * pool of orc_baseline_bam, into `out` at the ISIZE prefix sum.  Returns
+ * ORC_ERR_INVALID_ARGUMENT (with *total set) when out_cap is short. */
+int orc_inflate_file(const uint8_t *file, size_t len, int threads, uint8_t *out, uint64_t out_cap, uint64_t *members,
+                     uint64_t *total_out)
+{
+    size_t cap = len / 28 + 1;
+    orc_span *spans = (orc_span *)malloc(cap * sizeof *spans);
+    size_t n = 0, consumed = 0;
+    orc_error err;
+    *members = 0;
+    *total_out = 0;
+    if (orc_bgzf_discover(file, len, 0, spans, cap, &n, &consumed, &err)) { free(spans); return err.code; }
+    uint64_t *out_off = (uint64_t *)malloc((n + 1) * sizeof *out_off);
+    uint64_t total = 0;
+    for (size_t i = 0; i < n; ++i) { out_off[i] = total; total += spans[i].isize; }
+    out_off[n] = total;
+    *members = n;
+    *total_out = total;
+    int status = total > out_cap ? ORC_ERR_INVALID_ARGUMENT : ORC_OK;
+    if (!status) {
+        bl_ctx ctx;
+        ctx.file = file; ctx.spans = spans; ctx.out_off = out_off; ctx.out = out; ctx.n = n;
+        atomic_init(&ctx.next, 0);
+        atomic_init(&ctx.failed, 0);
+        ctx.done = (atomic_uchar *)calloc(n + 1, 1);
+        if (threads < 1) threads = 1;
+        pthread_t *tids = (pthread_t *)malloc(sizeof(pthread_t) * threads);
+        for (int t = 0; t < threads; ++t) pthread_create(&tids[t], NULL, bl_worker, &ctx);
+        for (int t = 0; t < threads; ++t) pthread_join(tids[t], NULL);
+        if (atomic_load(&ctx.failed)) status = ORC_ERR_CHECKSUM;
+        free(tids);
+        free((void *)ctx.done);
+    }
+    free(out_off);
+    free(spans);
+    return status;
+}
+
+/* Parity at scale: the whole BAM file as the oracle decodes it, so that a
+ * device run over the same file can be compared column for column.  Members
+ * are inflated and CRC/ISIZE-checked by the worker pool of orc_baseline_bam;
+ * then the header (header.rs:43-101), the serial scan (record.rs:58-95), the
+ * columns (batch.rs:165-177), each record's virtual offset (member compressed
+ * offset << 16 | in-member offset, virtual_offset.rs:24-70) and its aux
+ * directory (aux.rs:301-479, entries up to the first malformed field;
+ * aux_first holds records + 1 prefix entries).  A capacity that is too small
+ * returns ORC_ERR_INVALID_ARGUMENT with the sizes needed in res. */
+int orc_bam_file_decode(const uint8_t *file, size_t len, int threads, uint8_t *inflated, uint64_t inflated_cap,
+                        uint64_t *record_offsets, uint64_t *virtual_offsets, const orc_bam_columns *cols,
+                        uint32_t *aux_first, orc_aux_entry *aux, uint64_t rec_cap, uint64_t aux_cap,
+                        orc_file_decode *res)
+{
+    memset(res, 0, sizeof *res);
+    uint64_t total = 0, n_members = 0;
+    int status = orc_inflate_file(file, len, threads, inflated, inflated_cap, &n_members, &total);
+    res->members = n_members;
+    res->inflated_bytes = total;
+    /* the spans again, for the virtual offsets (discovery succeeded above) */
+    size_t cap = len / 28 + 1;
+    orc_span *spans = (orc_span *)malloc(cap * sizeof *spans);
+    size_t n = 0, consumed = 0;
+    orc_error err;
+    if (!status) orc_bgzf_discover(file, len, 0, spans, cap, &n, &consumed, &err);
+    uint64_t *out_off = (uint64_t *)malloc((n + 1) * sizeof *out_off);
+    uint64_t at = 0;
+    for (size_t i = 0; i < n; ++i) { out_off[i] = at; at += spans[i].isize; }
+    out_off[n] = at;
+    uint64_t start = 0;
+    int32_t nref = 0;
+    if (!status) status = orc_bam_header(inflated, total, &start, &nref, &err);
+    size_t nrec = 0;
+    uint64_t tail = 0;
+    if (!status) status = orc_bam_scan(inflated, total, start, record_offsets, rec_cap, &nrec, &tail, &err);
+    res->records_start = start;
+    res->n_ref = nref;
+    res->records = nrec;
+    res->tail = tail;
+    if (!status && nrec > rec_cap) status = ORC_ERR_INVALID_ARGUMENT;
+    if (!status) {
+        orc_bam_decode(inflated, record_offsets, nrec, cols);
+        size_t m = 0;
+        uint64_t k = 0;
+        for (size_t i = 0; i < nrec; ++i) {
+            uint64_t ro = record_offsets[i];
+            while (m + 1 < n && out_off[m + 1] <= ro) ++m;
+            virtual_offsets[i] = (spans[m].compressed_offset << 16) | (ro - out_off[m]);
+            const uint8_t *r = inflated + ro;
+            uint32_t bs = rd32(r);
+            uint32_t as = cols->aux_start[i];
+            uint32_t nt = 0;
+            aux_first[i] = (uint32_t)k;
+            if (as <= 4 + bs) {
+                orc_bam_aux(r, as, 4 + bs, k < aux_cap ? aux + k : NULL, k < aux_cap ? (uint32_t)(aux_cap - k) : 0, &nt);
+            }
+            k += nt;
+        }
+        aux_first[nrec] = (uint32_t)k;
+        res->aux_entries = k;
+        if (k > aux_cap) status = ORC_ERR_INVALID_ARGUMENT;
+    }
+    res->status = status;
+    free(out_off);
+    free(spans);
+    return status;
+}
+
+
 /* The reference's indexed query over one chunk, on the host: records of the
  * chain from `start` that begin before `chunk_end` (offsets in the inflated
  * chunk), kept when on reference `ref` their [pos + 1, pos + span] meets

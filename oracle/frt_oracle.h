@@ -124,6 +124,26 @@ typedef struct {
 
 int orc_baseline_bam(const uint8_t *file, size_t len, int threads, uint64_t max_members,
                      orc_baseline_result *res);
+/* Every member of a BGZF file inflated and checked on `threads` host threads. */
+int orc_inflate_file(const uint8_t *file, size_t len, int threads, uint8_t *out, uint64_t out_cap, uint64_t *members,
+                     uint64_t *total);
+/* The whole BAM file decoded by the oracle, for parity against a device run
+ * at full size (see frt_oracle.c). */
+typedef struct {
+    uint64_t members;
+    uint64_t inflated_bytes;
+    uint64_t records;
+    uint64_t aux_entries;
+    uint64_t tail;
+    uint64_t records_start;
+    int32_t n_ref;
+    int32_t status;
+} orc_file_decode;
+
+int orc_bam_file_decode(const uint8_t *file, size_t len, int threads, uint8_t *inflated, uint64_t inflated_cap,
+                        uint64_t *record_offsets, uint64_t *virtual_offsets, const orc_bam_columns *cols,
+                        uint32_t *aux_first, orc_aux_entry *aux, uint64_t rec_cap, uint64_t aux_cap,
+                        orc_file_decode *res);
 /* Records of one BAI chunk that a region query keeps (see frt_oracle.c). */
 uint64_t orc_region_records(const uint8_t *buf, uint64_t len, uint64_t start, uint64_t chunk_end, int32_t ref,
                             uint64_t beg, uint64_t end, uint64_t *out, uint64_t cap);

@@ -24,6 +24,12 @@ class OrcSpan(C.Structure):
                 ("isize", C.c_uint32), ("crc32", C.c_uint32)]
 
 
+class OrcFileDecode(C.Structure):
+    _fields_ = [("members", C.c_uint64), ("inflated_bytes", C.c_uint64), ("records", C.c_uint64),
+                ("aux_entries", C.c_uint64), ("tail", C.c_uint64), ("records_start", C.c_uint64),
+                ("n_ref", C.c_int32), ("status", C.c_int32)]
+
+
 class OrcBaseline(C.Structure):
     _fields_ = [("members", C.c_uint64), ("inflated_bytes", C.c_uint64), ("records", C.c_uint64),
                 ("aux_tags", C.c_uint64), ("checksum", C.c_uint64), ("seconds", C.c_double), ("status", C.c_int32)]
@@ -54,6 +60,9 @@ def lib():
         _lib.orc_bam_aux.argtypes = [_P, C.c_uint32, C.c_uint32, _P, C.c_uint32, _P]
         _lib.orc_baseline_bam.argtypes = [_P, C.c_size_t, C.c_int, C.c_uint64, _P]
         _lib.orc_baseline_file.argtypes = [_P, C.c_size_t, C.c_int, C.c_int, _P]
+        _lib.orc_inflate_file.argtypes = [_P, C.c_size_t, C.c_int, _P, C.c_uint64, _P, _P]
+        _lib.orc_bam_file_decode.argtypes = [_P, C.c_size_t, C.c_int, _P, C.c_uint64, _P, _P, _P, _P, _P, C.c_uint64,
+                                             C.c_uint64, _P]
         _lib.orc_region_records.restype = C.c_uint64
         _lib.orc_region_records.argtypes = [_P, C.c_uint64, C.c_uint64, C.c_uint64, C.c_int32, C.c_uint64, C.c_uint64,
                                             _P, C.c_uint64]
@@ -261,6 +270,51 @@ def baseline_bam(bgzf, threads: int, max_members: int = 0):
     return res
 
 
+def inflate_file(bgzf, threads: int, total: int | None = None) -> np.ndarray:
+    """Every member inflated and CRC/ISIZE-checked on `threads` host threads;
+    `total` (the inflated size, when known) saves a discovery pass."""
+    b = _buf(bgzf)
+    members, got = C.c_uint64(), C.c_uint64()
+    if total is None:
+        lib().orc_inflate_file(_ptr(b), b.size, threads, None, 0, C.byref(members), C.byref(got))
+        total = got.value
+    out = np.empty(max(int(total), 1), np.uint8)
+    rc = lib().orc_inflate_file(_ptr(b), b.size, threads, _ptr(out), out.size, C.byref(members), C.byref(got))
+    if rc:
+        raise RuntimeError(f"oracle inflate failed: code {rc}")
+    return out[: got.value]
+
+
+def decode_bam_file_mt(bgzf, threads: int, records: int, aux_entries: int, inflated_bytes: int) -> dict:
+    """The whole BAM file decoded by the oracle on `threads` inflate threads:
+    inflated bytes, the serial scan, every column, virtual offsets and the aux
+    directory.  The capacities come from the run being checked; a file that
+    needs more raises with the sizes the oracle found."""
+    b = _buf(bgzf)
+    inflated = np.empty(max(int(inflated_bytes), 1), np.uint8)
+    rec_cap = int(records) + 1
+    cols = {name: np.zeros(rec_cap, dtype=dt) for name, dt in BAM_COLUMNS}
+    ptrs = [_ptr(cols[name]) for name, _ in BAM_COLUMNS]
+    struct = (C.c_void_p * len(ptrs))(*ptrs)
+    offs = np.zeros(rec_cap, np.uint64)
+    vo = np.zeros(rec_cap, np.uint64)
+    first = np.zeros(rec_cap + 1, np.uint32)
+    aux = np.zeros(max(int(aux_entries), 1), dtype=AUX_DTYPE)
+    res = OrcFileDecode()
+    rc = lib().orc_bam_file_decode(_ptr(b), b.size, threads, _ptr(inflated), inflated.size, _ptr(offs), _ptr(vo),
+                                   C.byref(struct), _ptr(first), _ptr(aux), rec_cap, aux.size, C.byref(res))
+    if rc:
+        raise RuntimeError(f"oracle decode failed: code {rc}; records {res.records}, aux entries {res.aux_entries}, "
+                           f"inflated bytes {res.inflated_bytes}")
+    n = int(res.records)
+    out = {name: cols[name][:n] for name, _ in BAM_COLUMNS}
+    out["record_offsets"] = offs[:n]
+    out["virtual_offset"] = vo[:n]
+    out["aux_first"] = first[: n + 1]
+    return {"inflated": inflated[: res.inflated_bytes], "columns": out, "aux_entries": aux[: res.aux_entries],
+            "tail": int(res.tail), "records_start": int(res.records_start), "members": int(res.members)}
+
+
 # ---- FASTQ, BCF, FASTA (frt_oracle_formats.c) ------------------------------
 
 TILED, WALKED = 0, 1
@@ -269,10 +323,11 @@ FASTQ_COLUMNS = [("sequence_start", np.uint32), ("plus_start", np.uint32), ("qua
                  ("sequence_len", np.uint32), ("record_end", np.uint32)]
 
 
-def fastq_scan(buf, start: int = 0):
-    """FastqScanner::scan semantics: (offsets, tail, survivors, proof)."""
+def fastq_scan(buf, start: int = 0, cap: int | None = None):
+    """FastqScanner::scan semantics: (offsets, tail, survivors, proof).
+    `cap` bounds the offsets list (default: one per four bytes)."""
     b = _buf(buf)
-    cap = b.size // 4 + 1
+    cap = b.size // 4 + 1 if cap is None else int(cap)
     offs = np.zeros(cap, dtype=np.uint64)
     n, tail, surv, proof = C.c_size_t(), C.c_uint64(), C.c_uint64(), C.c_int()
     rc = lib().orc_fastq_scan(_ptr(b), b.size, start, _ptr(offs), cap, C.byref(n), C.byref(tail), C.byref(surv),
@@ -282,10 +337,10 @@ def fastq_scan(buf, start: int = 0):
     return offs[: n.value].copy(), tail.value, surv.value, proof.value
 
 
-def fastq_decode(buf, start: int = 0) -> dict:
+def fastq_decode(buf, start: int = 0, cap: int | None = None) -> dict:
     """Offsets, tail and the five line-bound columns of FastqScanner::decode."""
     b = _buf(buf)
-    offs, tail, surv, proof = fastq_scan(b, start)
+    offs, tail, surv, proof = fastq_scan(b, start, cap)
     cols = {name: np.zeros(len(offs), dtype=dt) for name, dt in FASTQ_COLUMNS}
     errors = lib().orc_fastq_decode(_ptr(b), b.size, _ptr(offs), len(offs),
                                     *[_ptr(cols[name]) for name, _ in FASTQ_COLUMNS])
@@ -343,11 +398,12 @@ FASTA_BOUNDS_DTYPE = np.dtype([("sequence_start", "<u4"), ("line_bases", "<u4"),
                                ("uniform", "u1"), ("sequence_len", "<u8"), ("record_end", "<u8")], align=True)
 
 
-def fasta_compact(buf) -> dict:
+def fasta_compact(buf, cap: int | None = None) -> dict:
     """FastaCompactor::compact semantics: the bases of every contig without
-    newlines, plus per-contig offsets, lengths, record offsets and layout."""
+    newlines, plus per-contig offsets, lengths, record offsets and layout.
+    `cap` bounds the contig count (default: one per two bytes)."""
     b = _buf(buf)
-    cap = b.size // 2 + 1
+    cap = b.size // 2 + 1 if cap is None else int(cap)
     so, sl, ro = (np.zeros(cap, dtype=np.uint64) for _ in range(3))
     bounds = np.zeros(cap, dtype=FASTA_BOUNDS_DTYPE)
     n, total = C.c_size_t(), C.c_uint64()

@@ -41,7 +41,7 @@ sys.path.insert(0, str(ROOT))
 from fritillaria_gb300 import synth  # noqa: E402
 from oracle import oracle  # noqa: E402
 
-TESTDATA = Path("/root/reference/testdata")
+from oracle.build import REFERENCE_TESTDATA as TESTDATA  # noqa: E402
 BASES = b"=ACMGRSVTWYHKDBN"
 OPS = b"MIDNSHP=X"
 N_HTSLIB = 1000

@@ -5,7 +5,6 @@ synthetic multi-contig indexes, the records those chunks reach against a
 brute-force overlap scan, the reference's merge/optimize known answers
 (crates/fritillaria-csi/src/binning_index.rs tests), and the error paths."""
 
-import os
 from pathlib import Path
 
 import numpy as np
@@ -14,8 +13,8 @@ import pytest
 from fritillaria_gb300 import synth
 from oracle import bai as obai
 from oracle import oracle
+from oracle.build import REFERENCE_TESTDATA as TESTDATA
 
-TESTDATA = Path(os.environ.get("FRT_REFERENCE_TESTDATA", "/root/reference/testdata"))
 
 
 @pytest.fixture(scope="module")

@@ -17,7 +17,6 @@ member offset.
 
 import ctypes as C
 import hashlib
-import os
 import zlib
 from pathlib import Path
 
@@ -25,10 +24,10 @@ import numpy as np
 import pytest
 
 from oracle import oracle
+from oracle.build import REFERENCE_TESTDATA as TESTDATA
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("fields_", "text_")))  # record-field and text inputs have their own tests
-TESTDATA = Path(os.environ.get("FRT_REFERENCE_TESTDATA", "/root/reference/testdata"))
 
 # frt_status / Error variants (crates/fritillaria-core/src/error.rs:14-67)
 INVALID_BLOCK, CHECKSUM, SIZE, INFLATE, MALFORMED = 2, 3, 4, 5, 6
@@ -296,3 +295,35 @@ def test_reference_crc_kernel_matches_oracle():
     lib.ref_crc32_blocks(buf.ctypes.data_as(C.c_void_p), off.ctypes.data_as(C.c_void_p),
                          ln.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p), n)
     assert np.array_equal(out, g["span_crc32"])
+
+
+def test_threaded_whole_file_decode_equals_the_serial_oracle():
+    """The whole-file decode the benchmark checks its full-size run against
+    (threaded inflate, scan, columns, virtual offsets, aux directory) gives
+    what the serial oracle functions give on the same file."""
+    from fritillaria_gb300 import synth
+
+    _, bgzf = synth.short_read_bam(3000, n_contigs=3, genome_len=3_000_000, seed=9, levels=(1, 6))
+    want = oracle.decode_bam_file(bgzf)
+    n = len(want["columns"]["pos"])
+    entries = sum(oracle.bam_aux(want["inflated"], int(o), int(want["columns"]["aux_start"][i]),
+                                 int(want["columns"]["record_end"][i]))[0].size
+                  for i, o in enumerate(want["columns"]["record_offsets"]))
+    got = oracle.decode_bam_file_mt(bgzf, 4, n, entries, want["inflated"].size)
+    assert np.array_equal(got["inflated"], want["inflated"])
+    assert got["tail"] == want["tail"] and got["records_start"] == want["records_start"]
+    for k, _ in oracle.BAM_COLUMNS:
+        assert np.array_equal(got["columns"][k], want["columns"][k]), k
+    assert np.array_equal(got["columns"]["record_offsets"], want["columns"]["record_offsets"])
+    vo = oracle.virtual_offsets(want["spans"], want["offsets"][:-1], want["columns"]["record_offsets"])
+    assert np.array_equal(got["columns"]["virtual_offset"], vo)
+    first = got["columns"]["aux_first"]
+    for i in (0, 1, n // 2, n - 1):
+        e, _ = oracle.bam_aux(want["inflated"], int(want["columns"]["record_offsets"][i]),
+                              int(want["columns"]["aux_start"][i]), int(want["columns"]["record_end"][i]))
+        assert np.array_equal(got["aux_entries"][first[i]:first[i + 1]], e)
+    assert int(first[-1]) == entries
+    # a capacity one record short is refused with the sizes found
+    with pytest.raises(RuntimeError, match="records"):
+        oracle.decode_bam_file_mt(bgzf, 2, n - 2, entries, want["inflated"].size)
+    assert np.array_equal(oracle.inflate_file(bgzf, 3), want["inflated"])

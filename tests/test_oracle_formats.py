@@ -13,7 +13,6 @@ Anchors:
     fixtures, on batch seams cut through them, and on synthetic data.
 """
 
-import os
 from pathlib import Path
 
 import numpy as np
@@ -21,9 +20,9 @@ import pytest
 
 from fritillaria_gb300 import synth
 from oracle import oracle
+from oracle.build import REFERENCE_TESTDATA as TESTDATA
 from oracle import ref as ref_kernels
 
-TESTDATA = Path(os.environ.get("FRT_REFERENCE_TESTDATA", "/root/reference/testdata"))
 
 
 def fixture(name):
