@@ -81,6 +81,16 @@ SERVING = {
 }
 
 METRIC = "BAM->device-column decompressed GB/s, batched vs plain, 1 GB300, bit-exact"
+# members per batch of the plain per-batch loop: the reference's default
+# (crates/fritillaria-bgzf/src/read.rs:37) first, then larger batches
+PLAIN_BATCHES = (256, 1024, 4096, 16384)
+
+
+def bam_config(workload: str, records: int, members: int, compressed: int, inflated: int, world: int) -> dict:
+    """The workload as both arms report it (the same keys and values)."""
+    return {"workload": workload, "description": WORKLOADS[workload]["desc"], "records": int(records),
+            "members": int(members), "compressed_bytes": int(compressed), "inflated_bytes": int(inflated),
+            "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"}
 # Inflate tunings measured on GB300 (written by the autotuner, one entry per
 # device and workload class); a miss is tuned at start-up and added.
 TUNING_CACHE = ROOT / "fritillaria_gb300" / "inflate_tuning.json"
@@ -206,19 +216,163 @@ def whole_job_gbs(bytes_per_rank: int, world: int, steps: int, ms: float) -> flo
     return world * bytes_per_rank * steps / (ms / 1e3) / 1e9
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def cpu_baseline(bgzf, inflated_bytes: int):
-    """The oracle's CPU restatement, all host threads, whole file (a bounded
-    sample: seconds of work on 16 cores)."""
+    """The oracle's CPU restatement of the reference's CPU path: all host
+    threads over the whole file (seconds of work on 16 cores), and one thread
+    over the file's first quarter of members (a bounded sample)."""
     from oracle import oracle
 
     threads = os.cpu_count() or 1
     res = oracle.baseline_bam(bgzf, threads)
     gbs = res.inflated_bytes / res.seconds / 1e9 if res.seconds > 0 else 0.0
+    quarter = max(1, res.members // 4)
+    one = oracle.baseline_bam(bgzf, 1, quarter)
+    one_gbs = one.inflated_bytes / one.seconds / 1e9 if one.seconds > 0 else 0.0
     return {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
             "sample": f"whole file: {res.members} members, {res.inflated_bytes} inflated bytes, {res.records} "
                       f"records, {res.seconds:.2f} s; C restatement of the noodles multithreaded BGZF reader "
                       f"(zlib 1.3 inflate + CRC32) and the serial record scan/columns/aux walk",
-            "records": res.records, "status": res.status}
+            "records": res.records, "status": res.status, "cpu_model": cpu_model(), "nproc": threads,
+            "one_thread": {"value": round(one_gbs, 3), "unit": "GB/s", "cores": 1,
+                           "sample": f"the first {one.members} members ({one.inflated_bytes} inflated bytes, "
+                                     f"{one.records} records), {one.seconds:.2f} s"}}
+
+
+class _DeviceBytes:
+    """A device byte range as a torch tensor view (no copy), through the CUDA
+    array interface."""
+
+    def __init__(self, ptr: int, n: int):
+        self.__cuda_array_interface__ = {"shape": (int(n),), "typestr": "|u1", "data": (int(ptr), False),
+                                         "version": 2, "strides": None}
+
+
+def same_bytes(ptr: int, n: int, host) -> bool:
+    """Whether n device bytes at ptr equal the host array, compared in
+    256 MiB slices (no full-size host copy)."""
+    import numpy as np
+    import torch
+
+    if host.size != n:
+        return False
+    if n == 0:
+        return True
+    view = torch.as_tensor(_DeviceBytes(ptr, n), device="cuda")
+    step = 1 << 28
+    for a in range(0, n, step):
+        if not np.array_equal(view[a:a + step].cpu().numpy(), host[a:a + step]):
+            return False
+    return True
+
+
+def oracle_bam(st, bgzf):
+    """The oracle's decode of the whole file (threaded inflate with CRC32/ISIZE
+    checks, serial scan, columns, virtual offsets, aux directory), sized from
+    the run it will check; (decode or None, error, seconds)."""
+    from oracle import oracle
+
+    t0 = time.perf_counter()
+    try:
+        want = oracle.decode_bam_file_mt(bgzf, os.cpu_count() or 1, st.records, st.aux_fields, st.inflated_bytes)
+        return want, None, time.perf_counter() - t0
+    except RuntimeError as e:
+        return None, str(e), time.perf_counter() - t0
+
+
+def parity_bam(eng, st, want, error: str | None, oracle_s: float) -> dict:
+    """Bit-exactness of the timed run at its full size: the engine's inflated
+    bytes, every column, the virtual offsets, the aux directory and the tail
+    against the oracle's decode of the same file.  Runs after the timed
+    region."""
+    import numpy as np
+
+    import fritillaria_gb300 as frt
+
+    t0 = time.perf_counter()
+    if want is None:
+        return {"checked": True, "match": False, "mismatch": [error], "seconds": round(oracle_s, 1)}
+    bad = []
+    ptr, n = eng.inflated_ptr()
+    if not same_bytes(ptr, n, want["inflated"]):
+        bad.append("inflated bytes")
+    if st.records != len(want["columns"]["pos"]):
+        bad.append("record count")
+    if st.tail != want["tail"]:
+        bad.append("tail")
+    names = list(frt.BAM_COLUMNS)
+    for name in names:
+        if not np.array_equal(eng.column(name), want["columns"][name]):
+            bad.append(name)
+    if not np.array_equal(eng.column("aux_entries"), want["aux_entries"]):
+        bad.append("aux_entries")
+    return {"checked": True, "match": not bad, "columns": len(names) + 1, "records": len(want["columns"]["pos"]),
+            "inflated_bytes": int(want["inflated"].size), "aux_entries": int(want["aux_entries"].size),
+            "mismatch": bad, "seconds": round(oracle_s + time.perf_counter() - t0, 1),
+            "against": "oracle whole-file decode (zlib inflate + CRC32/ISIZE on every member, serial scan_records, "
+                       "RecordBatch::decode columns, virtual offsets, aux directory)"}
+
+
+def reference_cuda(hbuf, want, inflated: int, blocks_per_batch: int = 256, sample_gb: float = 0.5) -> dict:
+    """The reference's own CUDA kernels, compiled from its sources for sm_103a
+    and driven in its launch order (reader batches of blocks_per_batch x 64 KiB
+    compressed, inflate_blocks a thread per member, host verification,
+    bam_scan_blocks, bam_reconcile<<<1,1>>>, emit, decode_fields) from the same
+    pinned host bytes as the plain arm.  Its one-thread-per-member inflate
+    runs at tens of MB/s, so it takes a bounded sample: the batches that start
+    within the first sample_gb of inflated bytes' worth of compressed input
+    (the whole file when it is smaller).  One run is checked against the
+    oracle's records of that prefix, then one is timed."""
+    import numpy as np
+
+    from oracle import ref_cuda
+
+    why = ref_cuda.available()
+    if why:
+        return {"unavailable": why}
+    ratio = inflated / max(1, hbuf.size)
+    stop = 0 if inflated <= sample_gb * 1e9 else int(sample_gb * 1e9 / ratio)
+    out = {"unit": "GB/s", "members_per_batch": blocks_per_batch,
+           "form": "reference kernels inflate.cu + bam_decode.cu (nvcc, sm_103a) under a C++ restatement of "
+                   "DeviceBgzfReader + CudaCodec + BamDecoder (oracle/ref_cuda_driver.cpp); wall time of the "
+                   "loop from pinned host memory",
+           "sample": "whole file" if not stop else f"the batches starting in the first {stop} compressed bytes"}
+    try:
+        n = 0 if want is None else len(want["columns"]["pos"])
+        res, cols = ref_cuda.run_bam(hbuf, blocks_per_batch, columns_cap=n + 16 if n else 0, stop_after=stop)
+        if want is not None:
+            k = int(res.records)
+            ok = k <= n and np.array_equal(cols["record_offsets"], want["columns"]["record_offsets"][:k])
+            for c in ("ref_id", "pos", "flags", "seq_len"):
+                ok = ok and np.array_equal(cols[c], want["columns"][c][:k])
+            out["matches_oracle"] = bool(ok and (stop or k == n))
+            del cols
+        res, _ = ref_cuda.run_bam(hbuf, blocks_per_batch, stop_after=stop)
+    except RuntimeError as e:
+        return {"unavailable": f"the reference's CUDA path failed: {e}"}
+    out.update({"value": round(res.consumed_bytes / res.seconds / 1e9, 4), "seconds": round(res.seconds, 3),
+                "records": int(res.records), "inflated_bytes": int(res.consumed_bytes), "batches": int(res.batches),
+                "inflate_kernel_ms": round(res.inflate_ms, 2), "reconcile_kernel_ms": round(res.reconcile_ms, 2),
+                "kernels_ms": round(res.kernels_ms, 2),
+                "reinflated_bytes": int(res.inflated_bytes - res.consumed_bytes)})
+    return out
 
 
 def run_reference(args, rank, world):
@@ -263,22 +417,24 @@ def run_reference(args, rank, world):
         fmt = {"bcf": 1, "fastq": 2, "fasta": 3}
         times, total = [], 0
         for i in range(args.warmup + args.steps):
-            secs, total, records = 0.0, 0, 0
+            secs, total, records, members = 0.0, 0, 0, 0
             for name, _, bgzf in files:
                 r = oracle.baseline_file(bgzf, fmt[name], threads)
                 secs, total, records = secs + r.seconds, total + r.inflated_bytes, records + r.records
+                members += r.members
             if i >= args.warmup:
                 times.append(secs)
         gbs = total * len(times) / sum(times) / 1e9
         line = {"impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * sum(times) / len(times), 3),
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-                "config": {"workload": args.workload, "description": MIXED[args.workload]["desc"],
-                           "inflated_bytes": total, "records": records},
+                "config": mixed_config(args.workload, members, sum(f[2].size for f in files), total, world),
                 "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                                 "cpu_model": cpu_model(), "nproc": threads, "records": records,
                                  "sample": "the three whole files per step; C restatement of the noodles CPU path "
                                            "(multithreaded BGZF inflate + serial scan/decode per format)"},
-                "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                        "note": "a CPU arm: the input and the columns stay in host memory, so no copy is declared"}}
         print(json.dumps(line), flush=True)
         return
     bgzf = generate(args.workload)
@@ -294,12 +450,13 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * total / len(times), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"],
-                   "records": res.records, "inflated_bytes": res.inflated_bytes, "members": res.members},
+        "config": bam_config(args.workload, res.records, res.members, len(bgzf), res.inflated_bytes, world),
         "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+                         "cpu_model": cpu_model(), "nproc": threads,
                          "sample": "whole file per step; C restatement of the noodles CPU path (the reference's "
                                    "Rust CPU path cannot be built here: no Rust toolchain)"},
-        "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "note": "a CPU arm: the input and the columns stay in host memory, so no copy is declared"},
     }
     print(json.dumps(line), flush=True)
 
@@ -529,16 +686,34 @@ def run_ours(args, rank, world, local):
 
     plain = None
     if not args.no_plain:
-        run_plain(frt, hbuf)  # warm
-        recs, infl, dt, batches = run_plain(frt, hbuf)
-        plain = {"value": round(infl / dt / 1e9, 3), "unit": "GB/s", "records": recs, "batches": batches,
-                 "members_per_batch": 256, "note": "per-batch reader+decoder from pinned host memory; "
-                                                  "compare with e2e",
-                 "batched_e2e_over_plain": round((inflated / e2e_s) / (infl / dt), 2)}
+        sweep = []
+        for bpb in PLAIN_BATCHES:
+            run_plain(frt, hbuf, bpb)  # warm
+            recs, infl, dt, batches = run_plain(frt, hbuf, bpb)
+            # the file's inflated bytes (members carried into the next batch
+            # are inflated twice; that work is not counted as output)
+            sweep.append({"members_per_batch": bpb, "value": round(inflated / dt / 1e9, 3), "batches": batches,
+                          "records": recs, "reinflated_bytes": int(infl - inflated)})
+        head = sweep[0]
+        plain = {"value": head["value"], "unit": "GB/s", "records": head["records"], "batches": head["batches"],
+                 "members_per_batch": PLAIN_BATCHES[0], "note": "per-batch reader+decoder from pinned host memory; "
+                                                                "compare with e2e",
+                 "batched_e2e_over_plain": round((inflated / e2e_s) / (head["value"] * 1e9), 2),
+                 "sweep": sweep,
+                 "sweep_note": "the same loop with larger batches (more members in flight per launch): what the "
+                               "batch size alone buys, against what the persistent kernel, the sorted queue and "
+                               "the graph add on top"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(bgzf, inflated)
+    parity = ref_cu = None
+    if rank == 0:
+        want, error, oracle_s = oracle_bam(st, bgzf)
+        parity = parity_bam(eng, st, want, error, oracle_s)
+        if not args.no_plain:
+            ref_cu = reference_cuda(hbuf, want, inflated)
+        del want
 
     if rank == 0:
         w = WORKLOADS[args.workload]
@@ -546,17 +721,16 @@ def run_ours(args, rank, world, local):
             "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": {"workload": args.workload, "description": w["desc"], "records": st.records,
-                       "members": st.members, "compressed_bytes": len(bgzf), "inflated_bytes": inflated,
-                       "aux_fields": st.aux_fields, "column_bytes": col_bytes, "speculation_fallbacks": st.fallbacks,
-                       "l2": "inputs larger than L2 (no flush)", "queue": "sorted by compressed size",
-                       "graph": True, "parallelism": f"replicas x{world}",
-                       "records_per_s": round(world * st.records * args.steps / (ms / 1e3), 1),
-                       "tuning": tuning},
+            "config": bam_config(args.workload, st.records, st.members, len(bgzf), inflated, world),
+            "engine": {"aux_fields": st.aux_fields, "column_bytes": col_bytes, "speculation_fallbacks": st.fallbacks,
+                       "queue": "sorted by compressed size", "graph": True,
+                       "records_per_s": round(world * st.records * args.steps / (ms / 1e3), 1), "tuning": tuning},
+            "parity": parity,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "plain": plain,
+            "reference_cuda": ref_cu,
             "record_fields": fields,
             "write_side": write,
             "gpu_launches": eng.launches_per_run() * args.steps,
@@ -564,8 +738,72 @@ def run_ours(args, rank, world, local):
             "wall_s": round(wall, 3),
         }
         print(json.dumps(line), flush=True)
+        if parity is not None and not parity["match"]:
+            print(f"parity mismatch: {parity['mismatch']}", file=sys.stderr, flush=True)
+            sys.exit(1)
     if dist:
         dist.destroy_process_group()
+
+
+def parity_mixed(eng, files) -> dict:
+    """Bit-exactness of the mixed-format run at its full size: each file's
+    inflated bytes and every column of its decoder against the oracle (the
+    threaded inflate with CRC32/ISIZE checks, then the format's CPU scan and
+    decode).  Runs after the timed region."""
+    import numpy as np
+
+    from oracle import oracle
+
+    t0 = time.perf_counter()
+    threads = os.cpu_count() or 1
+    ptr, _ = eng.inflated_ptr()
+    bad, per = [], {}
+    for i, (name, _, bgzf) in enumerate(files):
+        info = eng.file_info(i)
+        try:
+            raw = oracle.inflate_file(bgzf, threads, int(info.inflated_bytes))
+        except RuntimeError as e:
+            bad.append(f"{name}: {e}")
+            continue
+        if not same_bytes(ptr + int(info.inflated_offset), int(info.inflated_bytes), raw):
+            bad.append(f"{name}: inflated bytes")
+        res = eng.file_result(i)
+        if name == "bcf":
+            rs, ns, nc = oracle.bcf_header(raw)
+            want = oracle.bcf_decode(raw, rs, ns, nc)
+            cols, tail, n = want["columns"], want["tail"], len(want["columns"]["position"])
+        elif name == "fastq":
+            want = oracle.fastq_decode(raw, 0, cap=4 * int(info.records) + 1024)
+            cols, tail, n = want["columns"], want["tail"], len(want["columns"]["record_offsets"])
+        else:
+            want = oracle.fasta_compact(raw, cap=int(info.records) + 1024)
+            cols = {k: want[k] for k in ("sequence", "sequence_offsets", "sequence_lengths", "record_offsets")}
+            tail, n = want["sequence"].size, len(want["record_offsets"])
+        if info.records != n:
+            bad.append(f"{name}: record count")
+        if info.tail != tail:
+            bad.append(f"{name}: tail")
+        for k, v in cols.items():
+            if k == "sequence":
+                p, nb, _ = res.column_ptr(k)
+                ok = same_bytes(p, nb, v)
+            else:
+                ok = np.array_equal(res.column(k), v)
+            if not ok:
+                bad.append(f"{name}: {k}")
+        per[name] = {"records": int(n), "columns": len(cols), "inflated_bytes": int(raw.size)}
+        del raw, want, cols
+    return {"checked": True, "match": not bad, "files": per, "columns": sum(v["columns"] for v in per.values()),
+            "mismatch": bad, "seconds": round(time.perf_counter() - t0, 1),
+            "against": "oracle: threaded zlib inflate + CRC32/ISIZE of every member, then the reference's CPU scan "
+                       "and decode per format (BCF chain + site core, FASTQ scan + bounds, FASTA compaction)"}
+
+
+def mixed_config(workload: str, members: int, compressed: int, inflated: int, world: int) -> dict:
+    """The mixed workload as both arms report it (the same keys and values)."""
+    return {"workload": workload, "description": MIXED[workload]["desc"], "members": int(members),
+            "compressed_bytes": int(compressed), "inflated_bytes": int(inflated),
+            "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"}
 
 
 def generate_mixed(name: str):
@@ -774,17 +1012,18 @@ def run_mixed(args, rank, world, local):
                "sample": f"whole files: {parts}; C restatement of the noodles multithreaded BGZF reader (zlib 1.3 "
                          f"inflate + CRC32 on all cores) then the reference's serial CPU scan/decode per format"}
 
+    parity = parity_mixed(eng, files) if rank == 0 else None
+
     if rank == 0:
         w = MIXED[args.workload]
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-            "config": {"workload": args.workload, "description": w["desc"], "members": st.members,
-                       "compressed_bytes": int(blob.size), "inflated_bytes": int(inflated), "records": int(st.records),
-                       "column_bytes": int(col_bytes), "files": per, "l2": "inputs larger than L2 (no flush)",
-                       "queue": "sorted by compressed size", "graph": "discovery + plan + inflate",
-                       "parallelism": f"replicas x{world}", "tuning": tuning},
+            "config": mixed_config(args.workload, st.members, blob.size, inflated, world),
+            "engine": {"records": int(st.records), "column_bytes": int(col_bytes), "files": per,
+                       "queue": "sorted by compressed size", "graph": "discovery + plan + inflate", "tuning": tuning},
+            "parity": parity,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
@@ -794,6 +1033,9 @@ def run_mixed(args, rank, world, local):
             "wall_s": round(wall, 3),
         }
         print(json.dumps(line), flush=True)
+        if not parity["match"]:
+            print(f"parity mismatch: {parity['mismatch']}", file=sys.stderr, flush=True)
+            sys.exit(1)
     if dist:
         dist.destroy_process_group()
 

@@ -149,7 +149,7 @@ class InflateTuning(C.Structure):
 
 class InflateVariant(C.Structure):
     _fields_ = [("lit_bits", C.c_int32), ("dist_bits", C.c_int32), ("window", C.c_int32), ("queue", C.c_int32),
-                ("max_registers", C.c_int32), ("smem_per_warp", C.c_uint64)]
+                ("max_registers", C.c_int32), ("chains", C.c_int32), ("smem_per_warp", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

@@ -548,37 +548,49 @@ __device__ __forceinline__ int slow_symbol(WarpSmem<C> *sm, LaneBits &r, u32 pos
     return 0;
 }
 
-// One window of a Huffman block.  Lane 0 walks the serial chain -- one
-// table lookup and one shift per symbol, literals into the window buffer,
-// matches into the queue -- until the buffer or the queue is full or the
-// block ends; the warp then resolves the queued matches in parallel rounds
-// and writes the window to HBM with its CRC.  Truncation is checked once per
+// The serial part of one window of a Huffman block, run by the lane that
+// holds the member's reader: one table lookup and one shift per symbol,
+// literals into the window buffer, matches into the queue, until the buffer
+// or the queue is full or the block ends.  Truncation is checked once per
 // burst: bits past the payload read as zero, and a symbol that used one is
-// where a sequential decoder reports it.
+// where a sequential decoder reports it.  Sets o (bytes), nq (matches),
+// status and eob.
+template <class C>
+__device__ __forceinline__ void decode_symbols(WarpSmem<C> *sm, LaneBits &r, u32 total, u32 pos, u32 cap, u32 &o,
+                                               u32 &nq, u32 &status, int &eob)
+{
+    constexpr u32 WB = C::WB, MAXQ = C::MAXQ;
+    o = 0;
+    nq = 0;
+    status = INF_OK;
+    eob = 0;
+    // below lim every symbol fits the window and the declared size
+    const u32 room = cap - pos;
+    const u32 lim = room >= WB ? WB - 258u : (room > 258u ? room - 258u : 0u);
+    while (o < WB - 258u && nq < MAXQ) {
+        if (o < lim) {
+            fast_run(sm, r, pos, lim, o, nq);
+            if (o >= WB - 258u || nq >= MAXQ) break;
+        }
+        const int rc = slow_symbol(sm, r, pos, cap, o, nq, status);
+        if (rc == 1) eob = 1;
+        if (rc != 0) break;
+    }
+    if (r.tell() > total) status = INF_TRUNCATED; // a symbol needed bits past the payload
+}
+
+// One window of a Huffman block.  Lane 0 walks the serial chain
+// (decode_symbols); the warp then resolves the queued matches in parallel
+// rounds and writes the window to HBM with its CRC.
 template <class C>
 __device__ u32 decode_burst(WarpSmem<C> *sm, LaneBits &r, u32 total, u8 *out, u32 *pos_io, u32 cap, u32 *crc,
                             int *eob_out)
 {
-    constexpr u32 WB = C::WB, MAXQ = C::MAXQ;
     const u32 lane = lane_id();
     const u32 pos = *pos_io;
     u32 o = 0, nq = 0, status = INF_OK;
     int eob = 0;
-    if (lane == 0) {
-        // below lim every symbol fits the window and the declared size
-        const u32 room = cap - pos;
-        const u32 lim = room >= WB ? WB - 258u : (room > 258u ? room - 258u : 0u);
-        while (o < WB - 258u && nq < MAXQ) {
-            if (o < lim) {
-                fast_run(sm, r, pos, lim, o, nq);
-                if (o >= WB - 258u || nq >= MAXQ) break;
-            }
-            const int rc = slow_symbol(sm, r, pos, cap, o, nq, status);
-            if (rc == 1) eob = 1;
-            if (rc != 0) break;
-        }
-        if (r.tell() > total) status = INF_TRUNCATED; // a symbol needed bits past the payload
-    }
+    if (lane == 0) decode_symbols(sm, r, total, pos, cap, o, nq, status, eob);
     status = __shfl_sync(FRT_FULL_MASK, status, 0);
     *eob_out = __shfl_sync(FRT_FULL_MASK, eob, 0);
     o = __shfl_sync(FRT_FULL_MASK, o, 0);
@@ -591,11 +603,16 @@ __device__ u32 decode_burst(WarpSmem<C> *sm, LaneBits &r, u32 total, u8 *out, u3
     return INF_OK;
 }
 
-// Inflates one member with the calling warp into out[0, cap).  Returns the
-// status; *produced_out and *crc_out are valid in every lane.
+// The block starting at bit `bitpos` of a member, up to its first symbol, by
+// the whole warp; lane `leader` holds the member's reader and does the serial
+// parts.  A stored block is copied whole (its bytes written and folded into
+// the CRC; pos, crc and bitpos advance past it).  A Huffman block gets its
+// tables built in sm, bitpos moves past its header and the leader's reader is
+// placed at the first symbol (*huffman set).  *last is the block's BFINAL.
+// Returns the status; every output is warp-uniform.
 template <class C>
-__device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, WarpSmem<C> *sm, u32 *produced_out,
-                                   u32 *crc_out)
+__device__ __forceinline__ u32 block_header(WarpSmem<C> *sm, LaneBits &r, const u8 *in, u32 in_len, u8 *out, u32 cap, u32 &pos,
+                            u32 &crc, u32 &bitpos, int *last_out, bool *huffman, const u32 leader)
 {
     constexpr int LIT_BITS = C::LIT_BITS, DIST_BITS = C::DIST_BITS;
     constexpr u32 DIST_BASE = C::DIST_BASE, WB = C::WB;
@@ -604,6 +621,176 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, W
     // symbol, while the window buffer holds nothing: they live there.
     static_assert(C::WB >= 320, "the code lengths fit the window buffer");
     u8 *const lens = sm->win;
+    const u32 lane = lane_id();
+    const u32 total = 8u * in_len;
+    u32 status = INF_OK;
+    int type = 0, last = 0;
+    *huffman = false;
+    if (lane == leader) {
+        if (bitpos + 3 > total) {
+            status = INF_TRUNCATED;
+        } else {
+            r.seek(bitpos);
+            last = (int)r.peek(1);
+            type = (int)((r.buf >> 1) & 3u);
+        }
+    }
+    status = __shfl_sync(FRT_FULL_MASK, status, leader);
+    type = __shfl_sync(FRT_FULL_MASK, type, leader);
+    last = __shfl_sync(FRT_FULL_MASK, last, leader);
+    *last_out = last;
+    if (status != INF_OK) return status;
+    bitpos += 3;
+    if (type == 3) return INF_BLOCK_TYPE;
+
+    if (type == 0) {
+        // ---- stored block: copied by the whole warp -----------------------
+        u32 bytepos = (bitpos + 7) / 8, len = 0;
+        if (lane == leader) {
+            if (bytepos + 4 > in_len) {
+                status = INF_TRUNCATED;
+            } else {
+                u32 l = (u32)in[bytepos] | ((u32)in[bytepos + 1] << 8);
+                u32 nl = (u32)in[bytepos + 2] | ((u32)in[bytepos + 3] << 8);
+                if (l != (~nl & 0xffffu)) status = INF_STORED_LEN;
+                else if (bytepos + 4 + l > in_len) status = INF_TRUNCATED;
+                else if (pos + l > cap) status = INF_OUTPUT_OVERFLOW;
+                len = l;
+            }
+        }
+        status = __shfl_sync(FRT_FULL_MASK, status, leader);
+        if (status != INF_OK) return status;
+        len = __shfl_sync(FRT_FULL_MASK, len, leader);
+        const u8 *src = in + bytepos + 4;
+        bitpos = 8u * (bytepos + 4 + len);
+        while (len) {
+            u32 n = min(len, WB);
+            for (u32 j = lane; j < n; j += 32) sm->win[j] = src[j];
+            __syncwarp();
+            write_window(sm, out, pos, n, &crc);
+            pos += n;
+            src += n;
+            len -= n;
+        }
+        return INF_OK;
+    }
+
+    // ---- Huffman block: tables ------------------------------------------
+    if (type == 1) {
+        for (int s = lane; s < 288; s += 32) lens[s] = s < 144 ? 8 : (s < 256 ? 9 : (s < 280 ? 7 : 8));
+        __syncwarp();
+        build_table(lens, 288, LIT_BITS, sm->tab, sm->lsorted, &sm->lcode, sm->run, 0);
+        lens[lane] = 5;
+        __syncwarp();
+        build_table(lens, 32, DIST_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode, sm->run, 1);
+    } else {
+        int nlen = 0, ndist = 0, ncode = 0;
+        u32 bp = bitpos;
+        if (lane == leader) {
+            if (bp + 14 > total) {
+                status = INF_TRUNCATED;
+            } else {
+                r.seek(bp);
+                nlen = (int)r.peek(5) + 257;
+                ndist = (int)((r.buf >> 5) & 31u) + 1;
+                ncode = (int)((r.buf >> 10) & 15u) + 4;
+                r.drop(14);
+                if (nlen > 286 || ndist > 30) status = INF_BAD_COUNTS;
+            }
+            if (status == INF_OK) {
+                // the code-length code lengths arrive in this permuted order
+                const u8 order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
+                for (int i = 0; i < 19; ++i) lens[order[i]] = 0;
+                for (int i = 0; i < ncode; ++i) {
+                    r.refill();
+                    if (r.tell() + 3 > total) {
+                        status = INF_TRUNCATED;
+                        break;
+                    }
+                    lens[order[i]] = (u8)r.peek(3);
+                    r.drop(3);
+                }
+            }
+            bp = r.tell();
+        }
+        status = __shfl_sync(FRT_FULL_MASK, status, leader);
+        if (status != INF_OK) return status;
+        nlen = __shfl_sync(FRT_FULL_MASK, nlen, leader);
+        ndist = __shfl_sync(FRT_FULL_MASK, ndist, leader);
+        __syncwarp();
+        // the code-length code must be complete (all-zero counts as
+        // complete and fails at first use, as in the reference)
+        if (build_table(lens, 19, CL_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode, sm->run, 2) != 0)
+            return INF_BAD_TABLE;
+        if (lane == leader) {
+            int index = 0;
+            r.seek(bp);
+            while (index < nlen + ndist) {
+                r.refill();
+                u32 e = sm->tab[DIST_BASE + r.peek(CL_BITS)];
+                u32 L = e & 31u;
+                u32 left = total - min(total, r.tell());
+                if (L == 0) {
+                    status = left < 15 ? INF_TRUNCATED : INF_BAD_CODE;
+                    break;
+                }
+                if (L > left) {
+                    status = INF_TRUNCATED;
+                    break;
+                }
+                r.drop((int)L);
+                u32 sym = e >> 16;
+                if (sym < 16) {
+                    lens[index++] = (u8)sym;
+                    continue;
+                }
+                u32 val = 0;
+                u32 nb = sym == 16 ? 2 : (sym == 17 ? 3 : 7);
+                if (sym == 16) {
+                    if (index == 0) {
+                        status = INF_BAD_LENGTH_REPEAT;
+                        break;
+                    }
+                    val = lens[index - 1];
+                }
+                if (r.tell() + nb > total) {
+                    status = INF_TRUNCATED;
+                    break;
+                }
+                u32 rep = (sym == 18 ? 11u : 3u) + r.peek((int)nb);
+                r.drop((int)nb);
+                if (index + (int)rep > nlen + ndist) {
+                    status = INF_BAD_LENGTH_REPEAT;
+                    break;
+                }
+                while (rep--) lens[index++] = (u8)val;
+            }
+            if (status == INF_OK && lens[256] == 0) status = INF_BAD_TABLE;
+            bp = r.tell();
+        }
+        status = __shfl_sync(FRT_FULL_MASK, status, leader);
+        if (status != INF_OK) return status;
+        bitpos = __shfl_sync(FRT_FULL_MASK, bp, leader);
+        __syncwarp();
+        int rl = build_table(lens, nlen, LIT_BITS, sm->tab, sm->lsorted, &sm->lcode, sm->run, 0);
+        if (rl != 0 && (rl < 0 || nlen != (int)sm->lcode.count[0] + 1)) // incomplete only with one code
+            return INF_BAD_TABLE;
+        int rd = build_table(lens + nlen, ndist, DIST_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode, sm->run,
+                             1);
+        if (rd != 0 && (rd < 0 || ndist != (int)sm->dcode.count[0] + 1)) return INF_BAD_TABLE;
+    }
+    if (lane == leader) r.seek(bitpos);
+    *huffman = true;
+    return INF_OK;
+}
+
+// Inflates one member with the calling warp into out[0, cap).  Returns the
+// status; *produced_out and *crc_out are valid in every lane.
+template <class C>
+__device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, WarpSmem<C> *sm, u32 *produced_out,
+                                   u32 *crc_out)
+{
+    constexpr u32 WB = C::WB;
     const u32 lane = lane_id();
     LaneBits r;
     r.attach(in, in_len);
@@ -614,185 +801,22 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, W
     u32 pos = 0;    // bytes produced and written
     u32 crc = 0;    // CRC-32 of [0, pos)
     u32 status = INF_OK;
-    int last = 0;
-
     while (true) {
-        int type = 0;
-        if (lane == 0) {
-            if (bitpos + 3 > total) {
-                status = INF_TRUNCATED;
-            } else {
-                r.seek(bitpos);
-                last = (int)r.peek(1);
-                type = (int)((r.buf >> 1) & 3u);
-            }
-        }
-        status = __shfl_sync(FRT_FULL_MASK, status, 0);
+        int last = 0;
+        bool huffman = false;
+        status = block_header(sm, r, in, in_len, out, cap, pos, crc, bitpos, &last, &huffman, 0u);
         if (status != INF_OK) break;
-        type = __shfl_sync(FRT_FULL_MASK, type, 0);
-        last = __shfl_sync(FRT_FULL_MASK, last, 0);
-        bitpos += 3;
-        if (type == 3) {
-            status = INF_BLOCK_TYPE;
-            break;
-        }
-
-        if (type == 0) {
-            // ---- stored block: copied by the whole warp -----------------------
-            u32 bytepos = (bitpos + 7) / 8, len = 0;
-            if (lane == 0) {
-                if (bytepos + 4 > in_len) {
-                    status = INF_TRUNCATED;
-                } else {
-                    u32 l = (u32)in[bytepos] | ((u32)in[bytepos + 1] << 8);
-                    u32 nl = (u32)in[bytepos + 2] | ((u32)in[bytepos + 3] << 8);
-                    if (l != (~nl & 0xffffu)) status = INF_STORED_LEN;
-                    else if (bytepos + 4 + l > in_len) status = INF_TRUNCATED;
-                    else if (pos + l > cap) status = INF_OUTPUT_OVERFLOW;
-                    len = l;
-                }
+        if (huffman) {
+            // ---- Huffman block: symbols, a window at a time -----------------
+            while (true) {
+                int eob = 0;
+                status = decode_burst(sm, r, total, out, &pos, cap, &crc, &eob);
+                if (status != INF_OK || eob) break;
             }
-            status = __shfl_sync(FRT_FULL_MASK, status, 0);
             if (status != INF_OK) break;
-            len = __shfl_sync(FRT_FULL_MASK, len, 0);
-            const u8 *src = in + bytepos + 4;
-            bitpos = 8u * (bytepos + 4 + len);
-            while (len) {
-                u32 n = min(len, WB);
-                for (u32 j = lane; j < n; j += 32) sm->win[j] = src[j];
-                __syncwarp();
-                write_window(sm, out, pos, n, &crc);
-                pos += n;
-                src += n;
-                len -= n;
-            }
-            if (last) break;
-            continue;
+            if (lane == 0) bitpos = r.tell();
+            bitpos = __shfl_sync(FRT_FULL_MASK, bitpos, 0);
         }
-
-        // ---- Huffman block: tables ------------------------------------------
-        if (type == 1) {
-            for (int s = lane; s < 288; s += 32) lens[s] = s < 144 ? 8 : (s < 256 ? 9 : (s < 280 ? 7 : 8));
-            __syncwarp();
-            build_table(lens, 288, LIT_BITS, sm->tab, sm->lsorted, &sm->lcode, sm->run, 0);
-            lens[lane] = 5;
-            __syncwarp();
-            build_table(lens, 32, DIST_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode, sm->run, 1);
-        } else {
-            int nlen = 0, ndist = 0, ncode = 0;
-            u32 bp = bitpos;
-            if (lane == 0) {
-                if (bp + 14 > total) {
-                    status = INF_TRUNCATED;
-                } else {
-                    r.seek(bp);
-                    nlen = (int)r.peek(5) + 257;
-                    ndist = (int)((r.buf >> 5) & 31u) + 1;
-                    ncode = (int)((r.buf >> 10) & 15u) + 4;
-                    r.drop(14);
-                    if (nlen > 286 || ndist > 30) status = INF_BAD_COUNTS;
-                }
-                if (status == INF_OK) {
-                    // the code-length code lengths arrive in this permuted order
-                    const u8 order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
-                    for (int i = 0; i < 19; ++i) lens[order[i]] = 0;
-                    for (int i = 0; i < ncode; ++i) {
-                        r.refill();
-                        if (r.tell() + 3 > total) {
-                            status = INF_TRUNCATED;
-                            break;
-                        }
-                        lens[order[i]] = (u8)r.peek(3);
-                        r.drop(3);
-                    }
-                }
-                bp = r.tell();
-            }
-            status = __shfl_sync(FRT_FULL_MASK, status, 0);
-            if (status != INF_OK) break;
-            nlen = __shfl_sync(FRT_FULL_MASK, nlen, 0);
-            ndist = __shfl_sync(FRT_FULL_MASK, ndist, 0);
-            __syncwarp();
-            // the code-length code must be complete (all-zero counts as
-            // complete and fails at first use, as in the reference)
-            if (build_table(lens, 19, CL_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode, sm->run, 2) != 0) {
-                status = INF_BAD_TABLE;
-                break;
-            }
-            if (lane == 0) {
-                int index = 0;
-                r.seek(bp);
-                while (index < nlen + ndist) {
-                    r.refill();
-                    u32 e = sm->tab[DIST_BASE + r.peek(CL_BITS)];
-                    u32 L = e & 31u;
-                    u32 left = total - min(total, r.tell());
-                    if (L == 0) {
-                        status = left < 15 ? INF_TRUNCATED : INF_BAD_CODE;
-                        break;
-                    }
-                    if (L > left) {
-                        status = INF_TRUNCATED;
-                        break;
-                    }
-                    r.drop((int)L);
-                    u32 sym = e >> 16;
-                    if (sym < 16) {
-                        lens[index++] = (u8)sym;
-                        continue;
-                    }
-                    u32 val = 0;
-                    u32 nb = sym == 16 ? 2 : (sym == 17 ? 3 : 7);
-                    if (sym == 16) {
-                        if (index == 0) {
-                            status = INF_BAD_LENGTH_REPEAT;
-                            break;
-                        }
-                        val = lens[index - 1];
-                    }
-                    if (r.tell() + nb > total) {
-                        status = INF_TRUNCATED;
-                        break;
-                    }
-                    u32 rep = (sym == 18 ? 11u : 3u) + r.peek((int)nb);
-                    r.drop((int)nb);
-                    if (index + (int)rep > nlen + ndist) {
-                        status = INF_BAD_LENGTH_REPEAT;
-                        break;
-                    }
-                    while (rep--) lens[index++] = (u8)val;
-                }
-                if (status == INF_OK && lens[256] == 0) status = INF_BAD_TABLE;
-                bp = r.tell();
-            }
-            status = __shfl_sync(FRT_FULL_MASK, status, 0);
-            if (status != INF_OK) break;
-            bitpos = __shfl_sync(FRT_FULL_MASK, bp, 0);
-            __syncwarp();
-            int rl = build_table(lens, nlen, LIT_BITS, sm->tab, sm->lsorted, &sm->lcode, sm->run, 0);
-            if (rl != 0 && (rl < 0 || nlen != (int)sm->lcode.count[0] + 1)) { // incomplete only with one code
-                status = INF_BAD_TABLE;
-                break;
-            }
-            int rd = build_table(lens + nlen, ndist, DIST_BITS, sm->tab + DIST_BASE, sm->dsorted, &sm->dcode,
-                                 sm->run, 1);
-            if (rd != 0 && (rd < 0 || ndist != (int)sm->dcode.count[0] + 1)) {
-                status = INF_BAD_TABLE;
-                break;
-            }
-        }
-
-        // ---- Huffman block: symbols, a window at a time ----------------------
-        if (lane == 0) r.seek(bitpos);
-        while (true) {
-            int eob = 0;
-            status = decode_burst(sm, r, total, out, &pos, cap, &crc, &eob);
-            if (status != INF_OK || eob) break;
-        }
-        if (status != INF_OK) break;
-        if (lane == 0) bitpos = r.tell();
-        bitpos = __shfl_sync(FRT_FULL_MASK, bitpos, 0);
-        if (status != INF_OK) break;
         if (last) break;
     }
     *produced_out = pos;
@@ -867,6 +891,215 @@ k_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out
     }
 }
 
+// ---- several chains per warp -------------------------------------------------
+// One lane walking one member's chain leaves 31 lanes of every instruction of
+// the decode loop idle.  The multi-chain form gives a warp K members: lanes
+// 0..K-1 each hold one member's reader and decode a window of symbols side by
+// side, so an instruction both (or all) take serves K symbols; a literal and a
+// match diverge, and SIMT runs both paths, but the common part is shared.  The
+// work that is not on the chain (block headers and tables, match resolution,
+// the coalesced window write and its CRC) stays warp-cooperative and goes one
+// member at a time.  Each member keeps its own tables, window buffer and
+// queue (K times the shared memory of the one-chain form per warp).
+
+enum : u32 { SLOT_EMPTY = 0, SLOT_HEADER = 1, SLOT_DECODE = 2, SLOT_DONE = 3 };
+
+// A member in flight in a multi-chain warp.  In shared memory: the
+// cooperative phases read every member's state.
+struct Slot {
+    const u8 *in;
+    u8 *out;
+    u32 m, in_len, cap;
+    u32 pos;    // bytes produced and written
+    u32 crc;    // CRC-32 of [0, pos)
+    u32 bitpos; // next unread bit at a block header
+    u32 status, phase;
+    u32 o, nq; // the last burst: bytes in the window buffer, queued matches
+    int last, eob;
+};
+
+template <class C, int K> __host__ __device__ constexpr size_t multi_slots_bytes()
+{
+    return (sizeof(Slot) * K + 15) & ~(size_t)15;
+}
+template <class C, int K> __host__ __device__ constexpr size_t multi_warp_bytes()
+{
+    return multi_slots_bytes<C, K>() + K * warp_smem_bytes<C>();
+}
+
+// K members per warp until no member is left.  PERSISTENT: members come from
+// the device work queue (one per pop) and are verified against their
+// trailers as they finish; otherwise slot s takes member first + s once.
+template <class C, int K, bool PERSISTENT>
+__device__ void inflate_multi(unsigned char *wbase, const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out,
+                              const u64 *out_off, const u32 *caps, const u32 *crc_expect, u32 *status, u32 *produced,
+                              u32 *crc, const u32 *order, u32 n, u64 out_capacity, u32 *queue_head,
+                              unsigned long long *block_err, u32 first)
+{
+    static_assert(K >= 2 && K <= 32, "chains per warp");
+    const u32 lane = lane_id();
+    Slot *slots = (Slot *)wbase;
+    WarpSmem<C> *sms = (WarpSmem<C> *)(wbase + multi_slots_bytes<C, K>());
+    constexpr u32 PW = C::WB / 32;
+    for (u32 w = lane; w < K * PW; w += 32) sms[w / PW].pend[w % PW] = 0;
+    if (lane < K) slots[lane].phase = SLOT_EMPTY;
+    LaneBits r; // lane s < K: the reader of slot s's member
+    bool more = true;
+    __syncwarp();
+    while (true) {
+        // 1. a member for every empty slot
+        if (more) {
+            bool exhausted = false;
+            if (lane < K && slots[lane].phase == SLOT_EMPTY) {
+                u32 m = 0xffffffffu;
+                if (PERSISTENT) {
+                    const u32 q = atomicAdd(queue_head, 1u);
+                    if (q < n) m = order ? order[q] : q;
+                    else exhausted = true;
+                } else {
+                    m = first + lane;
+                }
+                if (m < n) {
+                    Slot &S = slots[lane];
+                    const u32 cap = caps[m];
+                    S.m = m;
+                    S.in = in + in_off[m];
+                    S.in_len = in_len[m];
+                    S.out = out + out_off[m];
+                    S.cap = cap;
+                    S.pos = 0;
+                    S.crc = 0;
+                    S.bitpos = 0;
+                    S.last = 0;
+                    S.status = INF_OK;
+                    if (PERSISTENT && out_off[m] + cap > out_capacity) {
+                        S.status = INF_OUTPUT_OVERFLOW; // sizes changed since the buffers were planned
+                        S.phase = SLOT_DONE;
+                    } else {
+                        S.phase = SLOT_HEADER;
+                        r.attach(S.in, S.in_len);
+                    }
+                }
+            }
+            if (!PERSISTENT) more = false;
+            else if (__any_sync(FRT_FULL_MASK, exhausted)) more = false;
+        }
+        __syncwarp();
+        const u32 busy = __ballot_sync(FRT_FULL_MASK, lane < K && slots[lane].phase != SLOT_EMPTY);
+        if (!busy) {
+            if (!more) break;
+            continue;
+        }
+        // 2. block headers (and whole stored blocks), one member at a time
+        for (u32 t = __ballot_sync(FRT_FULL_MASK, lane < K && slots[lane].phase == SLOT_HEADER); t; t &= t - 1) {
+            const u32 s = __ffs(t) - 1;
+            Slot &S = slots[s];
+            u32 pos = S.pos, c = S.crc, bp = S.bitpos;
+            int last = 0;
+            bool huffman = false;
+            const u32 st = block_header(&sms[s], r, S.in, S.in_len, S.out, S.cap, pos, c, bp, &last, &huffman, s);
+            __syncwarp();
+            if (lane == 0) {
+                S.pos = pos;
+                S.crc = c;
+                S.bitpos = bp;
+                S.last = last;
+                S.status = st;
+                S.phase = st != INF_OK ? SLOT_DONE : (huffman ? SLOT_DECODE : (last ? SLOT_DONE : SLOT_HEADER));
+            }
+            __syncwarp();
+        }
+        // 3. a window of symbols for every decoding member, side by side
+        const u32 dec = __ballot_sync(FRT_FULL_MASK, lane < K && slots[lane].phase == SLOT_DECODE);
+        if ((dec >> lane) & 1u) {
+            Slot &S = slots[lane];
+            u32 o, nq, st;
+            int eob;
+            decode_symbols(&sms[lane], r, 8u * S.in_len, S.pos, S.cap, o, nq, st, eob);
+            S.o = o;
+            S.nq = nq;
+            S.status = st;
+            S.eob = eob;
+        }
+        __syncwarp();
+        // 4. each window's matches resolved and its bytes written, one member at a time
+        for (u32 t = dec; t; t &= t - 1) {
+            const u32 s = __ffs(t) - 1;
+            Slot &S = slots[s];
+            if (S.status == INF_OK) {
+                const u32 pos = S.pos, o = S.o;
+                u32 c = S.crc;
+                resolve(&sms[s], S.out, pos, S.nq);
+                write_window(&sms[s], S.out, pos, o, &c);
+                u32 bp = 0;
+                if (lane == s) bp = r.tell();
+                bp = __shfl_sync(FRT_FULL_MASK, bp, s);
+                const int eob = S.eob, last = S.last;
+                __syncwarp();
+                if (lane == 0) {
+                    S.pos = pos + o;
+                    S.crc = c;
+                    if (eob) {
+                        S.bitpos = bp;
+                        S.phase = last ? SLOT_DONE : SLOT_HEADER;
+                    }
+                }
+            } else {
+                __syncwarp();
+                if (lane == 0) S.phase = SLOT_DONE;
+            }
+            __syncwarp();
+        }
+        // 5. finished members: results and, in the batched form, the trailer check
+        if (lane < K && slots[lane].phase == SLOT_DONE) {
+            Slot &S = slots[lane];
+            const u32 m = S.m, st = S.status, p = S.pos, c = S.crc;
+            status[m] = st;
+            produced[m] = p;
+            crc[m] = st == INF_OK ? c : 0u;
+            if (PERSISTENT) {
+                const u32 cap = S.cap;
+                unsigned long long code = st != INF_OK ? 5ull : (p != cap ? 4ull : (c != crc_expect[m] ? 3ull : 0ull));
+                if (code) atomicMin(block_err, ((unsigned long long)m << 8) | code);
+            }
+            S.phase = SLOT_EMPTY;
+        }
+        __syncwarp();
+    }
+}
+
+// Plain form with K members per warp, members in span order.
+template <class C, int K>
+__global__ void __maxnreg__(C::REGS)
+k_inflate_members_multi(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out, const u64 *out_off,
+                        const u32 *out_cap, u32 *status, u32 *produced, u32 *crc, u32 n)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const u32 warp = threadIdx.x / 32;
+    const u32 first = (blockIdx.x * (blockDim.x / 32) + warp) * K;
+    if (first >= n) return;
+    inflate_multi<C, K, false>(smem + warp * multi_warp_bytes<C, K>(), in, in_off, in_len, out, out_off, out_cap,
+                               nullptr, status, produced, crc, nullptr, n, ~0ull, nullptr, nullptr, first);
+}
+
+// Batched form with K members per warp: the persistent grid of
+// k_inflate_persistent, each slot popping its own members (the chunk is one).
+template <class C, int K>
+__global__ void __maxnreg__(C::REGS)
+k_inflate_persistent_multi(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out, const u64 *out_off,
+                           const u32 *isize, const u32 *crc_expect, u32 *status, u32 *produced, u32 *crc,
+                           const u32 *order, const u64 *n_ptr, u64 n_cap, u64 out_capacity, u32 *queue_head,
+                           u32 chunk, unsigned long long *block_err)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    (void)chunk;
+    const u32 warp = threadIdx.x / 32;
+    u64 n64 = *n_ptr;
+    const u32 n = (u32)(n64 < n_cap ? n64 : n_cap);
+    inflate_multi<C, K, true>(smem + warp * multi_warp_bytes<C, K>(), in, in_off, in_len, out, out_off, isize,
+                              crc_expect, status, produced, crc, order, n, out_capacity, queue_head, block_err, 0u);
+}
+
 } // namespace
 
 // Standalone CRC of already-inflated members (the reference's crc32_blocks,
@@ -913,8 +1146,15 @@ struct Variant {
 
 template <class C> Variant make_variant()
 {
-    return {{C::LIT_BITS, C::DIST_BITS, (int32_t)C::WB, (int32_t)C::MAXQ, C::REGS, (uint64_t)warp_smem_bytes<C>()},
+    return {{C::LIT_BITS, C::DIST_BITS, (int32_t)C::WB, (int32_t)C::MAXQ, C::REGS, 1, (uint64_t)warp_smem_bytes<C>()},
             k_inflate_members<C>, k_inflate_persistent<C>};
+}
+
+template <class C, int K> Variant make_multi_variant()
+{
+    return {{C::LIT_BITS, C::DIST_BITS, (int32_t)C::WB, (int32_t)C::MAXQ, C::REGS, K,
+             (uint64_t)multi_warp_bytes<C, K>()},
+            k_inflate_members_multi<C, K>, k_inflate_persistent_multi<C, K>};
 }
 
 // The compiled variants: the table roots trade shared memory (members in
@@ -929,6 +1169,9 @@ const Variant kVariants[] = {
     make_variant<Cfg<9, 8, 2048, 384, 80>>(),  make_variant<Cfg<9, 7, 1024, 256, 80>>(),
     make_variant<Cfg<10, 8, 2048, 384, 80>>(), make_variant<Cfg<9, 7, 1024, 256, 72>>(),
     make_variant<Cfg<9, 7, 1024, 192, 64>>(), make_variant<Cfg<9, 7, 1024, 160, 56>>(),
+    // several chains per warp (the shared memory per warp is K members')
+    make_multi_variant<Cfg<9, 7, 1024, 192, 128>, 2>(), make_multi_variant<Cfg<9, 7, 1024, 192, 128>, 4>(),
+    make_multi_variant<Cfg<9, 7, 2048, 384, 128>, 4>(), make_multi_variant<Cfg<9, 7, 1024, 192, 128>, 8>(),
 };
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 
@@ -1044,8 +1287,8 @@ cudaError_t frt_launch_inflate_members(const u8 *in, const u64 *in_off, const u3
                                        u32 *crc, u32 n, const frt_inflate_tuning &t, cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
-    const u32 w = (u32)t.warps_per_cta;
-    kVariants[t.variant].members<<<(n + w - 1) / w, w * 32, frt_inflate_smem_bytes(t), s>>>(
+    const u32 w = (u32)t.warps_per_cta * (u32)kVariants[t.variant].info.chains; // members per CTA
+    kVariants[t.variant].members<<<(n + w - 1) / w, t.warps_per_cta * 32, frt_inflate_smem_bytes(t), s>>>(
         in, in_off, in_len, out, out_off, out_cap, status, produced, crc, n);
     return cudaGetLastError();
 }

@@ -320,6 +320,7 @@ uint32_t variant_set_hash()
         mix(info.window);
         mix(info.queue);
         mix(info.max_registers);
+        mix(info.chains);
         mix((int64_t)info.smem_per_warp);
     }
     return h;
@@ -367,7 +368,7 @@ Json tuning_json(const frt_inflate_tuning &t, double ms, double gbs, uint64_t me
     j.set("warps_per_cta", Json::number(t.warps_per_cta));
     j.set("ctas_per_sm", Json::number(t.ctas_per_sm));
     j.set("queue_chunk", Json::number(t.queue_chunk));
-    j.set("warps_per_member", Json::number(1));
+    j.set("chains", Json::number(info.chains));
     j.set("sample_members", Json::number((double)members));
     j.set("sample_ms", Json::number(ms));
     j.set("sample_gbs", Json::number(gbs));
@@ -389,16 +390,17 @@ bool tuning_from_json(const Json &j, frt_inflate_tuning *t)
         *v = x->num;
         return true;
     };
-    double v, w, c, q, lb, db, win, qu, mr;
+    double v, w, c, q, lb, db, win, qu, mr, ch = 1;
     if (!num("variant", &v) || !num("warps_per_cta", &w) || !num("ctas_per_sm", &c) || !num("queue_chunk", &q) ||
         !num("lit_bits", &lb) || !num("dist_bits", &db) || !num("window", &win) || !num("queue", &qu) ||
         !num("max_registers", &mr))
         return false;
+    num("chains", &ch); // entries written before multi-chain variants have one chain
     frt_inflate_variant info{};
     if (frt_inflate_variant_info((int32_t)v, &info, nullptr) != FRT_OK) return false;
     // the variant index must still name the same shape
     if (info.lit_bits != (int)lb || info.dist_bits != (int)db || info.window != (int)win || info.queue != (int)qu ||
-        info.max_registers != (int)mr)
+        info.max_registers != (int)mr || info.chains != (int)ch)
         return false;
     *t = frt_inflate_tuning{(int32_t)v, (int32_t)w, (int32_t)c, (int32_t)q};
     return true;

@@ -589,7 +589,7 @@ void frt_server_release(frt_server *s, uint64_t request);
  * set and workload class. */
 typedef struct {
     int32_t variant;       /* index of a compiled variant */
-    int32_t warps_per_cta; /* 1..8; one member per warp */
+    int32_t warps_per_cta; /* 1..8; each warp takes the variant's chains of members */
     int32_t ctas_per_sm;   /* 0: as many as fit */
     int32_t queue_chunk;   /* members per queue pop, 1..64 */
 } frt_inflate_tuning;
@@ -600,6 +600,7 @@ typedef struct {
     int32_t window;         /* window buffer per warp, bytes */
     int32_t queue;          /* matches queued per window */
     int32_t max_registers;  /* register cap per thread */
+    int32_t chains;         /* members a warp decodes side by side, one lane each */
     uint64_t smem_per_warp; /* shared memory per warp, bytes */
 } frt_inflate_variant;
 

@@ -16,7 +16,7 @@ from oracle.build import REF_CUBIN, build_ref_cuda
 
 class RefCudaResult(C.Structure):
     _fields_ = [("records", C.c_uint64), ("inflated_bytes", C.c_uint64), ("members", C.c_uint64),
-                ("batches", C.c_uint64), ("seconds", C.c_double), ("inflate_ms", C.c_double),
+                ("consumed_bytes", C.c_uint64), ("batches", C.c_uint64), ("seconds", C.c_double), ("inflate_ms", C.c_double),
                 ("reconcile_ms", C.c_double), ("kernels_ms", C.c_double), ("status", C.c_int32)]
 
 
@@ -47,7 +47,7 @@ def _load():
             raise RuntimeError("no reference cubin")
         lib = C.CDLL(str(path))
         lib.refcu_open.argtypes = [C.c_char_p, C.c_int]
-        lib.refcu_run_bam.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_void_p, C.c_void_p]
+        lib.refcu_run_bam.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint64, C.c_void_p, C.c_void_p]
         lib.refcu_last_error.restype = C.c_char_p
         if lib.refcu_open(str(REF_CUBIN).encode(), 0):
             raise RuntimeError(lib.refcu_last_error().decode())
@@ -55,11 +55,13 @@ def _load():
     return _lib
 
 
-def run_bam(bgzf: np.ndarray, blocks_per_batch: int = 256, columns_cap: int = 0):
+def run_bam(bgzf: np.ndarray, blocks_per_batch: int = 256, columns_cap: int = 0, stop_after: int = 0):
     """The reference's reader + CudaCodec + BamDecoder loop over a whole BGZF
-    BAM in host memory.  Returns (result, columns or None); with columns_cap
-    the record offsets (whole-file inflated coordinates), ref_id, pos, flags
-    and seq_len come back for comparison with the oracle."""
+    BAM in host memory (with stop_after, only the batches that start before
+    that compressed offset: a bounded sample).  Returns (result, columns or
+    None); with columns_cap the record offsets (whole-file inflated
+    coordinates), ref_id, pos, flags and seq_len come back for comparison
+    with the oracle."""
     lib = _load()
     b = np.ascontiguousarray(bgzf, dtype=np.uint8)
     res = RefCudaResult()
@@ -71,7 +73,7 @@ def run_bam(bgzf: np.ndarray, blocks_per_batch: int = 256, columns_cap: int = 0)
                 "seq_len": np.zeros(columns_cap, np.uint32)}
         spec = RefCudaColumns(*(cols[k].ctypes.data for k in ("record_offsets", "ref_id", "pos", "flags",
                                                                "seq_len")), columns_cap)
-    rc = lib.refcu_run_bam(b.ctypes.data, b.size, blocks_per_batch, C.byref(res),
+    rc = lib.refcu_run_bam(b.ctypes.data, b.size, blocks_per_batch, stop_after, C.byref(res),
                            C.byref(spec) if spec is not None else None)
     if rc:
         raise RuntimeError(f"reference CUDA path failed ({rc}): {lib.refcu_last_error().decode()}")

@@ -85,6 +85,7 @@ typedef struct {
     uint64_t records;
     uint64_t inflated_bytes;
     uint64_t members;    /* members inflated, counting re-inflated carries */
+    uint64_t consumed_bytes; /* inflated bytes consumed once (the carried member's bytes count in the next batch) */
     uint64_t batches;
     double seconds;      /* wall time of the whole loop */
     double inflate_ms;   /* inflate_blocks kernel time, summed over batches (CUDA events) */
@@ -121,8 +122,11 @@ int refcu_open(const char *cubin_path, int device)
     return 0;
 }
 
-int refcu_run_bam(const uint8_t *file, uint64_t len, uint32_t blocks_per_batch, refcu_result *res,
-                  const refcu_columns *cols)
+/* Runs the loop over the file; with stop_after > 0 the consumer stops once
+ * the next batch would start at or past that compressed offset (a bounded
+ * sample of the file). */
+int refcu_run_bam(const uint8_t *file, uint64_t len, uint32_t blocks_per_batch, uint64_t stop_after,
+                  refcu_result *res, const refcu_columns *cols)
 {
     memset(res, 0, sizeof *res);
     if (!g_mod.mod) {
@@ -168,6 +172,7 @@ int refcu_run_bam(const uint8_t *file, uint64_t len, uint32_t blocks_per_batch, 
     uint64_t prev_start = UINT64_MAX, prev_end = 0; // the last window inflated
     while (!status) {
         if (batch_offset >= len) break;
+        if (stop_after && batch_offset >= stop_after) break;
         // nothing new can be read and the window would be rebuilt identically:
         // the stream ends inside a record (device_read.rs:190-203)
         if (read_pos >= len && batch_offset == prev_start && prev_end == len) {
@@ -365,8 +370,10 @@ int refcu_run_bam(const uint8_t *file, uint64_t len, uint32_t blocks_per_batch, 
             while (b + 1 < n && out_off[b + 1] <= tail) ++b;
             batch_offset = spans[b].compressed_offset;
             carry_start = tail - out_off[b];
+            res->consumed_bytes += out_off[b];
         } else {
             batch_offset = after_members;
+            res->consumed_bytes += total;
         }
     }
     cudaStreamSynchronize(st);

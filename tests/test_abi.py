@@ -153,4 +153,4 @@ def test_shipped_tuning_cache_names_compiled_variants():
         v = vs[e["variant"]]
         assert (e["lit_bits"], e["dist_bits"], e["window"], e["queue"], e["max_registers"]) == (
             v["lit_bits"], v["dist_bits"], v["window"], v["queue"], v["max_registers"]), key
-        assert 1 <= e["warps_per_cta"] <= 8 and 1 <= e["queue_chunk"] <= 64 and e["warps_per_member"] == 1
+        assert 1 <= e["warps_per_cta"] <= 8 and 1 <= e["queue_chunk"] <= 64 and e.get("chains", 1) >= 1

@@ -164,3 +164,75 @@ def test_autotune_caches_and_reads_back(frt, bam, tmp_path):
     doc2["entries"][first["key"]]["lit_bits"] = 3
     cache.write_text(json.dumps(doc2))
     assert not eng2.autotune(cache)["from_cache"]
+
+
+def _strategy_file():
+    """Members of every zlib strategy and level over varied payloads, with
+    stored, fixed and dynamic blocks, empty members and the EOF block."""
+    from test_gpu_inflate import build_file
+
+    return build_file(np.random.default_rng(5))
+
+
+def _tampered(what: str):
+    from test_gpu_inflate import member
+
+    rng = np.random.default_rng(11)
+    parts = [member(bytes(rng.integers(65, 70, 20000, dtype=np.uint8)), 6) for _ in range(5)]
+    bad = bytearray(parts[3])
+    if what == "crc":
+        bad[-8] ^= 0xFF
+    else:
+        bad[40] ^= 0x55
+    parts[3] = bytes(bad)
+    return np.frombuffer(b"".join(parts), np.uint8)
+
+
+def test_every_variant_inflates_every_block_kind(frt):
+    """Plain form of every variant (one chain or several per warp) on stored,
+    fixed and dynamic blocks of every zlib strategy, empty members and the EOF
+    block: the oracle's bytes, and a tampered member fails with the oracle's
+    error variant and member offset."""
+    data = _strategy_file()
+    spans, _ = oracle.discover(data)
+    want, offs = oracle.inflate_batch(data, spans)
+    for what in ("crc", "payload"):
+        bad = _tampered(what)
+        bspans, _ = oracle.discover(bad)
+        with pytest.raises(oracle.OracleError) as oe:
+            oracle.inflate_batch(bad, bspans)
+        for t in _tunings(frt):
+            frt.set_default_tuning(t)
+            codec = frt.CudaCodec(0)
+            if what == "crc":
+                got, goffs = codec.inflate_batch(data, spans)
+                assert np.array_equal(goffs, offs) and np.array_equal(got, want), t.as_dict()
+            with pytest.raises(frt.FrtError) as ei:
+                codec.inflate_batch_device(bad, bspans)
+            assert (ei.value.code, ei.value.offset) == (oe.value.code, oe.value.offset), (t.as_dict(), what)
+
+
+def test_every_variant_reports_the_first_bad_member_in_the_engine(frt, bam):
+    """The batched (persistent) form of every variant: a tampered trailer or
+    payload is reported for the first failing member in file order."""
+    torch = pytest.importorskip("torch")
+    bgzf, r = bam
+    spans = r["spans"]
+    eng, dev = _engine(frt, torch, bgzf)  # bound on good bytes, then overwritten
+    for k, flip in ((5, "crc"), (2, "payload")):
+        bad = bgzf.copy()
+        if flip == "crc":
+            bad[int(spans[k]["payload_start"] + spans[k]["payload_len"])] ^= 0xFF
+        else:
+            bad[int(spans[k]["payload_start"]) + 30] ^= 0x55
+        with pytest.raises(oracle.OracleError) as oe:
+            oracle.inflate_batch(bad, oracle.discover(bad)[0])
+        dev.copy_(torch.from_numpy(bad).to("cuda"))
+        torch.cuda.synchronize()
+        for t in _tunings(frt):
+            eng.set_tuning(t)
+            eng.run()
+            with pytest.raises(frt.FrtError) as ei:
+                eng.finish()
+            assert ei.value.code == oe.value.code and ei.value.offset == int(spans[k]["compressed_offset"]), \
+                (t.as_dict(), flip)
