@@ -1171,7 +1171,6 @@ const Variant kVariants[] = {
     make_variant<Cfg<9, 7, 1024, 192, 64>>(), make_variant<Cfg<9, 7, 1024, 160, 56>>(),
     // several chains per warp (the shared memory per warp is K members')
     make_multi_variant<Cfg<9, 7, 1024, 192, 128>, 2>(), make_multi_variant<Cfg<9, 7, 1024, 192, 128>, 4>(),
-    make_multi_variant<Cfg<9, 7, 2048, 384, 128>, 4>(), make_multi_variant<Cfg<9, 7, 1024, 192, 128>, 8>(),
 };
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 

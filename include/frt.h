@@ -88,7 +88,9 @@ int frt_select_codec(int backend, frt_codec **out, int *resolved, frt_error *err
 
 /* CudaCodec::new / with_context(ctx, stream), crates/fritillaria-cuda/src/lib.rs:170-213.
  * `stream` may be NULL (the codec creates its own) or a cudaStream_t on
- * `device` owned by the caller. */
+ * `device` owned by the caller.  Allocations and launches happen in the
+ * device's primary context (the one cudarc's CudaContext::new retains); a
+ * caller's stream must belong to that context. */
 int frt_codec_create(int device, void *stream, frt_codec **out, frt_error *err);
 void frt_codec_destroy(frt_codec *codec);
 /* DeviceBlockCodec::name / device_ordinal, crates/fritillaria-core/src/device.rs:306-324. */
