@@ -105,19 +105,21 @@ __device__ __forceinline__ void load64(const u8 *buf, u64 p0, u64 lo, u64 hi, bo
     }
 }
 
-__device__ __forceinline__ u32 byte_of(const u32 w[16], int i) { return (w[i >> 2] >> (8 * (i & 3))) & 0xffu; }
 
 // =============================================================================
 // FASTQ
 // =============================================================================
 
+// Newlines per tile; *last_nl (when given) says whether the byte before hi
+// is one, so that the caller knows the line count with the newline count.
 __global__ void __launch_bounds__(TB) k_fq_nl_count(const u8 *buf, u64 lo, u64 hi, u64 tbase, bool aligned,
-                                                    u32 *tile_count)
+                                                    u32 *tile_count, u32 *last_nl)
 {
     __shared__ u32 s_warp[TB / 32];
     u64 p0 = tbase + (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
     u32 w[16];
     load64(buf, p0, lo, hi, aligned, w);
+    if (last_nl && hi > lo && hi - 1 >= p0 && hi - 1 < p0 + CH) *last_nl = buf[hi - 1] == '\n' ? 1u : 0u;
     u32 c = 0;
 #pragma unroll
     for (int k = 0; k < 16; ++k) c += __popc(__vcmpeq4(w[k], 0x0a0a0a0au)) >> 3;
@@ -126,8 +128,10 @@ __global__ void __launch_bounds__(TB) k_fq_nl_count(const u8 *buf, u64 lo, u64 h
     if (threadIdx.x == 0) tile_count[blockIdx.x] = tot;
 }
 
+// Positions in `buf` less `shift` are written: a caller whose batch starts
+// `shift` bytes past a 16-byte boundary passes that boundary as `buf`.
 __global__ void __launch_bounds__(TB) k_fq_nl_emit(const u8 *buf, u64 lo, u64 hi, u64 tbase, bool aligned,
-                                                   const u32 *tile_base, u64 *nl)
+                                                   const u32 *tile_base, u64 *nl, u64 shift)
 {
     __shared__ u32 s_warp[TB / 32];
     u64 p0 = tbase + (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
@@ -145,7 +149,7 @@ __global__ void __launch_bounds__(TB) k_fq_nl_emit(const u8 *buf, u64 lo, u64 hi
         u32 mk = m[k];
         while (mk) {
             int b = __ffs(mk) - 1;
-            nl[at++] = p0 + 4 * k + (b >> 3);
+            nl[at++] = p0 + 4 * k + (b >> 3) - shift;
             mk &= ~(0xffu << (b & ~7));
         }
     }
@@ -310,8 +314,9 @@ __global__ void k_fq_compact(const u32 *flags, const u32 *pos, u32 n_lines, u32 
 
 // bit 0: the survivors do not tile (fastq.rs:585-598); bit 1: they are not the
 // walk's chain either (a gap between records holds something besides newlines).
-__global__ void k_fq_check(FqIndex ix, const u32 *S, u32 n_s, u32 *fails)
+__global__ void k_fq_check(FqIndex ix, const u32 *S, const u32 *n_s_dev, u32 *fails)
 {
+    const u32 n_s = *n_s_dev;
     u32 j = blockIdx.x * blockDim.x + threadIdx.x;
     u32 f = 0;
     if (j + 1 < n_s) {
@@ -549,12 +554,108 @@ __global__ void __launch_bounds__(TB) k_bcf_sieve(const u8 *buf, u64 start, u64 
     }
 }
 
+// The single-pass sieve: the tile, staged with 16-byte loads from the
+// 16-byte boundary at or before the batch (`abuf`, `sh` bytes before `buf`),
+// is tested at every offset, first by the 24-bit n_sample match four offsets
+// at a time (two shared-memory words, two funnel shifts and three byte
+// compares), then by bcf_plausible.  Candidates go in position order into the
+// tile's slot of `lists` (SIEVE_CAP entries) and their number into
+// tile_count; a tile with more than SIEVE_CAP sets *overflow and the caller
+// runs the two-pass sieve instead.  The full validation of the candidates
+// runs afterwards, a thread each (k_bcf_check), so that its chains of
+// dependent loads (through a record's typed values, often past the staged
+// tile) overlap across all records instead of holding each tile.
+constexpr u32 SIEVE_CAP = 96;
+
+__global__ void __launch_bounds__(TB) k_bcf_sieve1(const u8 *abuf, u64 sh, u64 start, u64 len, u32 samples,
+                                                   u32 contigs, u32 *tile_count, u64 *lists, u32 *overflow)
+{
+    __shared__ __align__(16) u8 s[SIEVE_TILE + 48];
+    __shared__ u64 s_list[SIEVE_CAP];
+    __shared__ u32 s_n;
+    const u8 *buf = abuf + sh;
+    const u64 lo = start + sh, hi = len + sh; // candidate positions, in abuf coordinates
+    const u64 T0 = (lo & ~15ull) + (u64)blockIdx.x * SIEVE_TILE;
+    for (u32 i = threadIdx.x; i < (SIEVE_TILE + 48) / 16; i += TB) {
+        const u64 q = T0 + 16ull * i;
+        uint4 v;
+        if (q >= sh && q + 16 <= hi) {
+            v = __ldg(reinterpret_cast<const uint4 *>(abuf + q));
+        } else {
+            u32 w[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                u32 x = 0;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const u64 a = q + 4 * k + b;
+                    x |= (a >= sh && a < hi ? (u32)abuf[a] : 0u) << (8 * b);
+                }
+                w[k] = x;
+            }
+            v = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+        *reinterpret_cast<uint4 *>(s + 16 * i) = v;
+    }
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    const u32 *s32 = reinterpret_cast<const u32 *>(s);
+    const u32 b0 = (samples & 0xffu) * 0x01010101u, b1 = ((samples >> 8) & 0xffu) * 0x01010101u,
+              b2 = ((samples >> 16) & 0xffu) * 0x01010101u;
+    constexpr u32 PER = SIEVE_TILE / TB; // offsets a thread tests, a multiple of 4
+#pragma unroll 2
+    for (u32 g = 0; g < PER; g += 4) {
+        const u32 q = threadIdx.x * PER + g; // tile-relative, a multiple of 4
+        const u32 w0 = s32[(q + 28) >> 2], w1 = s32[(q + 32) >> 2];
+        u32 m = __vcmpeq4(w0, b0) & __vcmpeq4(__funnelshift_r(w0, w1, 8), b1) &
+                __vcmpeq4(__funnelshift_r(w0, w1, 16), b2);
+        while (m) {
+            const u32 k = (u32)(__ffs(m) - 1) >> 3;
+            m &= ~(0xffu << (8 * k));
+            const u64 pa = T0 + q + k; // abuf coordinates
+            if (pa < lo || pa >= hi) continue;
+            const u64 pos = pa - sh;
+            if (!bcf_plausible(s, q + k, pos, len, samples, contigs)) continue;
+            const u32 slot = atomicAdd(&s_n, 1u);
+            if (slot < SIEVE_CAP) s_list[slot] = pos;
+        }
+    }
+    __syncthreads();
+    const u32 n = s_n;
+    if (n > SIEVE_CAP) {
+        if (threadIdx.x == 0) {
+            atomicOr(overflow, 1u);
+            tile_count[blockIdx.x] = 0;
+        }
+        return;
+    }
+    for (u32 i = threadIdx.x; i < n; i += TB) {
+        const u64 v = s_list[i];
+        u32 r = 0;
+        for (u32 j = 0; j < n; ++j) r += s_list[j] < v;
+        lists[(u64)blockIdx.x * SIEVE_CAP + r] = v;
+    }
+    if (threadIdx.x == 0) tile_count[blockIdx.x] = n;
+}
+
+// Survivors of the single-pass sieve, tile lists concatenated in order.
+__global__ void k_bcf_gather(const u32 *tile_count, const u32 *tile_base, const u64 *lists, u64 n_tiles, u64 *V)
+{
+    const u64 t = (u64)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (t >= n_tiles) return;
+    const u32 c = tile_count[t], at = tile_base[t];
+    for (u32 j = threadIdx.x & 31; j < c; j += 32) V[at + j] = lists[t * SIEVE_CAP + j];
+}
+
 __device__ __forceinline__ u64 bcf_end(const u8 *buf, u64 pos)
 {
     return pos + 8 + (u64)ld_u32le(buf + pos) + (u64)ld_u32le(buf + pos + 4);
 }
 
-__global__ void k_bcf_check(const u8 *buf, u64 start, u64 len, const u64 *V, u32 nv, u32 *fails)
+// bit 0: the survivors do not tile; bit 1 (with `validate`): a candidate
+// failed the full validation, so the list is not the sieve's survivor list
+// and the caller takes the two-pass sieve.
+__global__ void k_bcf_check(const u8 *buf, u64 start, u64 len, const u64 *V, u32 nv, u32 *fails, bool validate)
 {
     u32 j = blockIdx.x * blockDim.x + threadIdx.x;
     u32 f = 0;
@@ -564,6 +665,7 @@ __global__ void k_bcf_check(const u8 *buf, u64 start, u64 len, const u64 *V, u32
         else {
             if (j == 0 && p != start) f = 1;
             if (j + 1 < nv && V[j + 1] != bcf_end(buf, p)) f = 1;
+            if (validate && !bcf_validate(buf, len, p)) f |= 2;
         }
     }
     u32 any = __reduce_or_sync(FRT_FULL_MASK, f);
@@ -575,7 +677,7 @@ __global__ void k_bcf_finalize(const u8 *buf, u64 start, u64 len, const u64 *V, 
                                const u32 *overflow, u64 *totals)
 {
     u32 nv = *nv_dev;
-    bool tiled = !*fails && !*overflow;
+    bool tiled = !(*fails & 1u) && !*overflow;
     u64 at = start;
     if (tiled && nv) at = bcf_end(buf, V[nv - 1]); // every survivor passed the range checks
     if (tiled && at + 8 <= len && bcf_end(buf, at) <= len) tiled = false; // a whole record the sieve missed
@@ -584,6 +686,7 @@ __global__ void k_bcf_finalize(const u8 *buf, u64 start, u64 len, const u64 *V, 
     totals[2] = tiled ? 0 : 1;
     totals[3] = nv;
     totals[4] = tiled ? 0 : 1;
+    totals[5] = *fails;
 }
 
 // The length-prefix walk of bcf_scan.cu:374-410; `out` null counts only.
@@ -688,7 +791,6 @@ __device__ __forceinline__ u32 f_then(u32 f, u32 g)
     if (g == F_ID) return f;
     return f == F_HDR || f == F_SEQ ? F_SEQ : F_OTHER;
 }
-__device__ __forceinline__ u32 f_step(u32 f, bool gt) { return gt ? F_HDR : f_then(f, F_OTHER); }
 
 // Exclusive scan of transfer functions across the block (composition).
 __device__ u32 block_excl_compose(u32 f, u32 *s_warp)
@@ -720,84 +822,74 @@ __device__ u32 block_excl_compose(u32 f, u32 *s_warp)
     return r;
 }
 
-struct FaChunk {
-    u32 w[16];
-    u32 prev; // the byte before the chunk (or '\n' at the buffer start)
-    u32 n;    // valid bytes in the chunk
+// A chunk of CH = 64 bytes as bit masks.  Its bytes come from aligned 16-byte
+// loads of `abuf`, the 16-byte boundary at or before the batch; the batch is
+// [lo, hi) of abuf.  nl and gt mark '\n' and '>', ls the line starts (the
+// batch start and every byte after a newline), hs/os the line starts that
+// open a definition line or another line.  Each byte's line is found by a
+// log-step fill: after it, O marks the bytes whose nearest line start at or
+// before them opens another (not a definition) line, and K the bytes with a
+// line start at or before them in the chunk.
+struct FaMasks {
+    u64 valid, nl, ls, hs, O, K;
 };
 
-__device__ __forceinline__ void fa_load(const u8 *buf, u64 len, bool aligned, u64 p0, FaChunk &c)
+__device__ __forceinline__ u32 nibble_of(u32 m) { return (((m >> 7) & 0x01010101u) * 0x01020408u) >> 24; }
+
+__device__ __forceinline__ void fa_masks(const u8 *abuf, u64 lo, u64 hi, u64 p0, FaMasks &f, u32 w[16])
 {
-    load64(buf, p0, 0, len, aligned, c.w);
-    c.prev = p0 == 0 ? (u32)'\n' : (p0 - 1 < len ? (u32)buf[p0 - 1] : 0u);
-    c.n = p0 >= len ? 0u : (u32)min((u64)CH, len - p0);
+    load64(abuf, p0, lo, hi, true, w);
+    u64 nl = 0, gt = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        nl |= (u64)nibble_of(__vcmpeq4(w[k], 0x0a0a0a0au)) << (4 * k);
+        gt |= (u64)nibble_of(__vcmpeq4(w[k], 0x3e3e3e3eu)) << (4 * k);
+    }
+    u64 valid = ~0ull;
+    if (p0 < lo) valid &= lo - p0 >= 64 ? 0ull : ~0ull << (lo - p0);
+    if (p0 + 64 > hi) valid &= hi <= p0 ? 0ull : (~0ull >> (64 - (hi - p0)));
+    nl &= valid;
+    gt &= valid;
+    const bool prev_nl = p0 > lo && abuf[p0 - 1] == '\n';
+    const u64 first = lo >= p0 && lo < p0 + 64 ? 1ull << (lo - p0) : 0ull;
+    const u64 ls = ((nl << 1) | (prev_nl ? 1ull : 0ull) | first) & valid;
+    const u64 hs = ls & gt, os = ls & ~gt;
+    u64 O = os, K = ls;
+#pragma unroll
+    for (int sft = 1; sft < 64; sft <<= 1) {
+        O |= (O << sft) & ~K;
+        K |= K << sft;
+    }
+    f.valid = valid;
+    f.nl = nl;
+    f.ls = ls;
+    f.hs = hs;
+    f.O = O;
+    f.K = K;
 }
 
-// The chunk's transfer function and its count of record starts.
-__device__ __forceinline__ void fa_summary(const FaChunk &c, u32 *f_out, u32 *contigs)
+// The chunk's transfer function: identity with no line start, else decided
+// by its last line start (a definition line: constant 1; another line after
+// a definition line in the chunk: constant 2; else OTHER).
+__device__ __forceinline__ u32 fa_func(const FaMasks &f)
 {
-    u32 f = F_ID, k = 0, prev = c.prev;
-#pragma unroll
-    for (int i = 0; i < CH; ++i) {
-        if ((u32)i < c.n) {
-            u32 b = byte_of(c.w, i);
-            if (prev == '\n') {
-                f = f_step(f, b == '>');
-                k += b == '>';
-            }
-            prev = b;
-        }
-    }
-    *f_out = f;
-    *contigs = k;
+    if (!f.ls) return F_ID;
+    const int last = 63 - __clzll((long long)f.ls);
+    if ((f.hs >> last) & 1ull) return F_HDR;
+    return f.hs ? F_SEQ : F_OTHER;
 }
 
-// Bases the chunk keeps, entering in state s.
-__device__ __forceinline__ u32 fa_kept(const FaChunk &c, u32 s)
+// The bytes the chunk keeps when it is entered in state s: bytes of sequence
+// lines that are not newlines.  A byte before the chunk's first line start is
+// in state s; a byte of a definition line is not kept; a byte of another line
+// is kept when a definition line came before it in the chunk or s is not 0.
+__device__ __forceinline__ u64 fa_keep(const FaMasks &f, u32 s)
 {
-    u32 kept = 0, prev = c.prev;
-#pragma unroll
-    for (int i = 0; i < CH; ++i) {
-        if ((u32)i < c.n) {
-            u32 b = byte_of(c.w, i);
-            if (prev == '\n') s = b == '>' ? 1u : (s == 0 ? 0u : 2u);
-            kept += (s == 2u && b != '\n');
-            prev = b;
-        }
-    }
-    return kept;
-}
-
-__global__ void __launch_bounds__(TB) k_fa_pass1(const u8 *buf, u64 len, bool aligned, u8 *tile_f, u32 *tile_contigs,
-                                                 unsigned long long *last_contig)
-{
-    __shared__ u32 s_warp[TB / 32];
-    FaChunk c;
-    u64 p0 = (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
-    fa_load(buf, len, aligned, p0, c);
-    u32 f, k;
-    fa_summary(c, &f, &k);
-    if (k) {
-        // position of the chunk's last record start, for the final-header check
-        u32 prev = c.prev;
-        u64 last = 0;
-#pragma unroll
-        for (int i = 0; i < CH; ++i) {
-            if ((u32)i < c.n) {
-                u32 b = byte_of(c.w, i);
-                if (prev == '\n' && b == '>') last = p0 + i;
-                prev = b;
-            }
-        }
-        atomicMax(last_contig, (unsigned long long)last + 1);
-    }
-    u32 tot;
-    block_excl_sum<u32>(k, s_warp, &tot);
-    u32 ex = block_excl_compose(f, s_warp);
-    if (threadIdx.x == TB - 1) {
-        tile_f[blockIdx.x] = (u8)f_then(ex, f);
-        tile_contigs[blockIdx.x] = tot;
-    }
+    const int fh = f.hs ? __ffsll((long long)f.hs) - 1 : 64;
+    const u64 below = fh >= 64 ? ~0ull : (1ull << fh) - 1ull;
+    const u64 text = f.valid & ~f.nl;
+    const u64 pre = ~f.K & text, other = f.O & text;
+    return (s == 2u ? pre : 0ull) | (s != 0u ? (other & below) : 0ull) | (other & ~below);
 }
 
 // One block: per tile its entry state and first contig index; the contig
@@ -869,62 +961,96 @@ __global__ void __launch_bounds__(1024) k_fa_tiles(const u8 *buf, u64 len, const
     }
 }
 
-__global__ void __launch_bounds__(TB) k_fa_pass2(const u8 *buf, u64 len, bool aligned, const u8 *tile_state,
-                                                 u32 *tile_kept)
+// Pass 1, per tile of TILE bytes (abuf coordinates from 0): the transfer
+// function, the record starts, and the bytes kept when the tile is entered in
+// each state (3 per tile); the position after the last record start goes to
+// *last_contig (batch coordinates, for the unterminated-header check).
+__global__ void __launch_bounds__(TB) k_fa_sum(const u8 *abuf, u64 sh, u64 len, u8 *tile_f, u32 *tile_contigs,
+                                               u32 *tile_kept3, unsigned long long *last_contig)
 {
     __shared__ u32 s_warp[TB / 32];
-    FaChunk c;
-    u64 p0 = (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
-    fa_load(buf, len, aligned, p0, c);
-    u32 f, k;
-    fa_summary(c, &f, &k);
-    u32 ex = block_excl_compose(f, s_warp);
-    u32 s = f_apply(ex, tile_state[blockIdx.x]);
-    u32 kept = fa_kept(c, s), tot;
-    block_excl_sum<u32>(kept, s_warp, &tot);
-    if (threadIdx.x == 0) tile_kept[blockIdx.x] = tot;
+    const u64 lo = sh, hi = len + sh;
+    const u64 p0 = (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
+    FaMasks m;
+    u32 w[16];
+    fa_masks(abuf, lo, hi, p0, m, w);
+    const u32 f = fa_func(m), k = (u32)__popcll(m.hs);
+    if (m.hs) atomicMax(last_contig, (unsigned long long)(p0 + 63 - __clzll((long long)m.hs) - sh + 1));
+    u32 kept[3];
+#pragma unroll
+    for (u32 st = 0; st < 3; ++st) kept[st] = (u32)__popcll(fa_keep(m, st));
+    const u32 ex = block_excl_compose(f, s_warp);
+    u32 tot;
+    block_excl_sum<u32>(k, s_warp, &tot);
+    if (threadIdx.x == TB - 1) tile_f[blockIdx.x] = (u8)f_then(ex, f);
+    if (threadIdx.x == 0) tile_contigs[blockIdx.x] = tot;
+#pragma unroll
+    for (u32 st = 0; st < 3; ++st) {
+        u32 t3;
+        block_excl_sum<u32>(kept[f_apply(ex, st)], s_warp, &t3);
+        if (threadIdx.x == 0) tile_kept3[3 * blockIdx.x + st] = t3;
+    }
 }
 
-__global__ void __launch_bounds__(TB) k_fa_pass3(const u8 *buf, u64 len, bool aligned, const u8 *tile_state,
-                                                 const u32 *contig_base, const u64 *out_base, u64 n_contigs, u8 *seq,
-                                                 u64 *seq_off, u64 *rec_off)
+// The kept count of each tile for the state it is entered in.
+__global__ void k_fa_select(const u32 *tile_kept3, const u8 *tile_state, u32 n_tiles, u32 *tile_kept)
+{
+    const u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n_tiles) tile_kept[t] = tile_kept3[3 * t + tile_state[t]];
+}
+
+// Pass 2: each tile's kept bytes, compacted in order through a shared-memory
+// staging buffer and written with coalesced stores, and each record's offset
+// and the offset of its first base.
+__global__ void __launch_bounds__(TB) k_fa_emit(const u8 *abuf, u64 sh, u64 len, const u8 *tile_state,
+                                                const u32 *contig_base, const u64 *out_base, u64 n_contigs, u8 *seq,
+                                                u64 *seq_off, u64 *rec_off)
 {
     __shared__ u32 s_warp[TB / 32];
-    __shared__ __align__(16) u8 s_out[TILE];
-    FaChunk c;
-    u64 p0 = (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
-    fa_load(buf, len, aligned, p0, c);
-    u32 f, k;
-    fa_summary(c, &f, &k);
-    u32 ex = block_excl_compose(f, s_warp);
-    u32 s = f_apply(ex, tile_state[blockIdx.x]);
-    u32 kept = fa_kept(c, s), tile_total;
-    u32 at = block_excl_sum<u32>(kept, s_warp, &tile_total);
-    u32 ci = contig_base[blockIdx.x] + block_excl_sum<u32>(k, s_warp, nullptr);
+    __shared__ __align__(16) u8 s_out[TILE + 16];
+    const u64 lo = sh, hi = len + sh;
+    const u64 p0 = (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
+    FaMasks m;
+    u32 w[16];
+    fa_masks(abuf, lo, hi, p0, m, w);
+    const u32 f = fa_func(m);
+    const u32 ex = block_excl_compose(f, s_warp);
+    const u32 st = f_apply(ex, tile_state[blockIdx.x]);
+    const u64 keep = fa_keep(m, st);
+    u32 tile_total;
+    const u32 at = block_excl_sum<u32>((u32)__popcll(keep), s_warp, &tile_total);
+    u32 ci = contig_base[blockIdx.x] + block_excl_sum<u32>((u32)__popcll(m.hs), s_warp, nullptr);
     const u64 obase = out_base[blockIdx.x];
-    u32 prev = c.prev, o = at;
-#pragma unroll
-    for (int i = 0; i < CH; ++i) {
-        if ((u32)i < c.n) {
-            u32 b = byte_of(c.w, i);
-            if (prev == '\n') {
-                if (b == '>') {
-                    if (ci < n_contigs) {
-                        rec_off[ci] = p0 + i;
-                        seq_off[ci] = obase + o;
-                    }
-                    ++ci;
-                    s = 1u;
-                } else if (s != 0u) {
-                    s = 2u;
-                }
-            }
-            if (s == 2u && b != '\n') s_out[o++] = (u8)b;
-            prev = b;
+    // record starts (a few per tile at most)
+    for (u64 h = m.hs; h; h &= h - 1) {
+        const int i = __ffsll((long long)h) - 1;
+        if (ci < n_contigs) {
+            rec_off[ci] = p0 + (u64)i - sh;
+            seq_off[ci] = obase + at + (u32)__popcll(keep & ((1ull << i) - 1ull));
         }
+        ++ci;
+    }
+    u32 o = at;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+        const u32 kb = (u32)(keep >> (4 * k)) & 15u, wk = w[k];
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+            if ((kb >> b) & 1u) s_out[o++] = (u8)(wk >> (8 * b));
     }
     __syncthreads();
-    for (u32 i = threadIdx.x; i < tile_total; i += TB) seq[obase + i] = s_out[i];
+    // the bytes before the output's first 4-byte boundary, then whole words
+    // put together from shared memory with funnel shifts, then the rest
+    const u32 h = min((u32)((4u - (u32)(obase & 3u)) & 3u), tile_total);
+    if (threadIdx.x < h) seq[obase + threadIdx.x] = s_out[threadIdx.x];
+    const u32 nw = (tile_total - h) >> 2;
+    u32 *dst = reinterpret_cast<u32 *>(seq + obase + h);
+    const u32 *s32 = reinterpret_cast<const u32 *>(s_out);
+    for (u32 j = threadIdx.x; j < nw; j += TB) {
+        const u32 off = h + 4u * j;
+        dst[j] = __funnelshift_r(s32[off >> 2], s32[(off >> 2) + 1], 8u * (off & 3u));
+    }
+    for (u32 i = h + 4u * nw + threadIdx.x; i < tile_total; i += TB) seq[obase + i] = s_out[i];
 }
 
 __global__ void k_fa_lengths(const u64 *seq_off, u64 n, u64 total, u64 *seq_len)
@@ -1176,32 +1302,33 @@ extern "C" int frt_fastq_decode(frt_fastq_scanner *sc, const frt_inflate_batch *
     }
     cudaStream_t st = s.stream;
     Work w(st);
-    const u64 tbase = start & ~15ull;
-    const u64 n_tiles = (len - tbase + TILE - 1) / TILE;
-    const bool aligned = ((uintptr_t)b->data & 15) == 0;
+    // The newline index reads aligned 16-byte blocks, so it works from the
+    // 16-byte boundary at or before the batch (the sh bytes before the batch
+    // are never read) and writes batch positions.
+    const u64 sh = (uintptr_t)b->data & 15u;
+    const u8 *abuf = b->data - sh;
+    const u64 tbase = (start + sh) & ~15ull;
+    const u64 n_tiles = (len + sh - tbase + TILE - 1) / TILE;
     u32 *tile_count, *tile_base, *partials, *d_u32;
     u64 *totals;
     if ((rc = w.get(&tile_count, n_tiles, err)) || (rc = w.get(&tile_base, n_tiles + 1, err)) ||
         (rc = w.get(&partials, frt_scan_partials_len(n_tiles) + frt_scan_partials_len(len) + 8, err)) ||
         (rc = w.get(&d_u32, 8, err)) || (rc = w.get(&totals, 8, err)))
         return rc;
-    k_fq_nl_count<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, tbase, aligned, tile_count);
+    k_fq_nl_count<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_count,
+                                                    d_u32 + 7);
     LAUNCH_OK("launching the newline count");
     cudaError_t e = frt_launch_scan_u32(tile_count, n_tiles, partials, tile_base, d_u32, st);
     if (e != cudaSuccess) return cuda_fail(err, e, "scanning newline counts");
-    uint32_t n_nl = 0;
-    if ((rc = read_back(st, d_u32, &n_nl, 4, err, "newline count"))) return rc;
+    uint32_t hd[8] = {};
+    if ((rc = read_back(st, d_u32, hd, sizeof hd, err, "newline count"))) return rc;
+    const uint32_t n_nl = hd[0];
     u64 *nl;
     if ((rc = w.get(&nl, (size_t)n_nl + 1, err))) return rc;
-    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, tbase, aligned, tile_base, nl);
+    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, sh);
     LAUNCH_OK("launching the newline index");
     // line starts: start, and one past every newline that is not the last byte
-    uint32_t n_lines = n_nl + 1;
-    {
-        uint64_t last_nl = 0;
-        if (n_nl && (rc = read_back(st, nl + n_nl - 1, &last_nl, 8, err, "last newline"))) return rc;
-        if (n_nl && last_nl + 1 >= len) n_lines = n_nl;
-    }
+    const uint32_t n_lines = n_nl && hd[7] ? n_nl : n_nl + 1;
     FqIndex ix{b->data, start, len, nl, n_nl, n_lines};
     u32 *flags, *pos, *S, *W, *fails;
     if ((rc = w.get(&flags, n_lines, err)) || (rc = w.get(&pos, (size_t)n_lines + 1, err)) ||
@@ -1212,11 +1339,10 @@ extern "C" int frt_fastq_decode(frt_fastq_scanner *sc, const frt_inflate_batch *
     LAUNCH_OK("launching the line validation");
     if ((e = frt_launch_scan_u32(flags, n_lines, partials, pos, d_u32, st)) != cudaSuccess)
         return cuda_fail(err, e, "scanning record starts");
-    uint32_t n_s = 0;
-    if ((rc = read_back(st, d_u32, &n_s, 4, err, "record starts"))) return rc;
-    if ((rc = w.get(&S, (size_t)n_s + 1, err)) || (rc = w.get(&W, (size_t)n_s + 1, err))) return rc;
+    // the record starts are at most the lines: no read-back to size them
+    if ((rc = w.get(&S, (size_t)n_lines + 1, err)) || (rc = w.get(&W, (size_t)n_lines + 1, err))) return rc;
     k_fq_compact<<<grid_for(n_lines, 256), 256, 0, st>>>(flags, pos, n_lines, S);
-    k_fq_check<<<grid_for(n_s + 1, 256), 256, 0, st>>>(ix, S, n_s, fails);
+    k_fq_check<<<grid_for(n_lines + 1, 256), 256, 0, st>>>(ix, S, d_u32, fails);
     k_fq_finalize<<<1, 1, 0, st>>>(ix, flags, S, d_u32, fails, W, totals);
     LAUNCH_OK("launching the tiling checks");
     uint64_t tot[5];
@@ -1304,23 +1430,54 @@ extern "C" int frt_bcf_decode(frt_bcf_scanner *sc, const frt_inflate_batch *b, u
         (rc = w.get(&totals, 8, err)))
         return rc;
     cudaMemsetAsync(d_u32, 0, 32, st);
-    k_bcf_sieve<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, samples, contigs, 0, tile_count, nullptr,
-                                                  nullptr, nullptr);
+    // One pass: per-tile survivor lists, their counts scanned, then gathered.
+    // A tile with more survivors than its list holds sends the batch to the
+    // two-pass sieve (count, scan, emit).
+    const u64 sh = (uintptr_t)b->data & 15u;
+    const u64 n_tiles1 = (((len + sh) - ((start + sh) & ~15ull)) + SIEVE_TILE - 1) / SIEVE_TILE;
+    u32 *count1, *base1;
+    u64 *lists;
+    if ((rc = w.get(&count1, n_tiles1, err)) || (rc = w.get(&base1, n_tiles1 + 1, err)) ||
+        (rc = w.get(&lists, n_tiles1 * SIEVE_CAP, err)))
+        return rc;
+    if ((rc = w.get(&partials, frt_scan_partials_len(n_tiles1) + 8, err))) return rc;
+    k_bcf_sieve1<<<(unsigned)n_tiles1, TB, 0, st>>>(b->data - sh, sh, start, len, samples, contigs, count1, lists,
+                                                    d_u32 + 5);
     LAUNCH_OK("launching the BCF sieve");
-    cudaError_t e = frt_launch_scan_u32(tile_count, n_tiles, partials, tile_base, d_u32, st);
+    cudaError_t e = frt_launch_scan_u32(count1, n_tiles1, partials, base1, d_u32, st);
     if (e != cudaSuccess) return cuda_fail(err, e, "scanning survivors");
-    uint32_t nv = 0;
-    if ((rc = read_back(st, d_u32, &nv, 4, err, "survivor count"))) return rc;
-    u64 *V;
-    if ((rc = w.get(&V, (size_t)nv + 1, err))) return rc;
+    uint32_t head[6] = {};
+    if ((rc = read_back(st, d_u32, head, sizeof head, err, "survivor count"))) return rc;
+    uint32_t nv = head[0];
+    u64 *V = nullptr;
     u32 *fails = d_u32 + 2, *overflow = d_u32 + 3;
-    k_bcf_sieve<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, samples, contigs, 1, tile_count, tile_base, V,
-                                                  overflow);
-    k_bcf_check<<<grid_for(nv + 1, 256), 256, 0, st>>>(b->data, start, len, V, nv, fails);
-    k_bcf_finalize<<<1, 1, 0, st>>>(b->data, start, len, V, d_u32, fails, overflow, totals);
-    LAUNCH_OK("launching the BCF tiling proof");
-    uint64_t tot[5];
-    if ((rc = read_back(st, totals, tot, sizeof tot, err, "BCF scan"))) return rc;
+    uint64_t tot[6];
+    bool exact = head[5] != 0; // the two-pass sieve, which validates in the sieve
+    if (!exact) {
+        if ((rc = w.get(&V, (size_t)nv + 1, err))) return rc;
+        k_bcf_gather<<<(unsigned)((n_tiles1 + 7) / 8), 256, 0, st>>>(count1, base1, lists, n_tiles1, V);
+        k_bcf_check<<<grid_for(nv + 1, 256), 256, 0, st>>>(b->data, start, len, V, nv, fails, true);
+        k_bcf_finalize<<<1, 1, 0, st>>>(b->data, start, len, V, d_u32, fails, overflow, totals);
+        LAUNCH_OK("launching the BCF tiling proof");
+        if ((rc = read_back(st, totals, tot, sizeof tot, err, "BCF scan"))) return rc;
+        exact = (tot[5] & 2u) != 0; // a candidate is not a record: its list is not the survivors'
+    }
+    if (exact) {
+        cudaMemsetAsync(d_u32, 0, 32, st);
+        k_bcf_sieve<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, samples, contigs, 0, tile_count,
+                                                      nullptr, nullptr, nullptr);
+        LAUNCH_OK("launching the BCF sieve");
+        if ((e = frt_launch_scan_u32(tile_count, n_tiles, partials, tile_base, d_u32, st)) != cudaSuccess)
+            return cuda_fail(err, e, "scanning survivors");
+        if ((rc = read_back(st, d_u32, &nv, 4, err, "survivor count"))) return rc;
+        if ((rc = w.get(&V, (size_t)nv + 1, err))) return rc;
+        k_bcf_sieve<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, samples, contigs, 1, tile_count,
+                                                      tile_base, V, overflow);
+        k_bcf_check<<<grid_for(nv + 1, 256), 256, 0, st>>>(b->data, start, len, V, nv, fails, false);
+        k_bcf_finalize<<<1, 1, 0, st>>>(b->data, start, len, V, d_u32, fails, overflow, totals);
+        LAUNCH_OK("launching the BCF tiling proof");
+        if ((rc = read_back(st, totals, tot, sizeof tot, err, "BCF scan"))) return rc;
+    }
     const u64 *list = V;
     if (tot[4]) { // the walk (bcf.rs:376-410): count, then emit
         k_bcf_walk<<<1, 1, 0, st>>>(b->data, start, len, nullptr, totals);
@@ -1541,23 +1698,28 @@ extern "C" int frt_fasta_compact(frt_fasta_compactor *sc, const frt_inflate_batc
         set_error(err, FRT_ERR_INVALID_ARGUMENT, 0, 0, 0, 0, nullptr, "FASTA batch too large");
         return FRT_ERR_INVALID_ARGUMENT;
     }
-    const bool aligned = ((uintptr_t)b->data & 15) == 0;
+    // the passes read aligned 16-byte blocks from the 16-byte boundary at or
+    // before the batch (the sh bytes before it are never read)
+    const u64 sh = (uintptr_t)b->data & 15u;
+    const u8 *abuf = b->data - sh;
+    const u64 n_tiles2 = (len + sh + TILE - 1) / TILE;
     u8 *tile_f, *tile_state;
-    u32 *tile_contigs, *contig_base, *tile_kept;
+    u32 *tile_contigs, *contig_base, *tile_kept, *tile_kept3;
     u64 *out_base, *totals;
     unsigned long long *last_contig;
-    if ((rc = w.get(&tile_f, n_tiles, err)) || (rc = w.get(&tile_state, n_tiles, err)) ||
-        (rc = w.get(&tile_contigs, n_tiles, err)) || (rc = w.get(&contig_base, n_tiles, err)) ||
-        (rc = w.get(&tile_kept, n_tiles, err)) || (rc = w.get(&out_base, n_tiles + 1, err)) ||
-        (rc = w.get(&totals, 8, err)) || (rc = w.get(&last_contig, 2, err)))
+    if ((rc = w.get(&tile_f, n_tiles2, err)) || (rc = w.get(&tile_state, n_tiles2, err)) ||
+        (rc = w.get(&tile_contigs, n_tiles2, err)) || (rc = w.get(&contig_base, n_tiles2, err)) ||
+        (rc = w.get(&tile_kept, n_tiles2, err)) || (rc = w.get(&tile_kept3, 3 * n_tiles2, err)) ||
+        (rc = w.get(&out_base, n_tiles2 + 1, err)) || (rc = w.get(&totals, 8, err)) ||
+        (rc = w.get(&last_contig, 2, err)))
         return rc;
     cudaMemsetAsync(last_contig, 0, 16, st);
     cudaMemsetAsync(totals, 0, 64, st);
-    k_fa_pass1<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, len, aligned, tile_f, tile_contigs, last_contig);
-    k_fa_tiles<<<1, 1024, 0, st>>>(b->data, len, tile_f, tile_contigs, (u32)n_tiles, tile_state, contig_base,
+    k_fa_sum<<<(unsigned)n_tiles2, TB, 0, st>>>(abuf, sh, len, tile_f, tile_contigs, tile_kept3, last_contig);
+    k_fa_tiles<<<1, 1024, 0, st>>>(b->data, len, tile_f, tile_contigs, (u32)n_tiles2, tile_state, contig_base,
                                    last_contig, totals);
-    k_fa_pass2<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, len, aligned, tile_state, tile_kept);
-    k_scan_tiles64<<<1, 1024, 0, st>>>(tile_kept, (u32)n_tiles, out_base, totals + 1);
+    k_fa_select<<<grid_for(n_tiles2, 256), 256, 0, st>>>(tile_kept3, tile_state, (u32)n_tiles2, tile_kept);
+    k_scan_tiles64<<<1, 1024, 0, st>>>(tile_kept, (u32)n_tiles2, out_base, totals + 1);
     LAUNCH_OK("launching the FASTA scans");
     uint64_t tot[3];
     if ((rc = read_back(st, totals, tot, sizeof tot, err, "FASTA layout"))) return rc;
@@ -1573,7 +1735,7 @@ extern "C" int frt_fasta_compact(frt_fasta_compactor *sc, const frt_inflate_batc
     c->col_bytes[FRT_FASTA_COL_SEQUENCE] = total;
     u64 *seq_off = colp<u64>(c, FRT_FASTA_COL_SEQUENCE_OFFSETS), *seq_len = colp<u64>(c, FRT_FASTA_COL_SEQUENCE_LENGTHS),
         *rec_off = colp<u64>(c, FRT_FASTA_COL_RECORD_OFFSETS);
-    k_fa_pass3<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, len, aligned, tile_state, contig_base, out_base, n, c->seq,
+    k_fa_emit<<<(unsigned)n_tiles2, TB, 0, st>>>(abuf, sh, len, tile_state, contig_base, out_base, n, c->seq,
                                                  seq_off, rec_off);
     k_fa_lengths<<<grid_for(n, 256), 256, 0, st>>>(seq_off, n, total, seq_len);
     cudaError_t e = cudaGetLastError();
@@ -1719,30 +1881,32 @@ extern "C" int frt_text_scan(frt_text_scanner *sc, const frt_inflate_batch *b, u
     }
     cudaStream_t st = s.stream;
     Work w(st);
-    const u64 tbase = start & ~15ull;
-    const u64 n_tiles = (len - tbase + TILE - 1) / TILE;
-    const bool aligned = ((uintptr_t)b->data & 15) == 0;
+    // The newline index reads aligned 16-byte blocks, so it works from the
+    // 16-byte boundary at or before the batch (the sh bytes before the batch
+    // are never read) and writes batch positions.
+    const u64 sh = (uintptr_t)b->data & 15u;
+    const u8 *abuf = b->data - sh;
+    const u64 tbase = (start + sh) & ~15ull;
+    const u64 n_tiles = (len + sh - tbase + TILE - 1) / TILE;
     u32 *tile_count, *tile_base, *partials, *d_u32;
     if ((rc = w.get(&tile_count, n_tiles, err)) || (rc = w.get(&tile_base, n_tiles + 1, err)) ||
         (rc = w.get(&partials, frt_scan_partials_len(n_tiles) + frt_scan_partials_len(len) + 8, err)) ||
         (rc = w.get(&d_u32, 8, err)))
         return rc;
-    k_fq_nl_count<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, tbase, aligned, tile_count);
+    k_fq_nl_count<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_count,
+                                                    d_u32 + 7);
     LAUNCH_OK("launching the newline count");
     cudaError_t e = frt_launch_scan_u32(tile_count, n_tiles, partials, tile_base, d_u32, st);
     if (e != cudaSuccess) return cuda_fail(err, e, "scanning newline counts");
-    uint32_t n_nl = 0;
-    if ((rc = read_back(st, d_u32, &n_nl, 4, err, "newline count"))) return rc;
+    uint32_t hd[8] = {};
+    if ((rc = read_back(st, d_u32, hd, sizeof hd, err, "newline count"))) return rc;
+    const uint32_t n_nl = hd[0];
     u64 *nl;
     if ((rc = w.get(&nl, (size_t)n_nl + 1, err))) return rc;
-    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(b->data, start, len, tbase, aligned, tile_base, nl);
+    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, sh);
     LAUNCH_OK("launching the newline index");
-    uint32_t n_lines = n_nl + 1; // line starts: start, and one past every newline that is not the last byte
-    {
-        uint64_t last_nl = 0;
-        if (n_nl && (rc = read_back(st, nl + n_nl - 1, &last_nl, 8, err, "last newline"))) return rc;
-        if (n_nl && last_nl + 1 >= len) n_lines = n_nl;
-    }
+    // line starts: start, and one past every newline that is not the last byte
+    const uint32_t n_lines = n_nl && hd[7] ? n_nl : n_nl + 1;
     FqIndex ix{b->data, start, len, nl, n_nl, n_lines};
     u32 *is_rec, *is_hdr, *rec_pos, *hdr_pos;
     if ((rc = w.get(&is_rec, n_lines, err)) || (rc = w.get(&is_hdr, n_lines, err)) ||
