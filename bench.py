@@ -76,6 +76,16 @@ SERVING = {
                     desc="32 BAI-indexed short-read BAMs (24 contigs, 3.1 Gb; record counts log-uniform "
                          "50k-2.5M, one twentieth of 1M-50M), Poisson arrivals at 2,000 req/s, regions on a "
                          "random contig with uniform start and log-uniform length 1 kb-10 Mb, 150 GB budget"),
+    "serving_quarter": dict(files=32, min_records=250_000, max_records=12_500_000, rate=2000.0, requests=4000,
+                            plain_requests=300, budget=150 << 30,
+                            desc="32 BAI-indexed short-read BAMs (24 contigs, 3.1 Gb; record counts log-uniform "
+                                 "250k-12.5M, one quarter of 1M-50M), Poisson arrivals at 2,000 req/s, regions on a "
+                                 "random contig with uniform start and log-uniform length 1 kb-10 Mb, 150 GB budget"),
+    "serving_full": dict(files=32, min_records=1_000_000, max_records=50_000_000, rate=2000.0, requests=4000,
+                         plain_requests=300, budget=150 << 30,
+                         desc="32 BAI-indexed short-read BAMs (24 contigs, 3.1 Gb; record counts log-uniform 1M-50M), "
+                              "Poisson arrivals at 2,000 req/s, regions on a random contig with uniform start and "
+                              "log-uniform length 1 kb-10 Mb, 150 GB budget"),
     "serving_small": dict(files=8, min_records=20_000, max_records=200_000, rate=2000.0, requests=800,
                           plain_requests=100, budget=150 << 30, desc="the serving workload at test size"),
 }
@@ -1109,6 +1119,15 @@ def latency_summary(rows):
             "completed_per_s": round(len(rows) / (span / 1e3), 1) if span > 0 else None}
 
 
+def tick_breakdown(st: dict) -> dict:
+    """Mean per-tick stage times of a serving run (frt_server_get_stats)."""
+    n = max(1, st["ticks"])
+    return {"ticks": st["ticks"], "requests_per_tick": round(st["requests"] / n, 1),
+            "members_per_tick": round(st["members"] / n, 1), "host_ms": round(st["host_ms"] / n, 3),
+            "upload_and_wait_ms": round(st["upload_ms"] / n, 3), "inflate_ms": round(st["inflate_ms"] / n, 3),
+            "scan_emit_ms": round(st["scan_ms"] / n, 3), "max_inflate_ms": st["max_inflate_ms"]}
+
+
 def run_serving(args, rank, world, local):
     import torch
 
@@ -1129,14 +1148,23 @@ def run_serving(args, rank, world, local):
     ids = [srv.add_bam(b, x) for b, x, _ in files]
     # warm-up: a few requests through every stage
     serve_stream(frt, srv, ids, [(0.0,) + r[1:] for r in reqs[: max(3, args.warmup)]])
+    srv.stats(reset=True)
     with Clocks(local) as clocks:
         t0 = time.perf_counter()
         rows = serve_stream(frt, srv, ids, reqs)
         wall = time.perf_counter() - t0
     batched = latency_summary(rows)
+    batched["ticks"] = tick_breakdown(srv.stats(reset=True))
     # capacity: the whole stream offered at once
     cap_rows = serve_stream(frt, srv, ids, [(0.0,) + r[1:] for r in reqs])
     capacity = latency_summary(cap_rows)
+    capacity["ticks"] = tick_breakdown(srv.stats(reset=True))
+    # one tick in flight: no tick shares the GPU with the one before it
+    srv.set_limits(0, 1)
+    one_rows = serve_stream(frt, srv, ids, reqs)
+    one_tick = latency_summary(one_rows)
+    one_tick["ticks"] = tick_breakdown(srv.stats(reset=True))
+    srv.set_limits(0, 2)
     # the plain per-request form: one request per tick, one tick in flight,
     # the same arrivals (a prefix of the stream: it cannot keep up)
     plain_srv = frt.RegionServer(0, budget_bytes=w["budget"])
@@ -1156,7 +1184,8 @@ def run_serving(args, rank, world, local):
                        "offered_req_per_s": w["rate"], "budget_bytes": w["budget"],
                        "l2": "region requests are independent (no flush)", "parallelism": f"replicas x{world}",
                        "tuning": tuning},
-            "serving": {"batched": batched, "capacity": capacity, "plain_per_request": plain,
+            "serving": {"batched": batched, "capacity": capacity, "one_tick_in_flight": one_tick,
+                        "plain_per_request": plain,
                         "note": "latency = device completion of the request's tick - arrival; plain = one request "
                                 "per tick, one tick in flight, on the first requests of the same stream"},
             "roofline": None, "cpu_baseline": None,

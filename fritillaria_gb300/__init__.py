@@ -291,6 +291,7 @@ def lib():
         "frt_server_destroy": (None, [_P]),
         "frt_server_set_limits": (None, [_P, C.c_uint32, C.c_uint32]),
         "frt_server_clock_ms": (C.c_double, [_P]),
+        "frt_server_get_stats": (C.c_int, [_P, _P, C.c_int32]),
         "frt_server_add_bam": (C.c_int, [_P, _P, C.c_size_t, _P, C.c_size_t, _P, _P]),
         "frt_server_submit": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, C.c_double, _P, _P]),
         "frt_server_progress": (C.c_int, [_P, _P, _P]),
@@ -1247,6 +1248,15 @@ class RegionInfo(C.Structure):
                 ("members", C.c_uint64), ("retries", C.c_uint32)]
 
 
+class ServerStats(C.Structure):
+    _fields_ = [("ticks", C.c_uint64), ("requests", C.c_uint64), ("members", C.c_uint64), ("host_ms", C.c_double),
+                ("upload_ms", C.c_double), ("inflate_ms", C.c_double), ("scan_ms", C.c_double),
+                ("max_inflate_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: (round(getattr(self, k), 3) if t is C.c_double else int(getattr(self, k))) for k, t in self._fields_}
+
+
 class RegionServer:
     """Region queries over resident BAMs with their BAIs, batched continuously
     into one persistent inflate per tick (frt_server_*)."""
@@ -1259,6 +1269,12 @@ class RegionServer:
 
     def set_limits(self, max_requests_per_tick: int = 0, max_ticks_in_flight: int = 2) -> None:
         lib().frt_server_set_limits(self._h, max_requests_per_tick, max_ticks_in_flight)
+
+    def stats(self, reset: bool = False) -> dict:
+        """Per-stage totals over finished ticks (frt_server_get_stats)."""
+        st = ServerStats()
+        lib().frt_server_get_stats(self._h, C.byref(st), int(reset))
+        return st.as_dict()
 
     def clock_ms(self) -> float:
         return lib().frt_server_clock_ms(self._h)

@@ -106,6 +106,12 @@ __device__ __forceinline__ void load64(const u8 *buf, u64 p0, u64 lo, u64 hi, bo
 }
 
 
+// 0x80 in every byte of x that is zero, 0 elsewhere (exact: no borrow runs
+// between bytes, as the high bits are handled apart from the low seven).
+__device__ __forceinline__ u32 zero_bytes(u32 x) { return ~(((x & 0x7f7f7f7fu) + 0x7f7f7f7fu) | x | 0x7f7f7f7fu); }
+// The four 0x80-or-0 bytes of z as bits 0..3 (byte order).
+__device__ __forceinline__ u32 byte_bits(u32 z) { return ((z >> 7) * 0x01020408u) >> 24; }
+
 // =============================================================================
 // FASTQ
 // =============================================================================
@@ -122,7 +128,7 @@ __global__ void __launch_bounds__(TB) k_fq_nl_count(const u8 *buf, u64 lo, u64 h
     if (last_nl && hi > lo && hi - 1 >= p0 && hi - 1 < p0 + CH) *last_nl = buf[hi - 1] == '\n' ? 1u : 0u;
     u32 c = 0;
 #pragma unroll
-    for (int k = 0; k < 16; ++k) c += __popc(__vcmpeq4(w[k], 0x0a0a0a0au)) >> 3;
+    for (int k = 0; k < 16; ++k) c += __popc(zero_bytes(w[k] ^ 0x0a0a0a0au));
     u32 tot;
     block_excl_sum<u32>(c, s_warp, &tot);
     if (threadIdx.x == 0) tile_count[blockIdx.x] = tot;
@@ -130,8 +136,10 @@ __global__ void __launch_bounds__(TB) k_fq_nl_count(const u8 *buf, u64 lo, u64 h
 
 // Positions in `buf` less `shift` are written: a caller whose batch starts
 // `shift` bytes past a 16-byte boundary passes that boundary as `buf`.
+// lf[i] gets the byte after newline i (the first byte of the next line, 0
+// past the batch), so that line tests need no scattered byte reads.
 __global__ void __launch_bounds__(TB) k_fq_nl_emit(const u8 *buf, u64 lo, u64 hi, u64 tbase, bool aligned,
-                                                   const u32 *tile_base, u64 *nl, u64 shift)
+                                                   const u32 *tile_base, u64 *nl, u8 *lf, u64 shift)
 {
     __shared__ u32 s_warp[TB / 32];
     u64 p0 = tbase + (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
@@ -140,17 +148,21 @@ __global__ void __launch_bounds__(TB) k_fq_nl_emit(const u8 *buf, u64 lo, u64 hi
     u32 m[16], c = 0;
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-        m[k] = __vcmpeq4(w[k], 0x0a0a0a0au);
-        c += __popc(m[k]) >> 3;
+        m[k] = zero_bytes(w[k] ^ 0x0a0a0a0au);
+        c += __popc(m[k]);
     }
     u32 at = tile_base[blockIdx.x] + block_excl_sum<u32>(c, s_warp, nullptr);
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
         u32 mk = m[k];
         while (mk) {
-            int b = __ffs(mk) - 1;
-            nl[at++] = p0 + 4 * k + (b >> 3) - shift;
-            mk &= ~(0xffu << (b & ~7));
+            const int b = (__ffs(mk) - 1) >> 3; // byte of the word
+            const u32 next = b < 3 ? (w[k] >> (8 * (b + 1))) & 0xffu
+                                   : (k < 15 ? w[k + 1 < 16 ? k + 1 : 15] & 0xffu
+                                             : (p0 + CH < hi ? (u32)buf[p0 + CH] : 0u));
+            lf[at] = (u8)next;
+            nl[at++] = p0 + 4 * k + b - shift;
+            mk &= mk - 1;
         }
     }
 }
@@ -160,16 +172,18 @@ struct FqIndex {
     u64 start, len;
     const u64 *nl;
     u32 n_nl, n_lines;
+    const u8 *lf; // lf[i]: the byte after newline i
     __device__ __forceinline__ u64 ls(u32 k) const { return k == 0 ? start : nl[k - 1] + 1; }
+    // the first byte of line k (a line that starts inside the batch)
+    __device__ __forceinline__ u32 first(u32 k) const { return k == 0 ? buf[start] : lf[k - 1]; }
     // end of the record whose definition is line k (valid record assumed)
     __device__ __forceinline__ u64 rec_end(u32 k) const { return k + 3 < n_nl ? nl[k + 3] + 1 : len; }
-    __device__ __forceinline__ bool blank(u32 k) const { return buf[ls(k)] == '\n'; }
+    __device__ __forceinline__ bool blank(u32 k) const { return first(k) == '\n'; }
     // bounds_at (fastq record.rs:79-130) from the index
     __device__ __forceinline__ bool valid(u32 k) const
     {
-        u64 p = ls(k);
-        if (buf[p] != '@' || k + 2 >= n_nl) return false;
-        if (buf[nl[k + 1] + 1] != '+') return false;
+        if (first(k) != '@' || k + 2 >= n_nl) return false;
+        if (lf[k + 1] != '+') return false;
         u64 seq_len = nl[k + 1] - nl[k] - 1;
         u64 qs = nl[k + 2] + 1, qe = k + 3 < n_nl ? nl[k + 3] : len;
         return qe - qs == seq_len;
@@ -193,7 +207,7 @@ __global__ void k_tx_lines(FqIndex ix, u32 comment, u32 secondary, u32 *is_rec, 
     const u64 s = ix.ls(k);
     u32 r = 0, h = 0;
     if (s < ix.len) {
-        const u32 first = ix.buf[s];
+        const u32 first = ix.first(k);
         if (first != '\n') {
             h = (first == comment || (secondary < 256u && first == secondary)) ? 1u : 0u;
             r = 1u - h;
@@ -232,12 +246,12 @@ struct TabSplit {
     }
 };
 
-// Bit i set when byte i of the block is a tab: __vcmpeq4 marks a byte 0xff,
+// Bit i set when byte i of the block is a tab: zero_bytes marks a byte 0x80,
 // and the multiply gathers the four top bits (7, 15, 23, 31) to bits 28-31
 // (its partial products never overlap, so nothing carries).
 __device__ __forceinline__ u32 tab_bits(uint4 v)
 {
-    auto f = [](u32 w) { return ((__vcmpeq4(w, 0x09090909u) & 0x80808080u) * 0x00204081u) >> 28; };
+    auto f = [](u32 w) { return (zero_bytes(w ^ 0x09090909u) * 0x00204081u) >> 28; };
     return f(v.x) | (f(v.y) << 4) | (f(v.z) << 8) | (f(v.w) << 12);
 }
 
@@ -557,8 +571,8 @@ __global__ void __launch_bounds__(TB) k_bcf_sieve(const u8 *buf, u64 start, u64 
 // The single-pass sieve: the tile, staged with 16-byte loads from the
 // 16-byte boundary at or before the batch (`abuf`, `sh` bytes before `buf`),
 // is tested at every offset, first by the 24-bit n_sample match four offsets
-// at a time (two shared-memory words, two funnel shifts and three byte
-// compares), then by bcf_plausible.  Candidates go in position order into the
+// at a time (two shared-memory words, two funnel shifts, the three bytes
+// compared by XOR and one zero-byte test), then by bcf_plausible.  Candidates go in position order into the
 // tile's slot of `lists` (SIEVE_CAP entries) and their number into
 // tile_count; a tile with more than SIEVE_CAP sets *overflow and the caller
 // runs the two-pass sieve instead.  The full validation of the candidates
@@ -602,16 +616,17 @@ __global__ void __launch_bounds__(TB) k_bcf_sieve1(const u8 *abuf, u64 sh, u64 s
     const u32 *s32 = reinterpret_cast<const u32 *>(s);
     const u32 b0 = (samples & 0xffu) * 0x01010101u, b1 = ((samples >> 8) & 0xffu) * 0x01010101u,
               b2 = ((samples >> 16) & 0xffu) * 0x01010101u;
-    constexpr u32 PER = SIEVE_TILE / TB; // offsets a thread tests, a multiple of 4
+    // groups of four offsets, consecutive lanes on consecutive groups (their
+    // shared-memory words fall in different banks)
 #pragma unroll 2
-    for (u32 g = 0; g < PER; g += 4) {
-        const u32 q = threadIdx.x * PER + g; // tile-relative, a multiple of 4
+    for (u32 g = threadIdx.x; g < SIEVE_TILE / 4; g += TB) {
+        const u32 q = 4u * g; // tile-relative
         const u32 w0 = s32[(q + 28) >> 2], w1 = s32[(q + 32) >> 2];
-        u32 m = __vcmpeq4(w0, b0) & __vcmpeq4(__funnelshift_r(w0, w1, 8), b1) &
-                __vcmpeq4(__funnelshift_r(w0, w1, 16), b2);
+        // byte k is zero where all three n_sample bytes match at offset q + k
+        u32 m = zero_bytes((w0 ^ b0) | (__funnelshift_r(w0, w1, 8) ^ b1) | (__funnelshift_r(w0, w1, 16) ^ b2));
         while (m) {
             const u32 k = (u32)(__ffs(m) - 1) >> 3;
-            m &= ~(0xffu << (8 * k));
+            m &= m - 1;
             const u64 pa = T0 + q + k; // abuf coordinates
             if (pa < lo || pa >= hi) continue;
             const u64 pos = pa - sh;
@@ -834,16 +849,20 @@ struct FaMasks {
     u64 valid, nl, ls, hs, O, K;
 };
 
-__device__ __forceinline__ u32 nibble_of(u32 m) { return (((m >> 7) & 0x01010101u) * 0x01020408u) >> 24; }
 
 __device__ __forceinline__ void fa_masks(const u8 *abuf, u64 lo, u64 hi, u64 p0, FaMasks &f, u32 w[16])
 {
     load64(abuf, p0, lo, hi, true, w);
     u64 nl = 0, gt = 0;
+    u32 any_gt = 0;
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-        nl |= (u64)nibble_of(__vcmpeq4(w[k], 0x0a0a0a0au)) << (4 * k);
-        gt |= (u64)nibble_of(__vcmpeq4(w[k], 0x3e3e3e3eu)) << (4 * k);
+        nl |= (u64)byte_bits(zero_bytes(w[k] ^ 0x0a0a0a0au)) << (4 * k);
+        any_gt |= zero_bytes(w[k] ^ 0x3e3e3e3eu);
+    }
+    if (any_gt) { // '>' is rare: its mask is built only where one occurs
+#pragma unroll
+        for (int k = 0; k < 16; ++k) gt |= (u64)byte_bits(zero_bytes(w[k] ^ 0x3e3e3e3eu)) << (4 * k);
     }
     u64 valid = ~0ull;
     if (p0 < lo) valid &= lo - p0 >= 64 ? 0ull : ~0ull << (lo - p0);
@@ -1324,12 +1343,13 @@ extern "C" int frt_fastq_decode(frt_fastq_scanner *sc, const frt_inflate_batch *
     if ((rc = read_back(st, d_u32, hd, sizeof hd, err, "newline count"))) return rc;
     const uint32_t n_nl = hd[0];
     u64 *nl;
-    if ((rc = w.get(&nl, (size_t)n_nl + 1, err))) return rc;
-    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, sh);
+    u8 *lf;
+    if ((rc = w.get(&nl, (size_t)n_nl + 1, err)) || (rc = w.get(&lf, (size_t)n_nl + 1, err))) return rc;
+    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, lf, sh);
     LAUNCH_OK("launching the newline index");
     // line starts: start, and one past every newline that is not the last byte
     const uint32_t n_lines = n_nl && hd[7] ? n_nl : n_nl + 1;
-    FqIndex ix{b->data, start, len, nl, n_nl, n_lines};
+    FqIndex ix{b->data, start, len, nl, n_nl, n_lines, lf};
     u32 *flags, *pos, *S, *W, *fails;
     if ((rc = w.get(&flags, n_lines, err)) || (rc = w.get(&pos, (size_t)n_lines + 1, err)) ||
         (rc = w.get(&fails, 4, err)))
@@ -1902,12 +1922,13 @@ extern "C" int frt_text_scan(frt_text_scanner *sc, const frt_inflate_batch *b, u
     if ((rc = read_back(st, d_u32, hd, sizeof hd, err, "newline count"))) return rc;
     const uint32_t n_nl = hd[0];
     u64 *nl;
-    if ((rc = w.get(&nl, (size_t)n_nl + 1, err))) return rc;
-    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, sh);
+    u8 *lf;
+    if ((rc = w.get(&nl, (size_t)n_nl + 1, err)) || (rc = w.get(&lf, (size_t)n_nl + 1, err))) return rc;
+    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, lf, sh);
     LAUNCH_OK("launching the newline index");
     // line starts: start, and one past every newline that is not the last byte
     const uint32_t n_lines = n_nl && hd[7] ? n_nl : n_nl + 1;
-    FqIndex ix{b->data, start, len, nl, n_nl, n_lines};
+    FqIndex ix{b->data, start, len, nl, n_nl, n_lines, lf};
     u32 *is_rec, *is_hdr, *rec_pos, *hdr_pos;
     if ((rc = w.get(&is_rec, n_lines, err)) || (rc = w.get(&is_hdr, n_lines, err)) ||
         (rc = w.get(&rec_pos, (size_t)n_lines + 1, err)) || (rc = w.get(&hdr_pos, (size_t)n_lines + 1, err)))

@@ -83,6 +83,8 @@ struct Tick {
     uint8_t *arena = nullptr;
     FrtRegionColumns cols{};
     cudaEvent_t done = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_inflate = nullptr, ev_inflated = nullptr; // the tick's stages on the device
+    double host_ms = 0;          // host time building and launching the tick
     void *host_status = nullptr; // pinned
     size_t host_bytes = 0;
     uint64_t budget_bytes = 0;
@@ -101,6 +103,8 @@ struct Tick {
     {
         for (void *p : allocs) cudaFreeAsync(p, stream);
         if (done) cudaEventDestroy(done);
+        for (cudaEvent_t ev : {ev_start, ev_inflate, ev_inflated})
+            if (ev) cudaEventDestroy(ev);
         if (host_status) cudaFreeHost(host_status);
         if (staging) cudaFreeHost(staging);
         if (in_use) *in_use -= budget_bytes;
@@ -128,6 +132,7 @@ struct frt_server {
     frt_inflate_tuning tuning{};
     int inflate_grid = 0;
     uint64_t pending = 0;         // submitted, not yet completed
+    frt_server_stats stats{};     // per-stage totals over finished ticks
 };
 
 namespace {
@@ -221,8 +226,11 @@ template <typename T> int talloc(Tick &t, T **p, size_t n, frt_error *err)
 // Launches one tick over `batch`.
 int launch_tick(frt_server *sv, std::vector<SrvReq *> &batch, frt_error *err)
 {
+    const double h0 = host_ms(sv->t0);
     auto t = std::make_shared<Tick>();
     t->stream = sv->stream;
+    for (cudaEvent_t *ev : {&t->ev_start, &t->ev_inflate, &t->ev_inflated}) cudaEventCreate(ev);
+    cudaEventRecord(t->ev_start, sv->stream);
     Plan pl;
     for (uint32_t i = 0; i < batch.size(); ++i) plan_request(sv, *batch[i], i, pl, *t);
     const uint32_t n = (uint32_t)pl.in_off.size(), ns = (uint32_t)pl.segs.size();
@@ -300,10 +308,12 @@ int launch_tick(frt_server *sv, std::vector<SrvReq *> &batch, frt_error *err)
         (e = cudaMemsetAsync(totals, 0, 32ull * ns + 32, st)))
         return cuda_fail(err, e, "uploading a tick");
     // inflate every member of the tick
+    cudaEventRecord(t->ev_inflate, st);
     if ((e = frt_launch_inflate_persistent(sv->files_arena, in_off, in_len, t->arena, out_off, isize, crc, status,
                                            produced, crc_out, order, n_dev, n, pl.arena_bytes, (u32 *)queue_head,
                                            (u32)sv->inflate_grid, block_err, sv->tuning, st)) != cudaSuccess)
         return cuda_fail(err, e, "launching the inflate");
+    cudaEventRecord(t->ev_inflated, st);
     int32_t n_ref = 0; // bounds refID in the record-start test
     for (SrvReq *r : batch) n_ref = std::max(n_ref, sv->files[r->file].n_ref < 0 ? (1 << 24) : sv->files[r->file].n_ref);
     if ((e = frt_launch_region_scan(t->arena, segs, seg_of, ns, n, n_ref, starts, coff, entry, count, land, flags,
@@ -329,6 +339,7 @@ int launch_tick(frt_server *sv, std::vector<SrvReq *> &batch, frt_error *err)
     sv->in_use += t->budget_bytes;
     t->in_use = &sv->in_use; // released when the tick's memory is
     sv->running.push_back(t);
+    t->host_ms = host_ms(sv->t0) - h0;
     return FRT_OK;
 }
 
@@ -338,6 +349,21 @@ void finish_tick(frt_server *sv, std::shared_ptr<Tick> t, uint32_t *completed)
     float ms = 0;
     cudaEventElapsedTime(&ms, sv->origin, t->done);
     const uint32_t n = t->n_members, ns = t->n_segs;
+    {
+        float up = 0, inf = 0, rest = 0;
+        cudaEventElapsedTime(&up, t->ev_start, t->ev_inflate);
+        cudaEventElapsedTime(&inf, t->ev_inflate, t->ev_inflated);
+        cudaEventElapsedTime(&rest, t->ev_inflated, t->done);
+        frt_server_stats &st = sv->stats;
+        st.ticks++;
+        st.requests += t->reqs.size();
+        st.members += n;
+        st.host_ms += t->host_ms;
+        st.upload_ms += up;
+        st.inflate_ms += inf;
+        st.scan_ms += rest;
+        if (inf > st.max_inflate_ms) st.max_inflate_ms = inf;
+    }
     const uint8_t *hs = (const uint8_t *)t->host_status;
     const uint32_t *status = (const uint32_t *)hs;
     const uint32_t *kept_first = (const uint32_t *)(hs + 4ull * n);
@@ -439,6 +465,14 @@ extern "C" void frt_server_set_limits(frt_server *s, uint32_t max_requests_per_t
 }
 
 extern "C" double frt_server_clock_ms(const frt_server *s) { return s ? host_ms(s->t0) : 0.0; }
+
+extern "C" int frt_server_get_stats(const frt_server *s, frt_server_stats *out, int32_t reset)
+{
+    if (!s || !out) return FRT_ERR_INVALID_ARGUMENT;
+    *out = s->stats;
+    if (reset) const_cast<frt_server *>(s)->stats = frt_server_stats{};
+    return FRT_OK;
+}
 
 extern "C" int frt_server_add_bam(frt_server *s, const uint8_t *bgzf, size_t len, const uint8_t *bai, size_t bai_len,
                                   int32_t *file_id, frt_error *err)

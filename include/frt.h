@@ -558,6 +558,17 @@ void frt_server_destroy(frt_server *s);
 void frt_server_set_limits(frt_server *s, uint32_t max_requests_per_tick, uint32_t max_ticks_in_flight);
 /* Milliseconds since the server was created (the clock of arrival_ms/done_ms). */
 double frt_server_clock_ms(const frt_server *s);
+/* Where the time of finished ticks went, summed over ticks: host time to plan,
+ * allocate and launch them; device time from a tick's start to its inflate
+ * (the table uploads, and any wait behind the tick before it on the stream),
+ * in the persistent inflate, and from there to completion (region scan,
+ * filter, emit, status copy).  No reference counterpart.  `reset` zeroes
+ * the totals after reading them. */
+typedef struct {
+    uint64_t ticks, requests, members;
+    double host_ms, upload_ms, inflate_ms, scan_ms, max_inflate_ms;
+} frt_server_stats;
+int frt_server_get_stats(const frt_server *s, frt_server_stats *out, int32_t reset);
 /* Makes a BGZF BAM and its BAI resident (before the first request). */
 int frt_server_add_bam(frt_server *s, const uint8_t *bgzf, size_t len, const uint8_t *bai, size_t bai_len,
                        int32_t *file_id, frt_error *err);
