@@ -149,7 +149,8 @@ class InflateTuning(C.Structure):
 
 class InflateVariant(C.Structure):
     _fields_ = [("lit_bits", C.c_int32), ("dist_bits", C.c_int32), ("window", C.c_int32), ("queue", C.c_int32),
-                ("max_registers", C.c_int32), ("chains", C.c_int32), ("smem_per_warp", C.c_uint64)]
+                ("max_registers", C.c_int32), ("chains", C.c_int32), ("stage_half", C.c_int32),
+                ("smem_per_warp", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -1267,7 +1268,7 @@ class RegionServer:
         _raise(lib().frt_server_create(device, stream, int(budget_bytes), C.byref(h), C.byref(err)), err)
         self._h = h
 
-    def set_limits(self, max_requests_per_tick: int = 0, max_ticks_in_flight: int = 2) -> None:
+    def set_limits(self, max_requests_per_tick: int = 0, max_ticks_in_flight: int = 1) -> None:
         lib().frt_server_set_limits(self._h, max_requests_per_tick, max_ticks_in_flight)
 
     def stats(self, reset: bool = False) -> dict:

@@ -26,6 +26,9 @@ enum : u32 {
     INF_BAD_TABLE = 7,
     INF_BAD_LENGTH_REPEAT = 8,
     INF_BAD_COUNTS = 9,
+    // not a reference code: a staging copy of the compressed member did not
+    // complete within its bound (a device fault, not a property of the data)
+    INF_STAGING_TIMEOUT = 10,
 };
 
 __device__ __forceinline__ u32 ld_u32le(const u8 *p)

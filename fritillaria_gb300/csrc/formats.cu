@@ -587,7 +587,6 @@ __global__ void __launch_bounds__(TB) k_bcf_sieve1(const u8 *abuf, u64 sh, u64 s
     __shared__ __align__(16) u8 s[SIEVE_TILE + 48];
     __shared__ u64 s_list[SIEVE_CAP];
     __shared__ u32 s_n;
-    const u8 *buf = abuf + sh;
     const u64 lo = start + sh, hi = len + sh; // candidate positions, in abuf coordinates
     const u64 T0 = (lo & ~15ull) + (u64)blockIdx.x * SIEVE_TILE;
     for (u32 i = threadIdx.x; i < (SIEVE_TILE + 48) / 16; i += TB) {
@@ -911,75 +910,6 @@ __device__ __forceinline__ u64 fa_keep(const FaMasks &f, u32 s)
     return (s == 2u ? pre : 0ull) | (s != 0u ? (other & below) : 0ull) | (other & ~below);
 }
 
-// One block: per tile its entry state and first contig index; the contig
-// count, and whether the last record's definition line is unterminated (such a
-// record is not a record, fasta record.rs:101-110).
-__global__ void __launch_bounds__(1024) k_fa_tiles(const u8 *buf, u64 len, const u8 *tile_f, const u32 *tile_contigs,
-                                                   u32 n_tiles, u8 *tile_state, u32 *contig_base,
-                                                   const unsigned long long *last_contig, u64 *totals)
-{
-    __shared__ u32 s_a[32], s_b[32];
-    u32 carry_f = F_ID, carry_c = 0;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (u32 b0 = 0; b0 < n_tiles; b0 += 1024) {
-        u32 t = b0 + threadIdx.x;
-        u32 f = t < n_tiles ? tile_f[t] : F_ID, c = t < n_tiles ? tile_contigs[t] : 0u;
-        u32 xf = f, xc = c;
-        for (int o = 1; o < 32; o <<= 1) {
-            u32 yf = __shfl_up_sync(FRT_FULL_MASK, xf, o), yc = __shfl_up_sync(FRT_FULL_MASK, xc, o);
-            if (lane >= o) {
-                xf = f_then(yf, xf);
-                xc += yc;
-            }
-        }
-        if (lane == 31) {
-            s_a[wid] = xf;
-            s_b[wid] = xc;
-        }
-        __syncthreads();
-        if (wid == 0) {
-            u32 wf = s_a[lane], wc = s_b[lane];
-            for (int o = 1; o < 32; o <<= 1) {
-                u32 yf = __shfl_up_sync(FRT_FULL_MASK, wf, o), yc = __shfl_up_sync(FRT_FULL_MASK, wc, o);
-                if (lane >= o) {
-                    wf = f_then(yf, wf);
-                    wc += yc;
-                }
-            }
-            s_a[lane] = wf;
-            s_b[lane] = wc;
-        }
-        __syncthreads();
-        // exclusive prefix for this thread within the chunk of 1024
-        u32 ef = __shfl_up_sync(FRT_FULL_MASK, xf, 1), ec = __shfl_up_sync(FRT_FULL_MASK, xc, 1);
-        if (lane == 0) {
-            ef = F_ID;
-            ec = 0;
-        }
-        u32 pf = wid ? s_a[wid - 1] : F_ID, pc = wid ? s_b[wid - 1] : 0u;
-        u32 before = f_then(carry_f, f_then(pf, ef));
-        if (t < n_tiles) {
-            tile_state[t] = (u8)f_apply(before, 0u);
-            contig_base[t] = carry_c + pc + ec;
-        }
-        u32 all_f = s_a[31], all_c = s_b[31];
-        __syncthreads();
-        carry_f = f_then(carry_f, all_f);
-        carry_c += all_c;
-    }
-    if (threadIdx.x == 0) {
-        u64 n = carry_c;
-        u64 drop = 0;
-        if (n && *last_contig) {
-            u64 p = *last_contig - 1;
-            while (p < len && buf[p] != '\n') ++p;
-            drop = p >= len;
-        }
-        totals[0] = n - drop; // contigs
-        totals[2] = drop;
-    }
-}
-
 // Pass 1, per tile of TILE bytes (abuf coordinates from 0): the transfer
 // function, the record starts, and the bytes kept when the tile is entered in
 // each state (3 per tile); the position after the last record start goes to
@@ -1011,11 +941,136 @@ __global__ void __launch_bounds__(TB) k_fa_sum(const u8 *abuf, u64 sh, u64 len, 
     }
 }
 
-// The kept count of each tile for the state it is entered in.
-__global__ void k_fa_select(const u32 *tile_kept3, const u8 *tile_state, u32 n_tiles, u32 *tile_kept)
+// The tiles' layout, in three parallel steps over chunks of 1,024 tiles (a
+// chunk a block): each chunk's composed function, record count and kept
+// bytes for each entering state; one block scans the chunks from state 0 at
+// the batch start; each chunk then gives its tiles their entry state, first
+// contig and output offset.
+
+// Exclusive scan across a block of 1,024 threads under an associative `op`
+// (earlier element on the left); *total gets the whole block's result.
+template <class T, class Op> __device__ __forceinline__ T excl_scan1024(T x, T id, Op op, T *s_w, T *total)
 {
-    const u32 t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n_tiles) tile_kept[t] = tile_kept3[3 * t + tile_state[t]];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    T inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const T y = __shfl_up_sync(FRT_FULL_MASK, inc, o);
+        if (lane >= o) inc = op(y, inc);
+    }
+    if (lane == 31) s_w[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        T wv = s_w[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const T y = __shfl_up_sync(FRT_FULL_MASK, wv, o);
+            if (lane >= o) wv = op(y, wv);
+        }
+        s_w[lane] = wv;
+    }
+    __syncthreads();
+    T ex = __shfl_up_sync(FRT_FULL_MASK, inc, 1);
+    if (lane == 0) ex = id;
+    const T r = wid ? op(s_w[wid - 1], ex) : ex;
+    if (total) *total = s_w[31];
+    __syncthreads();
+    return r;
+}
+
+struct FaCompose {
+    __device__ __forceinline__ u32 operator()(u32 f, u32 g) const { return f_then(f, g); }
+};
+struct AddU64 {
+    __device__ __forceinline__ u64 operator()(u64 a, u64 b) const { return a + b; }
+};
+
+__global__ void __launch_bounds__(1024) k_fa_chunks(const u8 *tile_f, const u32 *tile_contigs, const u32 *tile_kept3,
+                                                    u32 n_tiles, u8 *chunk_f, u32 *chunk_contigs, u64 *chunk_kept3)
+{
+    __shared__ u32 s_f[32];
+    __shared__ u64 s_k[32];
+    const u32 t = blockIdx.x * 1024 + threadIdx.x;
+    const bool in = t < n_tiles;
+    const u32 f = in ? tile_f[t] : F_ID;
+    u32 all_f;
+    const u32 ex = excl_scan1024<u32>(f, F_ID, FaCompose(), s_f, &all_f);
+    u64 c_all;
+    excl_scan1024<u64>(in ? tile_contigs[t] : 0u, 0ull, AddU64(), s_k, &c_all);
+    u64 k_all[3];
+#pragma unroll
+    for (u32 st = 0; st < 3; ++st)
+        excl_scan1024<u64>(in ? tile_kept3[3 * t + f_apply(ex, st)] : 0u, 0ull, AddU64(), s_k, &k_all[st]);
+    if (threadIdx.x == 0) {
+        chunk_f[blockIdx.x] = (u8)all_f;
+        chunk_contigs[blockIdx.x] = (u32)c_all;
+        for (u32 st = 0; st < 3; ++st) chunk_kept3[3 * blockIdx.x + st] = k_all[st];
+    }
+}
+
+// One block over the chunks: entry state, first contig and output offset of
+// each chunk; totals = contigs, bases, whether the last record was dropped.  A
+// record whose definition line is not terminated is not a record
+// (fasta record.rs:101-110): the last record start (*last_contig - 1) is
+// checked for a newline after it.
+__global__ void __launch_bounds__(1024) k_fa_top(const u8 *buf, u64 len, const u8 *chunk_f, const u32 *chunk_contigs,
+                                                 const u64 *chunk_kept3, u32 n_chunks, u8 *chunk_state,
+                                                 u64 *chunk_contig_base, u64 *chunk_out_base,
+                                                 const unsigned long long *last_contig, u64 *totals)
+{
+    __shared__ u32 s_f[32];
+    __shared__ u64 s_k[32];
+    u32 carry_f = F_ID;
+    u64 carry_c = 0, carry_o = 0;
+    for (u32 b0 = 0; b0 < n_chunks; b0 += 1024) {
+        const u32 c = b0 + threadIdx.x;
+        const bool in = c < n_chunks;
+        u32 all_f;
+        const u32 ex = excl_scan1024<u32>(in ? chunk_f[c] : F_ID, F_ID, FaCompose(), s_f, &all_f);
+        const u32 state = f_apply(f_then(carry_f, ex), 0u);
+        u64 all_c, all_o;
+        const u64 cb = excl_scan1024<u64>(in ? chunk_contigs[c] : 0u, 0ull, AddU64(), s_k, &all_c);
+        const u64 ob = excl_scan1024<u64>(in ? chunk_kept3[3 * c + state] : 0ull, 0ull, AddU64(), s_k, &all_o);
+        if (in) {
+            chunk_state[c] = (u8)state;
+            chunk_contig_base[c] = carry_c + cb;
+            chunk_out_base[c] = carry_o + ob;
+        }
+        carry_f = f_then(carry_f, all_f);
+        carry_c += all_c;
+        carry_o += all_o;
+    }
+    if (threadIdx.x == 0) {
+        u64 drop = 0;
+        if (carry_c && *last_contig) {
+            u64 p = *last_contig - 1;
+            while (p < len && buf[p] != '\n') ++p;
+            drop = p >= len;
+        }
+        totals[0] = carry_c - drop;
+        totals[1] = carry_o;
+        totals[2] = drop;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_fa_apply(const u8 *tile_f, const u32 *tile_contigs, const u32 *tile_kept3,
+                                                   u32 n_tiles, const u8 *chunk_state, const u64 *chunk_contig_base,
+                                                   const u64 *chunk_out_base, u8 *tile_state, u32 *contig_base,
+                                                   u64 *out_base)
+{
+    __shared__ u32 s_f[32];
+    __shared__ u64 s_k[32];
+    const u32 t = blockIdx.x * 1024 + threadIdx.x;
+    const bool in = t < n_tiles;
+    const u32 ex = excl_scan1024<u32>(in ? tile_f[t] : F_ID, F_ID, FaCompose(), s_f, nullptr);
+    const u32 state = f_apply(ex, chunk_state[blockIdx.x]);
+    const u64 cb = excl_scan1024<u64>(in ? tile_contigs[t] : 0u, 0ull, AddU64(), s_k, nullptr);
+    const u64 ob = excl_scan1024<u64>(in ? tile_kept3[3 * t + state] : 0u, 0ull, AddU64(), s_k, nullptr);
+    if (in) {
+        tile_state[t] = (u8)state;
+        contig_base[t] = (u32)(chunk_contig_base[blockIdx.x] + cb);
+        out_base[t] = chunk_out_base[blockIdx.x] + ob;
+    }
 }
 
 // Pass 2: each tile's kept bytes, compacted in order through a shared-memory
@@ -1076,39 +1131,6 @@ __global__ void k_fa_lengths(const u64 *seq_off, u64 n, u64 total, u64 *seq_len)
 {
     u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) seq_len[i] = (i + 1 < n ? seq_off[i + 1] : total) - seq_off[i];
-}
-
-// Exclusive u64 scan of u32 tile values, one block (tiles number in the
-// hundreds of thousands at most).
-__global__ void __launch_bounds__(1024) k_scan_tiles64(const u32 *in, u32 n, u64 *out, u64 *total)
-{
-    __shared__ u64 s_w[32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    u64 carry = 0;
-    for (u32 b0 = 0; b0 < n; b0 += 1024) {
-        u32 t = b0 + threadIdx.x;
-        u64 v = t < n ? in[t] : 0, x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            u64 y = __shfl_up_sync(FRT_FULL_MASK, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane == 31) s_w[wid] = x;
-        __syncthreads();
-        if (wid == 0) {
-            u64 w = s_w[lane];
-            for (int o = 1; o < 32; o <<= 1) {
-                u64 y = __shfl_up_sync(FRT_FULL_MASK, w, o);
-                if (lane >= o) w += y;
-            }
-            s_w[lane] = w;
-        }
-        __syncthreads();
-        if (t < n) out[t] = carry + x - v + (wid ? s_w[wid - 1] : 0);
-        u64 all = s_w[31];
-        __syncthreads();
-        carry += all;
-    }
-    if (threadIdx.x == 0) *total = carry;
 }
 
 unsigned grid_for(u64 n, unsigned block) { return (unsigned)((n + block - 1) / block); }
@@ -1724,22 +1746,32 @@ extern "C" int frt_fasta_compact(frt_fasta_compactor *sc, const frt_inflate_batc
     const u8 *abuf = b->data - sh;
     const u64 n_tiles2 = (len + sh + TILE - 1) / TILE;
     u8 *tile_f, *tile_state;
-    u32 *tile_contigs, *contig_base, *tile_kept, *tile_kept3;
+    u32 *tile_contigs, *contig_base, *tile_kept3;
     u64 *out_base, *totals;
     unsigned long long *last_contig;
     if ((rc = w.get(&tile_f, n_tiles2, err)) || (rc = w.get(&tile_state, n_tiles2, err)) ||
         (rc = w.get(&tile_contigs, n_tiles2, err)) || (rc = w.get(&contig_base, n_tiles2, err)) ||
-        (rc = w.get(&tile_kept, n_tiles2, err)) || (rc = w.get(&tile_kept3, 3 * n_tiles2, err)) ||
+        (rc = w.get(&tile_kept3, 3 * n_tiles2, err)) ||
         (rc = w.get(&out_base, n_tiles2 + 1, err)) || (rc = w.get(&totals, 8, err)) ||
         (rc = w.get(&last_contig, 2, err)))
         return rc;
     cudaMemsetAsync(last_contig, 0, 16, st);
     cudaMemsetAsync(totals, 0, 64, st);
+    const u32 n_chunks = (u32)((n_tiles2 + 1023) / 1024);
+    u8 *chunk_f, *chunk_state;
+    u32 *chunk_contigs;
+    u64 *chunk_kept3, *chunk_contig_base, *chunk_out_base;
+    if ((rc = w.get(&chunk_f, n_chunks, err)) || (rc = w.get(&chunk_state, n_chunks, err)) ||
+        (rc = w.get(&chunk_contigs, n_chunks, err)) || (rc = w.get(&chunk_kept3, 3ull * n_chunks, err)) ||
+        (rc = w.get(&chunk_contig_base, n_chunks, err)) || (rc = w.get(&chunk_out_base, n_chunks, err)))
+        return rc;
     k_fa_sum<<<(unsigned)n_tiles2, TB, 0, st>>>(abuf, sh, len, tile_f, tile_contigs, tile_kept3, last_contig);
-    k_fa_tiles<<<1, 1024, 0, st>>>(b->data, len, tile_f, tile_contigs, (u32)n_tiles2, tile_state, contig_base,
-                                   last_contig, totals);
-    k_fa_select<<<grid_for(n_tiles2, 256), 256, 0, st>>>(tile_kept3, tile_state, (u32)n_tiles2, tile_kept);
-    k_scan_tiles64<<<1, 1024, 0, st>>>(tile_kept, (u32)n_tiles2, out_base, totals + 1);
+    k_fa_chunks<<<n_chunks, 1024, 0, st>>>(tile_f, tile_contigs, tile_kept3, (u32)n_tiles2, chunk_f, chunk_contigs,
+                                           chunk_kept3);
+    k_fa_top<<<1, 1024, 0, st>>>(b->data, len, chunk_f, chunk_contigs, chunk_kept3, n_chunks, chunk_state,
+                                 chunk_contig_base, chunk_out_base, last_contig, totals);
+    k_fa_apply<<<n_chunks, 1024, 0, st>>>(tile_f, tile_contigs, tile_kept3, (u32)n_tiles2, chunk_state,
+                                          chunk_contig_base, chunk_out_base, tile_state, contig_base, out_base);
     LAUNCH_OK("launching the FASTA scans");
     uint64_t tot[3];
     if ((rc = read_back(st, totals, tot, sizeof tot, err, "FASTA layout"))) return rc;

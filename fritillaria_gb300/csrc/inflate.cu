@@ -29,7 +29,9 @@
 // reference kernel (crates/fritillaria-cuda/kernels/inflate.cu:78-458), so a
 // stream it rejects is rejected here with the same code.
 
+#include <cstddef>
 #include <mutex>
+#include <type_traits>
 
 #include "common.cuh"
 #include "inflate.cuh"
@@ -45,8 +47,9 @@ constexpr u32 MAX_WB = 4096; // the largest window buffer of any variant
 // register cap (more warps per SM against fewer registers per lane).  The
 // library carries a few (kVariants below); a tuning picks one per device and
 // workload.
-template <int LB, int DB, u32 W, u32 Q, int R = 128> struct Cfg {
+template <int LB, int DB, u32 W, u32 Q, int R = 128, u32 S = 0> struct Cfg {
     static constexpr int REGS = R; // register cap per thread (ptxas), trading per-warp speed for occupancy
+    static constexpr u32 STAGE = S; // 0: read the compressed bytes through L1; else staging-ring half (bytes)
     static constexpr int LIT_BITS = LB;
     static constexpr int DIST_BITS = DB;
     static constexpr u32 DIST_BASE = 1u << LB; // distance entries follow the literal/length ones
@@ -61,6 +64,7 @@ template <int LB, int DB, u32 W, u32 Q, int R = 128> struct Cfg {
     static_assert(LB <= 15 && DB <= 15, "roots are at most the longest code");
     static_assert(Q <= 32 * 32, "a lane tracks at most 32 queued matches");
     static_assert(W % 32 == 0 && W > 2 * 258 && W <= MAX_WB, "pending bits cover whole words");
+    static_assert(S == 0 || (S >= 64 && (S & (S - 1)) == 0), "a staging half is a power of two of 64+ bytes");
 };
 
 // CRC-32 tables, computed at compile time: slice[k][b] is the register that
@@ -120,6 +124,11 @@ template <class C> struct WarpSmem {
     u32 pend[C::WB / 32]; // unresolved match destinations in the window
     u64 q[C::MAXQ];       // matches of the window: destination (member offset) | (len | dist << 9) << 32
     alignas(16) u8 win[C::WB + 264];
+    // staging (C::STAGE > 0): two ring halves filled by bulk copies, their
+    // barriers, and the barriers' phases and a give-up flag kept between members
+    alignas(16) u8 ring[C::STAGE ? 2 * C::STAGE : 16];
+    u64 bar[2];
+    u32 phase, broken;
 };
 
 __device__ __forceinline__ u32 lit_entry(u32 sym, u32 L)
@@ -261,11 +270,14 @@ struct LaneBits {
         bit0 = 8u * (u32)(a & 3ull);
         nwords = (bit0 + 8u * in_len + 31u) / 32u;
     }
+    template <class SM> __device__ __forceinline__ void attach(const u8 *in, u32 in_len, SM *) { attach(in, in_len); }
+    template <class SM> __device__ __forceinline__ void finish(SM *) {}
     __device__ __forceinline__ u32 word(u32 i) const { return i < nwords ? __ldg(base + i) : 0u; }
     __device__ __forceinline__ void seek(u32 p)
     {
         u32 a = p + bit0, w = a >> 5, sh = a & 31u;
-        buf = (((u64)word(w + 1) << 32) | word(w)) >> sh;
+        const u32 lo = word(w), hi = word(w + 1); // in order: the staged reader moves forward
+        buf = (((u64)hi << 32) | lo) >> sh;
         cnt = 64 - (int)sh;
         nw = w + 2;
     }
@@ -286,6 +298,164 @@ struct LaneBits {
         cnt -= n;
     }
 };
+
+// ---- staging the compressed bytes by bulk copies ------------------------------
+__device__ __forceinline__ u32 smem_u32(const void *p) { return (u32)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_try_wait(const u64 *bar, u32 parity)
+{
+    u32 ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// One lane's reader of a member whose compressed bytes are staged in shared
+// memory: the member's 16-byte-aligned words go, HALF bytes at a time, into
+// the two halves of a ring by cp.async.bulk copies (1-D, global to shared,
+// completing on one mbarrier per half); while the chain reads chunk c, chunk
+// c + 1 is already being copied.  The copies start at the 16-byte boundary at
+// or before the payload and cover whole 16-byte blocks up to its end; the few
+// words after the last whole block, and reads past the payload, take the
+// plain path of LaneBits.  A wait that does not complete within its bound
+// marks the warp's staging broken (`timeout`): the member fails with
+// INF_STAGING_TIMEOUT and the warp reads through L1 from then on.
+template <class C> struct RingBits {
+    static constexpr u32 HALF = C::STAGE;
+    enum : u32 { PEND0 = 1, PEND1 = 2, PHASE0 = 4, PHASE1 = 8, BROKEN = 16, TIMEOUT = 32 };
+    const u32 *base; // 16-byte-aligned word at or before the payload start
+    u32 nwords, bit0;
+    u64 buf;
+    int cnt;
+    u32 nw;
+    u8 *ring;     // two halves, then the two barriers (WarpSmem::ring, ::bar)
+    u32 bulk;     // bytes from base covered by bulk copies (a multiple of 16)
+    u32 hc0, hc1; // chunk held (or in flight) in each half
+    u32 ready;    // chunk resident and waited for
+    u32 st;       // PEND*, PHASE* (parity of each half's next completion), BROKEN, TIMEOUT
+
+    __device__ __forceinline__ u64 *bar() const { return reinterpret_cast<u64 *>(ring + 2 * HALF); }
+    __device__ __forceinline__ void attach(const u8 *in, u32 in_len, WarpSmem<C> *sm)
+    {
+        static_assert(offsetof(WarpSmem<C>, bar) == offsetof(WarpSmem<C>, ring) + 2 * C::STAGE,
+                      "the barriers follow the ring");
+        const u64 a = (u64)in, b = a & ~15ull;
+        base = (const u32 *)b;
+        bit0 = 8u * (u32)(a - b);
+        nwords = (bit0 + 8u * in_len + 31u) / 32u;
+        const u64 e = (a + in_len) & ~15ull;
+        bulk = e > b ? (u32)(e - b) : 0u;
+        ring = sm->ring;
+        hc0 = hc1 = ready = 0xffffffffu;
+        st = sm->phase * PHASE0 | (sm->broken ? BROKEN : 0u);
+    }
+    __device__ __forceinline__ bool wait(u32 h)
+    {
+        const u32 par = (st >> (2 + h)) & 1u;
+        for (u32 it = 0; it < (1u << 20); ++it) {
+            if (mbar_try_wait(bar() + h, par)) {
+                st ^= PHASE0 << h;
+                st &= ~(PEND0 << h);
+                return true;
+            }
+        }
+        st |= BROKEN | TIMEOUT;
+        return false;
+    }
+    __device__ __forceinline__ void issue(u32 c, u32 h)
+    {
+        const u32 off = c * HALF, bytes = min(HALF, bulk - off);
+        u8 *dst = ring + h * HALF;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); // earlier reads of the half come first
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar() + h)), "r"(bytes)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(dst)),
+                     "l"((const u8 *)base + off), "r"(bytes), "r"(smem_u32(bar() + h))
+                     : "memory");
+        st |= PEND0 << h;
+        if (h) hc1 = c;
+        else hc0 = c;
+    }
+    __device__ __forceinline__ void make_ready(u32 c)
+    {
+        const u32 h = c & 1u, g = h ^ 1u;
+        if ((h ? hc1 : hc0) != c) {
+            if (((st >> h) & 1u) && !wait(h)) return;
+            issue(c, h);
+        }
+        if (((st >> h) & 1u) && !wait(h)) return;
+        ready = c;
+        const u32 n = c + 1;
+        if (n * HALF < bulk && (g ? hc1 : hc0) != n) {
+            if (((st >> g) & 1u) && !wait(g)) return;
+            issue(n, g);
+        }
+    }
+    __device__ __forceinline__ u32 word(u32 i)
+    {
+        const u32 o = 4u * i;
+        if (o < bulk && !(st & BROKEN)) {
+            const u32 c = o / HALF;
+            if (c != ready) make_ready(c);
+            if (!(st & BROKEN)) return *(const u32 *)(ring + (c & 1u) * HALF + (o & (HALF - 1u)));
+        }
+        return i < nwords ? __ldg(base + i) : 0u;
+    }
+    __device__ __forceinline__ u32 timeout() const { return (st & TIMEOUT) ? 1u : 0u; }
+    // every copy in flight completed, and the barrier phases kept for the
+    // warp's next member (called by the reading lane)
+    __device__ __forceinline__ void finish(WarpSmem<C> *sm)
+    {
+        for (u32 h = 0; h < 2; ++h)
+            if (((st >> h) & 1u) && !(st & BROKEN)) wait(h);
+        sm->phase = (st >> 2) & 3u;
+        sm->broken = (st & BROKEN) ? 1u : 0u;
+    }
+    __device__ __forceinline__ void seek(u32 p)
+    {
+        u32 a = p + bit0, w = a >> 5, sh = a & 31u;
+        const u32 lo = word(w), hi = word(w + 1); // in order: the staged reader moves forward
+        buf = (((u64)hi << 32) | lo) >> sh;
+        cnt = 64 - (int)sh;
+        nw = w + 2;
+    }
+    __device__ __forceinline__ void refill()
+    {
+        if (cnt <= 32) {
+            buf |= (u64)word(nw) << cnt;
+            cnt += 32;
+            ++nw;
+        }
+    }
+    __device__ __forceinline__ u32 tell() const { return nw * 32u - (u32)cnt - bit0; }
+    __device__ __forceinline__ u32 peek(int n) const { return (u32)buf & ((1u << n) - 1u); }
+    __device__ __forceinline__ void drop(int n)
+    {
+        buf >>= n;
+        cnt -= n;
+    }
+};
+
+// The reader a variant uses.
+template <class C> using Reader = typename std::conditional<(C::STAGE > 0), RingBits<C>, LaneBits>::type;
+
+// The staging barriers of a warp, set up once per launch by its lane 0.
+template <class C> __device__ __forceinline__ void stage_init(WarpSmem<C> *sm)
+{
+    if constexpr (C::STAGE > 0) {
+        if (lane_id() == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(sm->bar)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(sm->bar + 1)) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            sm->phase = 0;
+            sm->broken = 0;
+        }
+        __syncwarp();
+    }
+}
 
 // Pending-bit helpers over the window buffer.  Destinations of different
 // matches can share a word, hence the atomics.
@@ -423,7 +593,7 @@ template <class C> __device__ void write_window(const WarpSmem<C> *sm, u8 *out, 
 // followed by a second lookup without going round the loop (the buffer still
 // holds a root's worth of bits), as literals come in runs.
 template <class C>
-__device__ __forceinline__ void fast_run(WarpSmem<C> *sm, LaneBits &r, u32 pos, u32 lim, u32 &o_io, u32 &nq_io)
+__device__ __forceinline__ void fast_run(WarpSmem<C> *sm, Reader<C> &r, u32 pos, u32 lim, u32 &o_io, u32 &nq_io)
 {
     constexpr u32 LIT_MASK = C::LIT_MASK, DIST_MASK = C::DIST_MASK, DIST_BASE = C::DIST_BASE, MAXQ = C::MAXQ;
     u64 buf = r.buf;
@@ -481,7 +651,7 @@ __device__ __forceinline__ void fast_run(WarpSmem<C> *sm, LaneBits &r, u32 pos, 
 // in the order of the reference kernel.  Returns 0 to go on, 1 at the end of
 // the block, 2 on an error (status set).
 template <class C>
-__device__ __forceinline__ int slow_symbol(WarpSmem<C> *sm, LaneBits &r, u32 pos, u32 cap, u32 &o, u32 &nq, u32 &status)
+__device__ __forceinline__ int slow_symbol(WarpSmem<C> *sm, Reader<C> &r, u32 pos, u32 cap, u32 &o, u32 &nq, u32 &status)
 {
     constexpr int LIT_BITS = C::LIT_BITS, DIST_BITS = C::DIST_BITS;
     constexpr u32 LIT_MASK = C::LIT_MASK, DIST_MASK = C::DIST_MASK, DIST_BASE = C::DIST_BASE;
@@ -556,7 +726,7 @@ __device__ __forceinline__ int slow_symbol(WarpSmem<C> *sm, LaneBits &r, u32 pos
 // where a sequential decoder reports it.  Sets o (bytes), nq (matches),
 // status and eob.
 template <class C>
-__device__ __forceinline__ void decode_symbols(WarpSmem<C> *sm, LaneBits &r, u32 total, u32 pos, u32 cap, u32 &o,
+__device__ __forceinline__ void decode_symbols(WarpSmem<C> *sm, Reader<C> &r, u32 total, u32 pos, u32 cap, u32 &o,
                                                u32 &nq, u32 &status, int &eob)
 {
     constexpr u32 WB = C::WB, MAXQ = C::MAXQ;
@@ -583,7 +753,7 @@ __device__ __forceinline__ void decode_symbols(WarpSmem<C> *sm, LaneBits &r, u32
 // (decode_symbols); the warp then resolves the queued matches in parallel
 // rounds and writes the window to HBM with its CRC.
 template <class C>
-__device__ u32 decode_burst(WarpSmem<C> *sm, LaneBits &r, u32 total, u8 *out, u32 *pos_io, u32 cap, u32 *crc,
+__device__ u32 decode_burst(WarpSmem<C> *sm, Reader<C> &r, u32 total, u8 *out, u32 *pos_io, u32 cap, u32 *crc,
                             int *eob_out)
 {
     const u32 lane = lane_id();
@@ -611,7 +781,7 @@ __device__ u32 decode_burst(WarpSmem<C> *sm, LaneBits &r, u32 total, u8 *out, u3
 // placed at the first symbol (*huffman set).  *last is the block's BFINAL.
 // Returns the status; every output is warp-uniform.
 template <class C>
-__device__ __forceinline__ u32 block_header(WarpSmem<C> *sm, LaneBits &r, const u8 *in, u32 in_len, u8 *out, u32 cap, u32 &pos,
+__device__ __forceinline__ u32 block_header(WarpSmem<C> *sm, Reader<C> &r, const u8 *in, u32 in_len, u8 *out, u32 cap, u32 &pos,
                             u32 &crc, u32 &bitpos, int *last_out, bool *huffman, const u32 leader)
 {
     constexpr int LIT_BITS = C::LIT_BITS, DIST_BITS = C::DIST_BITS;
@@ -792,8 +962,8 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, W
 {
     constexpr u32 WB = C::WB;
     const u32 lane = lane_id();
-    LaneBits r;
-    r.attach(in, in_len);
+    Reader<C> r;
+    r.attach(in, in_len, sm);
     for (u32 w = lane; w < WB / 32; w += 32) sm->pend[w] = 0;
     __syncwarp();
     const u32 total = 8u * in_len;
@@ -819,6 +989,15 @@ __device__ u32 inflate_member_warp(const u8 *in, u32 in_len, u8 *out, u32 cap, W
         }
         if (last) break;
     }
+    if constexpr (C::STAGE > 0) {
+        u32 to = 0;
+        if (lane == 0) {
+            r.finish(sm);
+            to = r.timeout();
+        }
+        if (__shfl_sync(FRT_FULL_MASK, to, 0)) status = INF_STAGING_TIMEOUT;
+        __syncwarp();
+    }
     *produced_out = pos;
     *crc_out = crc;
     return status;
@@ -837,6 +1016,7 @@ k_inflate_members(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out, c
     WarpSmem<C> *wsm = (WarpSmem<C> *)(smem + warp * warp_smem_bytes<C>());
     u32 m = blockIdx.x * (blockDim.x / 32) + warp;
     if (m >= n) return;
+    stage_init<C>(wsm);
     u32 p = 0, c = 0;
     u32 st = inflate_member_warp<C>(in + in_off[m], in_len[m], out + out_off[m], out_cap[m], wsm, &p, &c);
     if (lane_id() == 0) {
@@ -864,6 +1044,7 @@ k_inflate_persistent(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out
     u64 n64 = *n_ptr;
     const u32 n = (u32)(n64 < n_cap ? n64 : n_cap);
     if (chunk == 0) chunk = 1;
+    stage_init<C>(wsm);
     while (true) {
         u32 base = 0;
         if (lane_id() == 0) base = atomicAdd(queue_head, chunk);
@@ -943,7 +1124,7 @@ __device__ void inflate_multi(unsigned char *wbase, const u8 *in, const u64 *in_
     constexpr u32 PW = C::WB / 32;
     for (u32 w = lane; w < K * PW; w += 32) sms[w / PW].pend[w % PW] = 0;
     if (lane < K) slots[lane].phase = SLOT_EMPTY;
-    LaneBits r; // lane s < K: the reader of slot s's member
+    Reader<C> r; // lane s < K: the reader of slot s's member
     bool more = true;
     __syncwarp();
     while (true) {
@@ -1146,13 +1327,14 @@ struct Variant {
 
 template <class C> Variant make_variant()
 {
-    return {{C::LIT_BITS, C::DIST_BITS, (int32_t)C::WB, (int32_t)C::MAXQ, C::REGS, 1, (uint64_t)warp_smem_bytes<C>()},
+    return {{C::LIT_BITS, C::DIST_BITS, (int32_t)C::WB, (int32_t)C::MAXQ, C::REGS, 1, (int32_t)C::STAGE,
+             (uint64_t)warp_smem_bytes<C>()},
             k_inflate_members<C>, k_inflate_persistent<C>};
 }
 
 template <class C, int K> Variant make_multi_variant()
 {
-    return {{C::LIT_BITS, C::DIST_BITS, (int32_t)C::WB, (int32_t)C::MAXQ, C::REGS, K,
+    return {{C::LIT_BITS, C::DIST_BITS, (int32_t)C::WB, (int32_t)C::MAXQ, C::REGS, K, (int32_t)C::STAGE,
              (uint64_t)multi_warp_bytes<C, K>()},
             k_inflate_members_multi<C, K>, k_inflate_persistent_multi<C, K>};
 }
@@ -1171,6 +1353,8 @@ const Variant kVariants[] = {
     make_variant<Cfg<9, 7, 1024, 192, 64>>(), make_variant<Cfg<9, 7, 1024, 160, 56>>(),
     // several chains per warp (the shared memory per warp is K members')
     make_multi_variant<Cfg<9, 7, 1024, 192, 128>, 2>(), make_multi_variant<Cfg<9, 7, 1024, 192, 128>, 4>(),
+    // compressed bytes staged in shared memory by bulk copies (ring halves of 256 bytes)
+    make_variant<Cfg<9, 7, 1024, 192, 64, 256>>(),
 };
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 

@@ -58,6 +58,7 @@ const char *inflate_status_message(uint32_t s)
     case 7: return "malformed Huffman table";
     case 8: return "invalid code-length repeat";
     case 9: return "code counts exceed the DEFLATE maximum";
+    case 10: return "a staging copy of the compressed member did not complete";
     default: return "unknown device error";
     }
 }

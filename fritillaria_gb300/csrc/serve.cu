@@ -118,7 +118,9 @@ struct frt_server {
     SharedStream *shared = nullptr;
     cudaStream_t stream = nullptr;
     uint64_t budget = 0, in_use = 0;
-    uint32_t max_batch = 0xffffffffu, max_ticks = 2;
+    // one tick in flight: a tick does not share the GPU with the one before
+    // it, which measured lower latency at the same request rate than two
+    uint32_t max_batch = 0xffffffffu, max_ticks = 1;
     uint8_t *files_arena = nullptr;
     uint64_t files_bytes = 0, files_cap = 0;
     std::vector<SrvFile> files;

@@ -321,6 +321,7 @@ uint32_t variant_set_hash()
         mix(info.queue);
         mix(info.max_registers);
         mix(info.chains);
+        mix(info.stage_half);
         mix((int64_t)info.smem_per_warp);
     }
     return h;
@@ -369,6 +370,7 @@ Json tuning_json(const frt_inflate_tuning &t, double ms, double gbs, uint64_t me
     j.set("ctas_per_sm", Json::number(t.ctas_per_sm));
     j.set("queue_chunk", Json::number(t.queue_chunk));
     j.set("chains", Json::number(info.chains));
+    j.set("stage_half", Json::number(info.stage_half));
     j.set("sample_members", Json::number((double)members));
     j.set("sample_ms", Json::number(ms));
     j.set("sample_gbs", Json::number(gbs));
@@ -395,12 +397,14 @@ bool tuning_from_json(const Json &j, frt_inflate_tuning *t)
         !num("lit_bits", &lb) || !num("dist_bits", &db) || !num("window", &win) || !num("queue", &qu) ||
         !num("max_registers", &mr))
         return false;
+    double sh = 0;
     num("chains", &ch); // entries written before multi-chain variants have one chain
+    num("stage_half", &sh);
     frt_inflate_variant info{};
     if (frt_inflate_variant_info((int32_t)v, &info, nullptr) != FRT_OK) return false;
     // the variant index must still name the same shape
     if (info.lit_bits != (int)lb || info.dist_bits != (int)db || info.window != (int)win || info.queue != (int)qu ||
-        info.max_registers != (int)mr || info.chains != (int)ch)
+        info.max_registers != (int)mr || info.chains != (int)ch || info.stage_half != (int)sh)
         return false;
     *t = frt_inflate_tuning{(int32_t)v, (int32_t)w, (int32_t)c, (int32_t)q};
     return true;

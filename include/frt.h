@@ -554,7 +554,8 @@ typedef struct {
  * bytes, scan scratch and results, held until released). */
 int frt_server_create(int device, void *stream, uint64_t budget_bytes, frt_server **out, frt_error *err);
 void frt_server_destroy(frt_server *s);
-/* 0 for either limit: no limit on requests per tick; 1 tick in flight. */
+/* Requests per tick and ticks in flight (by default: no limit, and one).
+ * 0 for either limit: no limit on requests per tick; 1 tick in flight. */
 void frt_server_set_limits(frt_server *s, uint32_t max_requests_per_tick, uint32_t max_ticks_in_flight);
 /* Milliseconds since the server was created (the clock of arrival_ms/done_ms). */
 double frt_server_clock_ms(const frt_server *s);
@@ -614,6 +615,8 @@ typedef struct {
     int32_t queue;          /* matches queued per window */
     int32_t max_registers;  /* register cap per thread */
     int32_t chains;         /* members a warp decodes side by side, one lane each */
+    int32_t stage_half;     /* 0: compressed bytes read through L1; else the bytes of each half of a
+                               shared-memory ring they are staged in by bulk copies */
     uint64_t smem_per_warp; /* shared memory per warp, bytes */
 } frt_inflate_variant;
 
