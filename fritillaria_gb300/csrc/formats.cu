@@ -138,23 +138,20 @@ __global__ void __launch_bounds__(TB) k_fq_nl_count(const u8 *buf, u64 lo, u64 h
 // `shift` bytes past a 16-byte boundary passes that boundary as `buf`.
 // lf[i] gets the byte after newline i (the first byte of the next line, 0
 // past the batch), so that line tests need no scattered byte reads.
-__global__ void __launch_bounds__(TB) k_fq_nl_emit(const u8 *buf, u64 lo, u64 hi, u64 tbase, bool aligned,
+__global__ void __launch_bounds__(TB, 6) k_fq_nl_emit(const u8 *buf, u64 lo, u64 hi, u64 tbase, bool aligned,
                                                    const u32 *tile_base, u64 *nl, u8 *lf, u64 shift)
 {
     __shared__ u32 s_warp[TB / 32];
     u64 p0 = tbase + (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
     u32 w[16];
     load64(buf, p0, lo, hi, aligned, w);
-    u32 m[16], c = 0;
+    u32 c = 0;
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-        m[k] = zero_bytes(w[k] ^ 0x0a0a0a0au);
-        c += __popc(m[k]);
-    }
+    for (int k = 0; k < 16; ++k) c += __popc(zero_bytes(w[k] ^ 0x0a0a0a0au));
     u32 at = tile_base[blockIdx.x] + block_excl_sum<u32>(c, s_warp, nullptr);
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-        u32 mk = m[k];
+        u32 mk = zero_bytes(w[k] ^ 0x0a0a0a0au); // again, rather than held across the scan
         while (mk) {
             const int b = (__ffs(mk) - 1) >> 3; // byte of the word
             const u32 next = b < 3 ? (w[k] >> (8 * (b + 1))) & 0xffu
@@ -1076,7 +1073,7 @@ __global__ void __launch_bounds__(1024) k_fa_apply(const u8 *tile_f, const u32 *
 // Pass 2: each tile's kept bytes, compacted in order through a shared-memory
 // staging buffer and written with coalesced stores, and each record's offset
 // and the offset of its first base.
-__global__ void __launch_bounds__(TB) k_fa_emit(const u8 *abuf, u64 sh, u64 len, const u8 *tile_state,
+__global__ void __launch_bounds__(TB, 6) k_fa_emit(const u8 *abuf, u64 sh, u64 len, const u8 *tile_state,
                                                 const u32 *contig_base, const u64 *out_base, u64 n_contigs, u8 *seq,
                                                 u64 *seq_off, u64 *rec_off)
 {
