@@ -134,12 +134,13 @@ __global__ void __launch_bounds__(TB) k_fq_nl_count(const u8 *buf, u64 lo, u64 h
     if (threadIdx.x == 0) tile_count[blockIdx.x] = tot;
 }
 
-// Positions in `buf` less `shift` are written: a caller whose batch starts
-// `shift` bytes past a 16-byte boundary passes that boundary as `buf`.
-// lf[i] gets the byte after newline i (the first byte of the next line, 0
-// past the batch), so that line tests need no scattered byte reads.
+// The newline positions, as offsets from `lo` (the scan's start, in buf's
+// coordinates: a caller whose batch starts some bytes past a 16-byte boundary
+// passes that boundary as `buf`).  lf[i] gets the byte after newline i (the
+// first byte of the next line, 0 past the batch), so that line tests need no
+// scattered byte reads.
 __global__ void __launch_bounds__(TB, 6) k_fq_nl_emit(const u8 *buf, u64 lo, u64 hi, u64 tbase, bool aligned,
-                                                   const u32 *tile_base, u64 *nl, u8 *lf, u64 shift)
+                                                   const u32 *tile_base, u32 *nl, u8 *lf)
 {
     __shared__ u32 s_warp[TB / 32];
     u64 p0 = tbase + (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
@@ -158,7 +159,7 @@ __global__ void __launch_bounds__(TB, 6) k_fq_nl_emit(const u8 *buf, u64 lo, u64
                                    : (k < 15 ? w[k + 1 < 16 ? k + 1 : 15] & 0xffu
                                              : (p0 + CH < hi ? (u32)buf[p0 + CH] : 0u));
             lf[at] = (u8)next;
-            nl[at++] = p0 + 4 * k + b - shift;
+            nl[at++] = (u32)(p0 + 4 * k + b - lo); // relative to the batch's start position
             mk &= mk - 1;
         }
     }
@@ -167,22 +168,23 @@ __global__ void __launch_bounds__(TB, 6) k_fq_nl_emit(const u8 *buf, u64 lo, u64
 struct FqIndex {
     const u8 *buf;
     u64 start, len;
-    const u64 *nl;
+    const u32 *nl; // newline positions less `start` (a batch spans less than 4 GiB from start)
     u32 n_nl, n_lines;
     const u8 *lf; // lf[i]: the byte after newline i
-    __device__ __forceinline__ u64 ls(u32 k) const { return k == 0 ? start : nl[k - 1] + 1; }
+    __device__ __forceinline__ u64 nlp(u32 i) const { return start + nl[i]; } // newline i's position
+    __device__ __forceinline__ u64 ls(u32 k) const { return k == 0 ? start : nlp(k - 1) + 1; }
     // the first byte of line k (a line that starts inside the batch)
     __device__ __forceinline__ u32 first(u32 k) const { return k == 0 ? buf[start] : lf[k - 1]; }
     // end of the record whose definition is line k (valid record assumed)
-    __device__ __forceinline__ u64 rec_end(u32 k) const { return k + 3 < n_nl ? nl[k + 3] + 1 : len; }
+    __device__ __forceinline__ u64 rec_end(u32 k) const { return k + 3 < n_nl ? nlp(k + 3) + 1 : len; }
     __device__ __forceinline__ bool blank(u32 k) const { return first(k) == '\n'; }
     // bounds_at (fastq record.rs:79-130) from the index
     __device__ __forceinline__ bool valid(u32 k) const
     {
         if (first(k) != '@' || k + 2 >= n_nl) return false;
         if (lf[k + 1] != '+') return false;
-        u64 seq_len = nl[k + 1] - nl[k] - 1;
-        u64 qs = nl[k + 2] + 1, qe = k + 3 < n_nl ? nl[k + 3] : len;
+        u64 seq_len = (u64)nl[k + 1] - nl[k] - 1;
+        u64 qs = nlp(k + 2) + 1, qe = k + 3 < n_nl ? nlp(k + 3) : len;
         return qe - qs == seq_len;
     }
 };
@@ -223,7 +225,7 @@ __global__ void k_tx_place(FqIndex ix, const u32 *is_rec, const u32 *rec_pos, co
     const u64 s = ix.ls(k);
     if (is_rec[k]) {
         rec_off[rec_pos[k]] = s;
-        rec_end[rec_pos[k]] = k < ix.n_nl ? ix.nl[k] : ix.len;
+        rec_end[rec_pos[k]] = k < ix.n_nl ? ix.nlp(k) : ix.len;
     }
     if (is_hdr[k]) hdr_off[hdr_pos[k]] = s;
 }
@@ -400,12 +402,12 @@ __global__ void k_fq_decode(FqIndex ix, const u32 *list, u32 n, u64 *rec_off, u3
     if (i >= n) return;
     u32 k = list[i];
     u64 p = ix.ls(k);
-    u64 qe = k + 3 < ix.n_nl ? ix.nl[k + 3] : ix.len;
+    u64 qe = k + 3 < ix.n_nl ? ix.nlp(k + 3) : ix.len;
     u64 e = qe < ix.len ? qe + 1 : qe;
     rec_off[i] = p;
-    seq_start[i] = (u32)(ix.nl[k] + 1 - p);
-    plus_start[i] = (u32)(ix.nl[k + 1] + 1 - p);
-    qual_start[i] = (u32)(ix.nl[k + 2] + 1 - p);
+    seq_start[i] = (u32)(ix.nlp(k) + 1 - p);
+    plus_start[i] = (u32)(ix.nlp(k + 1) + 1 - p);
+    qual_start[i] = (u32)(ix.nlp(k + 2) + 1 - p);
     seq_len[i] = (u32)(ix.nl[k + 1] - ix.nl[k] - 1);
     rec_end[i] = (u32)(e - p);
 }
@@ -1361,10 +1363,10 @@ extern "C" int frt_fastq_decode(frt_fastq_scanner *sc, const frt_inflate_batch *
     uint32_t hd[8] = {};
     if ((rc = read_back(st, d_u32, hd, sizeof hd, err, "newline count"))) return rc;
     const uint32_t n_nl = hd[0];
-    u64 *nl;
+    u32 *nl;
     u8 *lf;
     if ((rc = w.get(&nl, (size_t)n_nl + 1, err)) || (rc = w.get(&lf, (size_t)n_nl + 1, err))) return rc;
-    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, lf, sh);
+    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, lf);
     LAUNCH_OK("launching the newline index");
     // line starts: start, and one past every newline that is not the last byte
     const uint32_t n_lines = n_nl && hd[7] ? n_nl : n_nl + 1;
@@ -1950,10 +1952,10 @@ extern "C" int frt_text_scan(frt_text_scanner *sc, const frt_inflate_batch *b, u
     uint32_t hd[8] = {};
     if ((rc = read_back(st, d_u32, hd, sizeof hd, err, "newline count"))) return rc;
     const uint32_t n_nl = hd[0];
-    u64 *nl;
+    u32 *nl;
     u8 *lf;
     if ((rc = w.get(&nl, (size_t)n_nl + 1, err)) || (rc = w.get(&lf, (size_t)n_nl + 1, err))) return rc;
-    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, lf, sh);
+    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, lf);
     LAUNCH_OK("launching the newline index");
     // line starts: start, and one past every newline that is not the last byte
     const uint32_t n_lines = n_nl && hd[7] ? n_nl : n_nl + 1;
