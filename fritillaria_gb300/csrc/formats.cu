@@ -312,17 +312,24 @@ __global__ void k_tx_starts(const u32 *tab_base, u32 n1, u64 *starts)
     if (i < n1) starts[i] = tab_base[i];
 }
 
-__global__ void k_fq_lines(FqIndex ix, u32 *flags)
+// The valid record starts among each block's TB lines (counted), then, after
+// a scan of the counts, the same test again with each valid line written in
+// order: no per-line flag array is stored and re-read.
+__global__ void __launch_bounds__(TB) k_fq_lines_count(FqIndex ix, u32 *block_count)
 {
-    u32 k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= ix.n_lines) return;
-    flags[k] = ix.valid(k) ? 1u : 0u;
+    const u32 k = blockIdx.x * TB + threadIdx.x;
+    const int v = k < ix.n_lines && ix.valid(k);
+    const int n = __syncthreads_count(v);
+    if (threadIdx.x == 0) block_count[blockIdx.x] = (u32)n;
 }
 
-__global__ void k_fq_compact(const u32 *flags, const u32 *pos, u32 n_lines, u32 *S)
+__global__ void __launch_bounds__(TB) k_fq_lines_emit(FqIndex ix, const u32 *block_base, u32 *S)
 {
-    u32 k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n_lines && flags[k]) S[pos[k]] = k;
+    __shared__ u32 s_warp[TB / 32];
+    const u32 k = blockIdx.x * TB + threadIdx.x;
+    const u32 v = k < ix.n_lines && ix.valid(k) ? 1u : 0u;
+    const u32 r = block_excl_sum<u32>(v, s_warp, nullptr);
+    if (v) S[block_base[blockIdx.x] + r] = k;
 }
 
 // bit 0: the survivors do not tile (fastq.rs:585-598); bit 1: they are not the
@@ -343,7 +350,7 @@ __global__ void k_fq_check(FqIndex ix, const u32 *S, const u32 *n_s_dev, u32 *fa
 }
 
 // totals: n, tail, proof, survivors, use_walk_list
-__global__ void k_fq_finalize(FqIndex ix, const u32 *flags, const u32 *S, const u32 *n_s_dev, const u32 *fails,
+__global__ void k_fq_finalize(FqIndex ix, const u32 *S, const u32 *n_s_dev, const u32 *fails,
                               u32 *W, u64 *totals)
 {
     u32 n_s = *n_s_dev;
@@ -371,7 +378,7 @@ __global__ void k_fq_finalize(FqIndex ix, const u32 *flags, const u32 *S, const 
             u32 c = a, m = 0;
             tail = ix.len;
             while (c < ix.n_lines) {
-                if (!flags[c]) {
+                if (!ix.valid(c)) {
                     tail = ix.ls(c);
                     break;
                 }
@@ -1371,20 +1378,21 @@ extern "C" int frt_fastq_decode(frt_fastq_scanner *sc, const frt_inflate_batch *
     // line starts: start, and one past every newline that is not the last byte
     const uint32_t n_lines = n_nl && hd[7] ? n_nl : n_nl + 1;
     FqIndex ix{b->data, start, len, nl, n_nl, n_lines, lf};
-    u32 *flags, *pos, *S, *W, *fails;
-    if ((rc = w.get(&flags, n_lines, err)) || (rc = w.get(&pos, (size_t)n_lines + 1, err)) ||
+    const u32 n_blocks = grid_for(n_lines, TB);
+    u32 *bcount, *bbase, *S, *W, *fails;
+    if ((rc = w.get(&bcount, n_blocks, err)) || (rc = w.get(&bbase, (size_t)n_blocks + 1, err)) ||
         (rc = w.get(&fails, 4, err)))
         return rc;
     cudaMemsetAsync(fails, 0, 16, st);
-    k_fq_lines<<<grid_for(n_lines, 256), 256, 0, st>>>(ix, flags);
+    k_fq_lines_count<<<n_blocks, TB, 0, st>>>(ix, bcount);
     LAUNCH_OK("launching the line validation");
-    if ((e = frt_launch_scan_u32(flags, n_lines, partials, pos, d_u32, st)) != cudaSuccess)
+    if ((e = frt_launch_scan_u32(bcount, n_blocks, partials, bbase, d_u32, st)) != cudaSuccess)
         return cuda_fail(err, e, "scanning record starts");
     // the record starts are at most the lines: no read-back to size them
     if ((rc = w.get(&S, (size_t)n_lines + 1, err)) || (rc = w.get(&W, (size_t)n_lines + 1, err))) return rc;
-    k_fq_compact<<<grid_for(n_lines, 256), 256, 0, st>>>(flags, pos, n_lines, S);
+    k_fq_lines_emit<<<n_blocks, TB, 0, st>>>(ix, bbase, S);
     k_fq_check<<<grid_for(n_lines + 1, 256), 256, 0, st>>>(ix, S, d_u32, fails);
-    k_fq_finalize<<<1, 1, 0, st>>>(ix, flags, S, d_u32, fails, W, totals);
+    k_fq_finalize<<<1, 1, 0, st>>>(ix, S, d_u32, fails, W, totals);
     LAUNCH_OK("launching the tiling checks");
     uint64_t tot[5];
     if ((rc = read_back(st, totals, tot, sizeof tot, err, "FASTQ scan"))) return rc;
