@@ -919,9 +919,9 @@ uint64_t decode_launches(const frt_engine::File &f)
 {
     switch (f.desc.format) {
     case FRT_FORMAT_BAM: return 7;   // spec, reconcile, decode, 3-kernel scan, aux directory
-    case FRT_FORMAT_BCF: return 8;   // sieve x2, 3-kernel scan, check, finalize, decode
-    case FRT_FORMAT_FASTQ: return 13; // newline count/emit, 2 scans, lines, compact, check, finalize, decode
-    default: return 6;                // three passes, tile scan, scan64, lengths
+    case FRT_FORMAT_BCF: return 8;   // sieve, 3-kernel scan, gather, check, finalize, decode
+    case FRT_FORMAT_FASTQ: return 13; // newline slots, scan, gather, line count, scan, line emit, check, finalize, decode
+    default: return 6;                // sum, chunk scan, top, apply, emit, lengths
     }
 }
 

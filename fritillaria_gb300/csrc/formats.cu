@@ -116,52 +116,98 @@ __device__ __forceinline__ u32 byte_bits(u32 z) { return ((z >> 7) * 0x01020408u
 // FASTQ
 // =============================================================================
 
-// Newlines per tile; *last_nl (when given) says whether the byte before hi
-// is one, so that the caller knows the line count with the newline count.
-__global__ void __launch_bounds__(TB) k_fq_nl_count(const u8 *buf, u64 lo, u64 hi, u64 tbase, bool aligned,
-                                                    u32 *tile_count, u32 *last_nl)
-{
-    __shared__ u32 s_warp[TB / 32];
-    u64 p0 = tbase + (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
-    u32 w[16];
-    load64(buf, p0, lo, hi, aligned, w);
-    if (last_nl && hi > lo && hi - 1 >= p0 && hi - 1 < p0 + CH) *last_nl = buf[hi - 1] == '\n' ? 1u : 0u;
-    u32 c = 0;
-#pragma unroll
-    for (int k = 0; k < 16; ++k) c += __popc(zero_bytes(w[k] ^ 0x0a0a0a0au));
-    u32 tot;
-    block_excl_sum<u32>(c, s_warp, &tot);
-    if (threadIdx.x == 0) tile_count[blockIdx.x] = tot;
-}
+// The newline index, in one read of the bytes.  Pass 1 (k_nl_slots) counts
+// each tile's newlines and, when they fit the tile's NL_SLOT slots, stores
+// their offsets within the tile and the byte after each; pass 2 (k_nl_gather),
+// after a scan of the counts, copies the slots to their places, and only a
+// tile with more newlines than slots reads its bytes again.  Both passes take
+// `buf` at a 16-byte boundary at or before the scan's start `lo`; positions
+// are written as offsets from `lo`.
+constexpr u32 NL_SLOT = 1024; // a tile of 16 KiB averaging 16 bytes a line or more fits
 
-// The newline positions, as offsets from `lo` (the scan's start, in buf's
-// coordinates: a caller whose batch starts some bytes past a 16-byte boundary
-// passes that boundary as `buf`).  lf[i] gets the byte after newline i (the
-// first byte of the next line, 0 past the batch), so that line tests need no
-// scattered byte reads.
-__global__ void __launch_bounds__(TB, 6) k_fq_nl_emit(const u8 *buf, u64 lo, u64 hi, u64 tbase, bool aligned,
-                                                   const u32 *tile_base, u32 *nl, u8 *lf)
+// The newlines of one 64-byte chunk in order: nl[at..] gets their offsets from
+// `lo`, lf[at..] the byte after each (the first byte of the next line, 0 past
+// hi).  `pos` maps a chunk byte to what is stored.
+template <typename P, typename F>
+__device__ __forceinline__ void chunk_newlines(const u8 *buf, u64 p0, u64 hi, const u32 w[16], u32 at, P *nl,
+                                               u8 *lf, F pos)
 {
-    __shared__ u32 s_warp[TB / 32];
-    u64 p0 = tbase + (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
-    u32 w[16];
-    load64(buf, p0, lo, hi, aligned, w);
-    u32 c = 0;
-#pragma unroll
-    for (int k = 0; k < 16; ++k) c += __popc(zero_bytes(w[k] ^ 0x0a0a0a0au));
-    u32 at = tile_base[blockIdx.x] + block_excl_sum<u32>(c, s_warp, nullptr);
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-        u32 mk = zero_bytes(w[k] ^ 0x0a0a0a0au); // again, rather than held across the scan
+        u32 mk = zero_bytes(w[k] ^ 0x0a0a0a0au);
         while (mk) {
             const int b = (__ffs(mk) - 1) >> 3; // byte of the word
             const u32 next = b < 3 ? (w[k] >> (8 * (b + 1))) & 0xffu
                                    : (k < 15 ? w[k + 1 < 16 ? k + 1 : 15] & 0xffu
                                              : (p0 + CH < hi ? (u32)buf[p0 + CH] : 0u));
             lf[at] = (u8)next;
-            nl[at++] = (u32)(p0 + 4 * k + b - lo); // relative to the batch's start position
+            nl[at++] = pos(4 * k + b);
             mk &= mk - 1;
         }
+    }
+}
+
+__device__ __forceinline__ u32 chunk_count(const u32 w[16])
+{
+    u32 c = 0;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) c += __popc(zero_bytes(w[k] ^ 0x0a0a0a0au));
+    return c;
+}
+
+// Pass 1.  *last_nl (when given) says whether the byte before hi is a newline,
+// so that the caller knows the line count with the newline count.
+__global__ void __launch_bounds__(TB, 6) k_nl_slots(const u8 *buf, u64 lo, u64 hi, u64 tbase, u32 *tile_count,
+                                                  u16 *slot_pos, u8 *slot_lf, u32 *last_nl)
+{
+    __shared__ u32 s_warp[TB / 32];
+    const u32 r0 = threadIdx.x * CH; // the chunk's offset in the tile
+    const u64 p0 = tbase + (u64)blockIdx.x * TILE + r0;
+    u32 w[16];
+    load64(buf, p0, lo, hi, true, w);
+    if (last_nl && hi > lo && hi - 1 >= p0 && hi - 1 < p0 + CH) *last_nl = buf[hi - 1] == '\n' ? 1u : 0u;
+    u32 tot;
+    const u32 at = block_excl_sum<u32>(chunk_count(w), s_warp, &tot);
+    if (threadIdx.x == 0) tile_count[blockIdx.x] = tot;
+    if (tot > NL_SLOT) return; // the gather reads this tile's bytes again
+    chunk_newlines(buf, p0, hi, w, at, slot_pos + (u64)blockIdx.x * NL_SLOT, slot_lf + (u64)blockIdx.x * NL_SLOT,
+                   [r0](u32 j) { return (u16)(r0 + j); });
+}
+
+// Pass 2, a warp per tile: tile_base is the exclusive scan of tile_count.
+__global__ void __launch_bounds__(TB, 6) k_nl_gather(const u8 *buf, u64 lo, u64 hi, u64 tbase, u64 n_tiles,
+                                                   const u32 *tile_count, const u32 *tile_base,
+                                                   const u16 *slot_pos, const u8 *slot_lf, u32 *nl, u8 *lf)
+{
+    const u64 tile = (u64)blockIdx.x * (TB / 32) + (threadIdx.x >> 5);
+    const u32 lane = threadIdx.x & 31;
+    if (tile >= n_tiles) return;
+    const u32 n = tile_count[tile], base = tile_base[tile];
+    const u64 t0 = tbase + tile * TILE;
+    if (n <= NL_SLOT) {
+        const u16 *sp = slot_pos + tile * NL_SLOT;
+        const u8 *sl = slot_lf + tile * NL_SLOT;
+        for (u32 i = lane; i < n; i += 32) {
+            nl[base + i] = (u32)(t0 + sp[i] - lo); // every newline is at or past lo
+            lf[base + i] = sl[i];
+        }
+        return;
+    }
+    // a tile denser than its slots: its bytes again, 32 chunks at a time
+    u32 at = base;
+    for (u32 r = 0; r < TILE; r += 32 * CH) {
+        const u64 p0 = t0 + r + lane * CH;
+        u32 w[16];
+        load64(buf, p0, lo, hi, true, w);
+        const u32 c = chunk_count(w);
+        u32 x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 y = __shfl_up_sync(FRT_FULL_MASK, x, o);
+            if (lane >= (u32)o) x += y;
+        }
+        chunk_newlines(buf, p0, hi, w, at + x - c, nl, lf, [p0, lo](u32 j) { return (u32)(p0 + j - lo); });
+        at += __shfl_sync(FRT_FULL_MASK, x, 31);
     }
 }
 
@@ -315,21 +361,56 @@ __global__ void k_tx_starts(const u32 *tab_base, u32 n1, u64 *starts)
 // The valid record starts among each block's TB lines (counted), then, after
 // a scan of the counts, the same test again with each valid line written in
 // order: no per-line flag array is stored and re-read.
-__global__ void __launch_bounds__(TB) k_fq_lines_count(FqIndex ix, u32 *block_count)
+// The validity of lines k0..k0+3 as bits 0..3.  Away from the batch's ends
+// the index entries they need come in two 16-byte and two 4-byte loads.
+__device__ __forceinline__ u32 valid4(const FqIndex &ix, u32 k0)
 {
-    const u32 k = blockIdx.x * TB + threadIdx.x;
-    const int v = k < ix.n_lines && ix.valid(k);
-    const int n = __syncthreads_count(v);
-    if (threadIdx.x == 0) block_count[blockIdx.x] = (u32)n;
+    u32 v = 0;
+    if (k0 == 0 || (u64)k0 + 8 > ix.n_nl || (((uintptr_t)ix.nl | (uintptr_t)ix.lf) & 15)) {
+#pragma unroll
+        for (u32 j = 0; j < 4; ++j)
+            if (k0 + j < ix.n_lines && ix.valid(k0 + j)) v |= 1u << j;
+        return v;
+    }
+    const uint4 a = *reinterpret_cast<const uint4 *>(ix.nl + k0);
+    const uint4 b = *reinterpret_cast<const uint4 *>(ix.nl + k0 + 4);
+    const u32 n[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    const u32 f = *reinterpret_cast<const u32 *>(ix.lf + k0), g = *reinterpret_cast<const u32 *>(ix.lf + k0 + 4);
+    // L[j + 1] = lf[k0 + j]: the first byte of line k0 + j + 1
+    const u32 L[6] = {ix.lf[k0 - 1], f & 0xffu, (f >> 8) & 0xffu, (f >> 16) & 0xffu, f >> 24, g & 0xffu};
+#pragma unroll
+    for (u32 j = 0; j < 4; ++j) {
+        // line k: '@' first, '+' first two lines on, and a quality line as long as
+        // its sequence line (all four lines end inside the batch, k + 3 < n_nl)
+        const bool ok = L[j] == '@' && L[j + 2] == '+' && n[j + 3] - n[j + 2] == n[j + 1] - n[j];
+        v |= ok ? 1u << j : 0u;
+    }
+    return v;
 }
 
-__global__ void __launch_bounds__(TB) k_fq_lines_emit(FqIndex ix, const u32 *block_base, u32 *S)
+// Record starts, four lines a thread: each thread's four validity bits go
+// to vmask, and each block's count to block_count.
+__global__ void __launch_bounds__(TB) k_fq_lines_count(FqIndex ix, u8 *vmask, u32 *block_count)
 {
     __shared__ u32 s_warp[TB / 32];
-    const u32 k = blockIdx.x * TB + threadIdx.x;
-    const u32 v = k < ix.n_lines && ix.valid(k) ? 1u : 0u;
-    const u32 r = block_excl_sum<u32>(v, s_warp, nullptr);
-    if (v) S[block_base[blockIdx.x] + r] = k;
+    const u32 t = blockIdx.x * TB + threadIdx.x;
+    const u32 v = (u64)t * 4 < ix.n_lines ? valid4(ix, t * 4) : 0u;
+    if ((u64)t * 4 < ix.n_lines) vmask[t] = (u8)v;
+    u32 tot;
+    block_excl_sum<u32>(__popc(v), s_warp, &tot);
+    if (threadIdx.x == 0) block_count[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(TB) k_fq_lines_emit(FqIndex ix, const u8 *vmask, const u32 *block_base, u32 *S)
+{
+    __shared__ u32 s_warp[TB / 32];
+    const u32 t = blockIdx.x * TB + threadIdx.x;
+    u32 v = (u64)t * 4 < ix.n_lines ? vmask[t] : 0u;
+    u32 at = block_base[blockIdx.x] + block_excl_sum<u32>(__popc(v), s_warp, nullptr);
+    while (v) {
+        S[at++] = t * 4 + (__ffs(v) - 1);
+        v &= v - 1;
+    }
 }
 
 // bit 0: the survivors do not tile (fastq.rs:585-598); bit 1: they are not the
@@ -1161,7 +1242,37 @@ struct Scanner {
     cudaStream_t stream = nullptr;
     SharedStream *shared = nullptr;
     std::mutex mu;
+    // The newline index's tile slots (3 bytes per NL_SLOT per tile), kept
+    // from call to call and grown to the largest batch seen: calls on the
+    // scanner's stream run in order, so one array serves them all.
+    void *slots = nullptr;
+    size_t slots_bytes = 0;
 };
+
+int scanner_slots(Scanner &s, u64 n_tiles, u16 **pos, u8 **lf, frt_error *err)
+{
+    const size_t need = (size_t)n_tiles * NL_SLOT * 3 + 16;
+    if (need > s.slots_bytes) {
+        dev_free(s.slots, s.stream);
+        s.slots = nullptr;
+        s.slots_bytes = 0;
+        int rc = dev_alloc(&s.slots, need, s.stream, err);
+        if (rc) return rc;
+        s.slots_bytes = need;
+    }
+    *pos = (u16 *)s.slots;
+    *lf = (u8 *)s.slots + (size_t)n_tiles * NL_SLOT * 2;
+    return FRT_OK;
+}
+
+void scanner_release(Scanner &s)
+{
+    if (s.slots) {
+        DeviceGuardLite g(s.device);
+        dev_free(s.slots, s.stream);
+    }
+    stream_release(s.shared);
+}
 
 int scanner_create(int device, void *stream, Scanner *s, frt_error *err)
 {
@@ -1315,7 +1426,7 @@ extern "C" int frt_fastq_scanner_create(int device, void *stream, frt_fastq_scan
 extern "C" void frt_fastq_scanner_destroy(frt_fastq_scanner *s)
 {
     if (!s) return;
-    stream_release(s->s.shared);
+    scanner_release(s->s);
     delete s;
 }
 
@@ -1357,13 +1468,16 @@ extern "C" int frt_fastq_decode(frt_fastq_scanner *sc, const frt_inflate_batch *
     const u64 tbase = (start + sh) & ~15ull;
     const u64 n_tiles = (len + sh - tbase + TILE - 1) / TILE;
     u32 *tile_count, *tile_base, *partials, *d_u32;
+    u16 *slot_pos;
+    u8 *slot_lf;
     u64 *totals;
     if ((rc = w.get(&tile_count, n_tiles, err)) || (rc = w.get(&tile_base, n_tiles + 1, err)) ||
         (rc = w.get(&partials, frt_scan_partials_len(n_tiles) + frt_scan_partials_len(len) + 8, err)) ||
-        (rc = w.get(&d_u32, 8, err)) || (rc = w.get(&totals, 8, err)))
+        (rc = w.get(&d_u32, 8, err)) || (rc = w.get(&totals, 8, err)) ||
+        (rc = scanner_slots(s, n_tiles, &slot_pos, &slot_lf, err)))
         return rc;
-    k_fq_nl_count<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_count,
-                                                    d_u32 + 7);
+    k_nl_slots<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, tile_count, slot_pos, slot_lf,
+                                                 d_u32 + 7);
     LAUNCH_OK("launching the newline count");
     cudaError_t e = frt_launch_scan_u32(tile_count, n_tiles, partials, tile_base, d_u32, st);
     if (e != cudaSuccess) return cuda_fail(err, e, "scanning newline counts");
@@ -1373,24 +1487,27 @@ extern "C" int frt_fastq_decode(frt_fastq_scanner *sc, const frt_inflate_batch *
     u32 *nl;
     u8 *lf;
     if ((rc = w.get(&nl, (size_t)n_nl + 1, err)) || (rc = w.get(&lf, (size_t)n_nl + 1, err))) return rc;
-    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, lf);
+    k_nl_gather<<<(unsigned)((n_tiles + TB / 32 - 1) / (TB / 32)), TB, 0, st>>>(
+        abuf, start + sh, len + sh, tbase, n_tiles, tile_count, tile_base, slot_pos, slot_lf, nl, lf);
     LAUNCH_OK("launching the newline index");
     // line starts: start, and one past every newline that is not the last byte
     const uint32_t n_lines = n_nl && hd[7] ? n_nl : n_nl + 1;
     FqIndex ix{b->data, start, len, nl, n_nl, n_lines, lf};
-    const u32 n_blocks = grid_for(n_lines, TB);
+    const u64 n_quads = ((u64)n_lines + 3) / 4; // the validation takes four lines a thread
+    const u32 n_blocks = grid_for(n_quads, TB);
     u32 *bcount, *bbase, *S, *W, *fails;
+    u8 *vmask;
     if ((rc = w.get(&bcount, n_blocks, err)) || (rc = w.get(&bbase, (size_t)n_blocks + 1, err)) ||
-        (rc = w.get(&fails, 4, err)))
+        (rc = w.get(&fails, 4, err)) || (rc = w.get(&vmask, n_quads, err)))
         return rc;
     cudaMemsetAsync(fails, 0, 16, st);
-    k_fq_lines_count<<<n_blocks, TB, 0, st>>>(ix, bcount);
+    k_fq_lines_count<<<n_blocks, TB, 0, st>>>(ix, vmask, bcount);
     LAUNCH_OK("launching the line validation");
     if ((e = frt_launch_scan_u32(bcount, n_blocks, partials, bbase, d_u32, st)) != cudaSuccess)
         return cuda_fail(err, e, "scanning record starts");
     // the record starts are at most the lines: no read-back to size them
     if ((rc = w.get(&S, (size_t)n_lines + 1, err)) || (rc = w.get(&W, (size_t)n_lines + 1, err))) return rc;
-    k_fq_lines_emit<<<n_blocks, TB, 0, st>>>(ix, bbase, S);
+    k_fq_lines_emit<<<n_blocks, TB, 0, st>>>(ix, vmask, bbase, S);
     k_fq_check<<<grid_for(n_lines + 1, 256), 256, 0, st>>>(ix, S, d_u32, fails);
     k_fq_finalize<<<1, 1, 0, st>>>(ix, S, d_u32, fails, W, totals);
     LAUNCH_OK("launching the tiling checks");
@@ -1437,7 +1554,7 @@ extern "C" int frt_bcf_scanner_create(int device, void *stream, frt_bcf_scanner 
 extern "C" void frt_bcf_scanner_destroy(frt_bcf_scanner *s)
 {
     if (!s) return;
-    stream_release(s->s.shared);
+    scanner_release(s->s);
     delete s;
 }
 
@@ -1712,7 +1829,7 @@ extern "C" int frt_fasta_compactor_create(int device, void *stream, frt_fasta_co
 extern "C" void frt_fasta_compactor_destroy(frt_fasta_compactor *s)
 {
     if (!s) return;
-    stream_release(s->s.shared);
+    scanner_release(s->s);
     delete s;
 }
 
@@ -1889,7 +2006,7 @@ extern "C" int frt_text_scanner_create(int device, void *stream, frt_text_scanne
 extern "C" void frt_text_scanner_destroy(frt_text_scanner *s)
 {
     if (!s) return;
-    stream_release(s->s.shared);
+    scanner_release(s->s);
     delete s;
 }
 
@@ -1948,12 +2065,14 @@ extern "C" int frt_text_scan(frt_text_scanner *sc, const frt_inflate_batch *b, u
     const u64 tbase = (start + sh) & ~15ull;
     const u64 n_tiles = (len + sh - tbase + TILE - 1) / TILE;
     u32 *tile_count, *tile_base, *partials, *d_u32;
+    u16 *slot_pos;
+    u8 *slot_lf;
     if ((rc = w.get(&tile_count, n_tiles, err)) || (rc = w.get(&tile_base, n_tiles + 1, err)) ||
         (rc = w.get(&partials, frt_scan_partials_len(n_tiles) + frt_scan_partials_len(len) + 8, err)) ||
-        (rc = w.get(&d_u32, 8, err)))
+        (rc = w.get(&d_u32, 8, err)) || (rc = scanner_slots(s, n_tiles, &slot_pos, &slot_lf, err)))
         return rc;
-    k_fq_nl_count<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_count,
-                                                    d_u32 + 7);
+    k_nl_slots<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, tile_count, slot_pos, slot_lf,
+                                                 d_u32 + 7);
     LAUNCH_OK("launching the newline count");
     cudaError_t e = frt_launch_scan_u32(tile_count, n_tiles, partials, tile_base, d_u32, st);
     if (e != cudaSuccess) return cuda_fail(err, e, "scanning newline counts");
@@ -1963,7 +2082,8 @@ extern "C" int frt_text_scan(frt_text_scanner *sc, const frt_inflate_batch *b, u
     u32 *nl;
     u8 *lf;
     if ((rc = w.get(&nl, (size_t)n_nl + 1, err)) || (rc = w.get(&lf, (size_t)n_nl + 1, err))) return rc;
-    k_fq_nl_emit<<<(unsigned)n_tiles, TB, 0, st>>>(abuf, start + sh, len + sh, tbase, true, tile_base, nl, lf);
+    k_nl_gather<<<(unsigned)((n_tiles + TB / 32 - 1) / (TB / 32)), TB, 0, st>>>(
+        abuf, start + sh, len + sh, tbase, n_tiles, tile_count, tile_base, slot_pos, slot_lf, nl, lf);
     LAUNCH_OK("launching the newline index");
     // line starts: start, and one past every newline that is not the last byte
     const uint32_t n_lines = n_nl && hd[7] ? n_nl : n_nl + 1;

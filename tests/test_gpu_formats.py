@@ -86,6 +86,29 @@ def test_fastq_edge_cases(gpu, case):
         assert (proof, survivors) == (want["proof"], want["survivors"]), (case, start)
 
 
+def test_fastq_tiles_denser_than_the_index_slots(gpu):
+    """The newline index keeps up to 1,024 newlines of each 16 KiB tile from
+    its one read of the bytes; a denser tile (records of a few bytes, runs of
+    blank lines) is read again.  Dense and ordinary tiles side by side, at
+    starts on and off a tile."""
+    codec, scanner = gpu.CudaCodec(0), gpu.FastqScanner(0)
+    normal, _ = synth.fastq(400, seed=5)
+    normal = bytes(normal)
+    tiny = b"".join(_rec(b"", b"ACGT"[i % 4:i % 4 + 1]) for i in range(6000))  # 8 bytes, 4 newlines
+    n = len(normal)
+    cases = [(normal + tiny + normal + tiny + normal, (0, 3, n, n + 8000, 2 * n + len(tiny) + 40)),
+             (normal + tiny + b"\n" * 20000 + normal + tiny[:30001] + normal, (0, n + 16, 16384))]
+    for raw, starts in cases:
+        batch = device_batch(gpu, codec, raw)
+        for start in starts:
+            want = oracle.fastq_decode(raw, start)
+            cb = scanner.decode(batch, start)
+            for k in FQ:
+                assert np.array_equal(cb.column(k), want["columns"][k]), (start, k)
+            assert cb.tail() == want["tail"], start
+            assert cb.scan_info()[:2] == (want["proof"], want["survivors"]), start
+
+
 def test_fastq_empty_batch_decodes_to_an_empty_column_set(gpu):
     codec, scanner = gpu.CudaCodec(0), gpu.FastqScanner(0)
     raw, _ = synth.fastq(50, seed=2)

@@ -105,6 +105,19 @@ def test_edges(gpu, scanner):
     assert len(empty) == 0 and empty.tail() == 0
 
 
+def test_tiles_denser_than_the_index_slots(gpu, scanner):
+    """Tiles of 16 KiB with more than 1,024 newlines are read twice by the
+    newline index, the others once: runs of two-byte lines between ordinary
+    text."""
+    codec = gpu.CudaCodec(0)
+    dense = np.frombuffer(b"r\tx\n" * 9000 + b"\n" * 12000, np.uint8)
+    buf = np.concatenate([random_text(11, 800, False), dense, random_text(12, 800, False), dense[:20001],
+                          random_text(13, 300, True)])
+    batch = device_batch(gpu, codec, buf)
+    for start in (0, 7, 16384 + 3, buf.size // 2):
+        check(gpu, scanner, batch, buf, start, text.SAM)
+
+
 def test_a_batch_cut_mid_line_carries_the_line(gpu, scanner):
     buf = np.load(GOLDEN / "text_real.npz")["calls_vcf"]
     cut = buf[: buf.size // 2]
