@@ -940,13 +940,14 @@ __device__ __forceinline__ void fa_masks(const u8 *abuf, u64 lo, u64 hi, u64 p0,
 {
     load64(abuf, p0, lo, hi, true, w);
     u64 nl = 0, gt = 0;
-    u32 any_gt = 0;
+    u32 odd = 0; // bit 6 of a byte: clear in '\n' and '>', set in every letter
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-        nl |= (u64)byte_bits(zero_bytes(w[k] ^ 0x0a0a0a0au)) << (4 * k);
-        any_gt |= zero_bytes(w[k] ^ 0x3e3e3e3eu);
+        const u32 z = zero_bytes(w[k] ^ 0x0a0a0a0au);
+        nl |= (u64)byte_bits(z) << (4 * k);
+        odd |= (~w[k] & 0x40404040u) ^ (z >> 1); // bit 6 clear, not a newline
     }
-    if (any_gt) { // '>' is rare: its mask is built only where one occurs
+    if (odd) { // '>' is rare: its mask is built only where a byte might be one
 #pragma unroll
         for (int k = 0; k < 16; ++k) gt |= (u64)byte_bits(zero_bytes(w[k] ^ 0x3e3e3e3eu)) << (4 * k);
     }
@@ -1001,10 +1002,11 @@ __device__ __forceinline__ u64 fa_keep(const FaMasks &f, u32 s)
 // function, the record starts, and the bytes kept when the tile is entered in
 // each state (3 per tile); the position after the last record start goes to
 // *last_contig (batch coordinates, for the unterminated-header check).
-__global__ void __launch_bounds__(TB) k_fa_sum(const u8 *abuf, u64 sh, u64 len, u8 *tile_f, u32 *tile_contigs,
+__global__ void __launch_bounds__(TB, 8) k_fa_sum(const u8 *abuf, u64 sh, u64 len, u8 *tile_f, u32 *tile_contigs,
                                                u32 *tile_kept3, unsigned long long *last_contig)
 {
     __shared__ u32 s_warp[TB / 32];
+    __shared__ u64 s_w64[TB / 32];
     const u64 lo = sh, hi = len + sh;
     const u64 p0 = (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
     FaMasks m;
@@ -1016,15 +1018,18 @@ __global__ void __launch_bounds__(TB) k_fa_sum(const u8 *abuf, u64 sh, u64 len, 
 #pragma unroll
     for (u32 st = 0; st < 3; ++st) kept[st] = (u32)__popcll(fa_keep(m, st));
     const u32 ex = block_excl_compose(f, s_warp);
-    u32 tot;
-    block_excl_sum<u32>(k, s_warp, &tot);
+    // one sum of four 16-bit fields: the record starts (a tile holds at most
+    // 8,193: each but the first follows a newline) and the bytes kept (at
+    // most 16,384) for each state the tile can be entered in
+    const u64 packed = (u64)k | (u64)kept[f_apply(ex, 0)] << 16 | (u64)kept[f_apply(ex, 1)] << 32 |
+                       (u64)kept[f_apply(ex, 2)] << 48;
+    u64 tot;
+    block_excl_sum<u64>(packed, s_w64, &tot);
     if (threadIdx.x == TB - 1) tile_f[blockIdx.x] = (u8)f_then(ex, f);
-    if (threadIdx.x == 0) tile_contigs[blockIdx.x] = tot;
+    if (threadIdx.x == 0) {
+        tile_contigs[blockIdx.x] = (u32)(tot & 0xffffu);
 #pragma unroll
-    for (u32 st = 0; st < 3; ++st) {
-        u32 t3;
-        block_excl_sum<u32>(kept[f_apply(ex, st)], s_warp, &t3);
-        if (threadIdx.x == 0) tile_kept3[3 * blockIdx.x + st] = t3;
+        for (u32 st = 0; st < 3; ++st) tile_kept3[3 * blockIdx.x + st] = (u32)(tot >> (16 * (st + 1))) & 0xffffu;
     }
 }
 
@@ -1168,6 +1173,7 @@ __global__ void __launch_bounds__(TB, 6) k_fa_emit(const u8 *abuf, u64 sh, u64 l
                                                 u64 *seq_off, u64 *rec_off)
 {
     __shared__ u32 s_warp[TB / 32];
+    __shared__ u64 s_w64[TB / 32];
     __shared__ __align__(16) u8 s_out[TILE + 16];
     const u64 lo = sh, hi = len + sh;
     const u64 p0 = (u64)blockIdx.x * TILE + (u64)threadIdx.x * CH;
@@ -1178,9 +1184,11 @@ __global__ void __launch_bounds__(TB, 6) k_fa_emit(const u8 *abuf, u64 sh, u64 l
     const u32 ex = block_excl_compose(f, s_warp);
     const u32 st = f_apply(ex, tile_state[blockIdx.x]);
     const u64 keep = fa_keep(m, st);
-    u32 tile_total;
-    const u32 at = block_excl_sum<u32>((u32)__popcll(keep), s_warp, &tile_total);
-    u32 ci = contig_base[blockIdx.x] + block_excl_sum<u32>((u32)__popcll(m.hs), s_warp, nullptr);
+    // bytes kept (low half) and record starts (high half) in one scan
+    u64 tot2;
+    const u64 ex2 = block_excl_sum<u64>((u64)__popcll(keep) | (u64)__popcll(m.hs) << 32, s_w64, &tot2);
+    const u32 at = (u32)ex2, tile_total = (u32)tot2;
+    u32 ci = contig_base[blockIdx.x] + (u32)(ex2 >> 32);
     const u64 obase = out_base[blockIdx.x];
     // record starts (a few per tile at most)
     for (u64 h = m.hs; h; h &= h - 1) {
