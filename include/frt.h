@@ -292,7 +292,11 @@ typedef enum {
     FRT_FASTA_COL_COUNT = 4
 } frt_fasta_column;
 
-/* FastqScanner::new / with_context, crates/fritillaria-cuda/src/fastq.rs:53-84. */
+/* FastqScanner::new / with_context, crates/fritillaria-cuda/src/fastq.rs:53-84.
+ * The scanner keeps one device array from call to call: the newline index's
+ * tile slots, 3/16 of the largest batch it has scanned (3 bytes for each of
+ * 1,024 newlines per 16 KiB tile), freed by frt_fastq_scanner_destroy.  The
+ * text scanner keeps the same array. */
 int frt_fastq_scanner_create(int device, void *stream, frt_fastq_scanner **out, frt_error *err);
 void frt_fastq_scanner_destroy(frt_fastq_scanner *s);
 /* FastqScanner::decode(batch, start) (fastq.rs:117-140; scan, fastq.rs:94-110,

@@ -109,6 +109,21 @@ def test_fastq_tiles_denser_than_the_index_slots(gpu):
             assert cb.scan_info()[:2] == (want["proof"], want["survivors"]), start
 
 
+def test_fastq_scanner_reuses_and_grows_its_index_slots(gpu):
+    """One scanner over a one-tile batch, a batch of many tiles (its kept
+    slot array grows) and the one-tile batch again: each equals the oracle."""
+    codec, scanner = gpu.CudaCodec(0), gpu.FastqScanner(0)
+    small, _ = synth.fastq(20, seed=8)
+    big, _ = synth.fastq(6000, seed=9)
+    for raw in (bytes(small), bytes(big), bytes(small), bytes(big)[:500_001]):
+        batch = device_batch(gpu, codec, raw)
+        want = oracle.fastq_decode(raw, 0)
+        cb = scanner.decode(batch, 0)
+        for k in FQ:
+            assert np.array_equal(cb.column(k), want["columns"][k]), (len(raw), k)
+        assert cb.tail() == want["tail"]
+
+
 def test_fastq_empty_batch_decodes_to_an_empty_column_set(gpu):
     codec, scanner = gpu.CudaCodec(0), gpu.FastqScanner(0)
     raw, _ = synth.fastq(50, seed=2)
