@@ -591,7 +591,9 @@ template <class C> __device__ void write_window(const WarpSmem<C> *sm, u8 *out, 
 // exit test at the bottom of the loop, and the refill takes a word loaded
 // one refill earlier, so its load latency is off the chain.  A literal is
 // followed by a second lookup without going round the loop (the buffer still
-// holds a root's worth of bits), as literals come in runs.
+// holds a root's worth of bits), as literals come in runs.  A literal whose
+// code is longer than the root (rare byte values: 5% of the symbols of a
+// short-read BAM) is decoded in the loop too; any other long code leaves it.
 template <class C>
 __device__ __forceinline__ void fast_run(WarpSmem<C> *sm, Reader<C> &r, u32 pos, u32 lim, u32 &o_io, u32 &nq_io)
 {
@@ -637,6 +639,15 @@ __device__ __forceinline__ void fast_run(WarpSmem<C> *sm, Reader<C> &r, u32 pos,
                 ++nq;
                 o += len;
                 go = nq < MAXQ;
+            }
+        } else if ((e & 0xE0u) == 0xE0u) { // a code longer than the root: a literal is taken here
+            u32 sym;
+            const u32 L = decode_long(buf, C::LIT_BITS, &sm->lcode, sm->lsorted, &sym);
+            if (L != 0u && sym < 256u) {
+                sm->win[o++] = (u8)sym;
+                buf >>= L;
+                cnt -= (int)L;
+                go = true;
             }
         }
     } while (go && o < lim);
