@@ -1166,13 +1166,17 @@ def run_serving(args, rank, world, local):
     cap_rows = serve_stream(frt, srv, ids, [(0.0,) + r[1:] for r in reqs])
     capacity = latency_summary(cap_rows)
     capacity["ticks"] = tick_breakdown(srv.stats(reset=True))
-    # two ticks in flight (the server's default is one): a tick may start
-    # while the one before it still runs
+    # fewer ticks in flight than the server's default of four (each tick on
+    # its own stream): one, where a request waits for the running tick, and two
+    srv.set_limits(0, 1)
+    one_rows = serve_stream(frt, srv, ids, reqs)
+    one_tick = latency_summary(one_rows)
+    one_tick["ticks"] = tick_breakdown(srv.stats(reset=True))
     srv.set_limits(0, 2)
     two_rows = serve_stream(frt, srv, ids, reqs)
     two_ticks = latency_summary(two_rows)
     two_ticks["ticks"] = tick_breakdown(srv.stats(reset=True))
-    srv.set_limits(0, 1)
+    srv.set_limits(0, 4)
     # the plain per-request form: one request per tick, one tick in flight,
     # the same arrivals (a prefix of the stream: it cannot keep up)
     plain_srv = frt.RegionServer(0, budget_bytes=w["budget"])
@@ -1192,10 +1196,11 @@ def run_serving(args, rank, world, local):
                        "offered_req_per_s": w["rate"], "budget_bytes": w["budget"],
                        "l2": "region requests are independent (no flush)", "parallelism": f"replicas x{world}",
                        "tuning": tuning},
-            "serving": {"batched": batched, "capacity": capacity, "two_ticks_in_flight": two_ticks,
+            "serving": {"batched": batched, "capacity": capacity, "one_tick_in_flight": one_tick,
+                        "two_ticks_in_flight": two_ticks,
                         "plain_per_request": plain,
                         "note": "latency = device completion of the request's tick - arrival; batched = every queued "
-                                "request that fits the budget in a tick, one tick in flight; plain = one request "
+                                "request that fits the budget in a tick, four ticks in flight; plain = one request "
                                 "per tick, one tick in flight, on the first requests of the same stream"},
             "roofline": None, "cpu_baseline": None,
             "e2e": {"value": batched["gbs"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,

@@ -1268,7 +1268,9 @@ class RegionServer:
         _raise(lib().frt_server_create(device, stream, int(budget_bytes), C.byref(h), C.byref(err)), err)
         self._h = h
 
-    def set_limits(self, max_requests_per_tick: int = 0, max_ticks_in_flight: int = 1) -> None:
+    def set_limits(self, max_requests_per_tick: int = 0, max_ticks_in_flight: int = 4) -> None:
+        """Requests per tick (0: no limit) and ticks in flight (the server
+        starts with no limit and four; each tick in flight has its own stream)."""
         lib().frt_server_set_limits(self._h, max_requests_per_tick, max_ticks_in_flight)
 
     def stats(self, reset: bool = False) -> dict:

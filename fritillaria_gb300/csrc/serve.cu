@@ -118,9 +118,10 @@ struct frt_server {
     SharedStream *shared = nullptr;
     cudaStream_t stream = nullptr;
     uint64_t budget = 0, in_use = 0;
-    // one tick in flight: a tick does not share the GPU with the one before
-    // it, which measured lower latency at the same request rate than two
-    uint32_t max_batch = 0xffffffffu, max_ticks = 1;
+    // four ticks in flight, each on its own stream: a request that arrives
+    // while ticks run starts in a tick of its own at once, on SMs the running
+    // ticks leave idle (a small tick puts one member on each of few SMs)
+    uint32_t max_batch = 0xffffffffu, max_ticks = 4;
     uint8_t *files_arena = nullptr;
     uint64_t files_bytes = 0, files_cap = 0;
     std::vector<SrvFile> files;
@@ -133,6 +134,17 @@ struct frt_server {
     frt_codec *codec = nullptr;   // for reading BAM headers at add time
     frt_inflate_tuning tuning{};
     int inflate_grid = 0;
+    // A tick with fewer members than the tuned grid has warps is launched
+    // one warp per CTA, at most one CTA per member: the block scheduler then
+    // spreads the members over the SMs, and each decodes with its SM nearly
+    // to itself (the tuned CTAs would put eight of them on one SM).
+    frt_inflate_tuning spread{};
+    int spread_grid = 0;
+    // With more than one tick in flight each runs on a stream of its own
+    // (created on first use, as many as ticks in flight), so a new tick's
+    // kernels start on the SMs the running one leaves idle.
+    std::vector<cudaStream_t> tick_streams;
+    uint64_t tick_seq = 0;
     uint64_t pending = 0;         // submitted, not yet completed
     frt_server_stats stats{};     // per-stage totals over finished ticks
 };
@@ -231,8 +243,23 @@ int launch_tick(frt_server *sv, std::vector<SrvReq *> &batch, frt_error *err)
     const double h0 = host_ms(sv->t0);
     auto t = std::make_shared<Tick>();
     t->stream = sv->stream;
+    if (sv->max_ticks > 1) {
+        while (sv->tick_streams.size() < sv->max_ticks) {
+            cudaStream_t q = nullptr;
+            cudaError_t ce = cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking);
+            if (ce != cudaSuccess) return cuda_fail(err, ce, "creating a tick stream");
+            sv->tick_streams.push_back(q);
+        }
+        t->stream = sv->tick_streams[sv->tick_seq++ % sv->max_ticks];
+        // after everything already on the server's stream (file uploads, releases)
+        cudaEvent_t ready = nullptr;
+        cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+        cudaEventRecord(ready, sv->stream);
+        cudaStreamWaitEvent(t->stream, ready, 0);
+        cudaEventDestroy(ready);
+    }
     for (cudaEvent_t *ev : {&t->ev_start, &t->ev_inflate, &t->ev_inflated}) cudaEventCreate(ev);
-    cudaEventRecord(t->ev_start, sv->stream);
+    cudaEventRecord(t->ev_start, t->stream);
     Plan pl;
     for (uint32_t i = 0; i < batch.size(); ++i) plan_request(sv, *batch[i], i, pl, *t);
     const uint32_t n = (uint32_t)pl.in_off.size(), ns = (uint32_t)pl.segs.size();
@@ -274,7 +301,7 @@ int launch_tick(frt_server *sv, std::vector<SrvReq *> &batch, frt_error *err)
         (rc = talloc(*t, &t->cols.flags, rb, err)) || (rc = talloc(*t, &t->cols.mapq, rb, err)) ||
         (rc = talloc(*t, &t->cols.seq_len, rb, err)) || (rc = talloc(*t, &t->cols.request, rb, err)))
         return rc;
-    cudaStream_t st = sv->stream;
+    cudaStream_t st = t->stream;
     auto up = [&](void *dst, const void *src, size_t bytes) {
         return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st) : cudaSuccess;
     };
@@ -311,9 +338,13 @@ int launch_tick(frt_server *sv, std::vector<SrvReq *> &batch, frt_error *err)
         return cuda_fail(err, e, "uploading a tick");
     // inflate every member of the tick
     cudaEventRecord(t->ev_inflate, st);
+    const bool few = sv->spread_grid > 0 && n < (uint64_t)sv->inflate_grid * (uint64_t)sv->tuning.warps_per_cta;
+    const frt_inflate_tuning &lt = few ? sv->spread : sv->tuning;
+    const u32 grid =
+        few ? (u32)std::max<uint64_t>(1, std::min<uint64_t>(n, (uint64_t)sv->spread_grid)) : (u32)sv->inflate_grid;
     if ((e = frt_launch_inflate_persistent(sv->files_arena, in_off, in_len, t->arena, out_off, isize, crc, status,
                                            produced, crc_out, order, n_dev, n, pl.arena_bytes, (u32 *)queue_head,
-                                           (u32)sv->inflate_grid, block_err, sv->tuning, st)) != cudaSuccess)
+                                           grid, block_err, lt, st)) != cudaSuccess)
         return cuda_fail(err, e, "launching the inflate");
     cudaEventRecord(t->ev_inflated, st);
     int32_t n_ref = 0; // bounds refID in the record-start test
@@ -431,6 +462,9 @@ extern "C" int frt_server_create(int device, void *stream, uint64_t budget_bytes
     s->budget = budget_bytes;
     s->tuning = frt_inflate_default();
     s->inflate_grid = frt_inflate_persistent_grid(s->tuning);
+    s->spread = s->tuning;
+    s->spread.warps_per_cta = 1;
+    s->spread_grid = frt_inflate_persistent_grid(s->spread);
     s->t0 = std::chrono::steady_clock::now();
     cudaEventCreate(&s->origin);
     cudaEventRecord(s->origin, s->stream);
@@ -449,8 +483,13 @@ extern "C" void frt_server_destroy(frt_server *s)
     if (!s) return;
     DeviceGuardLite g(s->device);
     cudaStreamSynchronize(s->stream);
+    for (cudaStream_t q : s->tick_streams) cudaStreamSynchronize(q);
     s->running.clear();
     s->reqs.clear();
+    for (cudaStream_t q : s->tick_streams) {
+        cudaStreamSynchronize(q);
+        cudaStreamDestroy(q);
+    }
     for (auto &f : s->files) frt_bai_free(f.bai);
     if (s->files_arena) cudaFree(s->files_arena);
     frt_codec_destroy(s->codec);

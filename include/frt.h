@@ -558,8 +558,10 @@ typedef struct {
  * bytes, scan scratch and results, held until released). */
 int frt_server_create(int device, void *stream, uint64_t budget_bytes, frt_server **out, frt_error *err);
 void frt_server_destroy(frt_server *s);
-/* Requests per tick and ticks in flight (by default: no limit, and one).
- * 0 for either limit: no limit on requests per tick; 1 tick in flight. */
+/* Requests per tick and ticks in flight (by default: no limit, and four).
+ * 0 for either limit: no limit on requests per tick; 1 tick in flight.
+ * With more than one tick in flight each tick runs on a stream the server
+ * creates, so ticks overlap on the device. */
 void frt_server_set_limits(frt_server *s, uint32_t max_requests_per_tick, uint32_t max_ticks_in_flight);
 /* Milliseconds since the server was created (the clock of arrival_ms/done_ms). */
 double frt_server_clock_ms(const frt_server *s);

@@ -99,6 +99,28 @@ def test_same_alone_and_in_the_mix(gpu, files):
         _check(srv, rid, files, f, ref, s, e)
 
 
+def test_ticks_in_flight_on_their_own_streams(gpu, files):
+    """Three ticks in flight, each on a stream of its own, with requests
+    submitted while ticks run and results released as they are read: every
+    request equals the indexed query."""
+    srv, ids = _server(gpu, files)
+    srv.set_limits(4, 3)
+    regs = _regions(45, 13)
+    rids = []
+    for f, ref, s, e in regs:
+        rids.append(srv.submit(ids[f], ref, s, e))
+        srv.progress()
+    srv.drain()
+    for rid, reg in zip(rids, regs):
+        _check(srv, rid, files, *reg)
+        srv.release(rid)
+    # and back to one tick in flight on the same server
+    srv.set_limits(0, 1)
+    rid = srv.submit(ids[1], *regs[0][1:])
+    srv.drain()
+    _check(srv, rid, files, 1, *regs[0][1:])
+
+
 def test_small_budget_serves_everything(gpu, files):
     srv, ids = _server(gpu, files, budget=8 << 20)
     srv.set_limits(0, 1)
