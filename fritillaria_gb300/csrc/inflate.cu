@@ -29,6 +29,7 @@
 // reference kernel (crates/fritillaria-cuda/kernels/inflate.cu:78-458), so a
 // stream it rejects is rejected here with the same code.
 
+#include <atomic>
 #include <cstddef>
 #include <mutex>
 #include <type_traits>
@@ -1476,11 +1477,42 @@ extern "C" int frt_inflate_set_default_tuning(int device, const frt_inflate_tuni
     return FRT_OK;
 }
 
+namespace {
+// One-warp CTAs of each variant an SM holds (0: not yet asked), for spread launches.
+std::atomic<int> g_spread_ctas[kNumVariants];
+
+// A launch of n members that one wave of one-warp CTAs holds is made one warp
+// per CTA, one CTA per member at most: the block scheduler deals CTAs out to
+// the SMs evenly, while CTAs of w warps put w members on one SM and leave
+// other SMs idle.  A member's decode is a serial chain, so a small launch
+// ends with its slowest member: fewer members per SM shorten it.  Returns
+// false (t unchanged) where the launch fills the GPU anyway.
+bool spread_launch(frt_inflate_tuning &t, u64 n, u32 *grid)
+{
+    if (t.warps_per_cta <= 1 || kVariants[t.variant].info.chains != 1 || n == 0) return false;
+    int per_sm = g_spread_ctas[t.variant].load(std::memory_order_relaxed);
+    if (per_sm == 0) {
+        frt_inflate_tuning one{t.variant, 1, 0, 1};
+        per_sm = frt_inflate_ctas_per_sm(one);
+        g_spread_ctas[t.variant].store(per_sm > 0 ? per_sm : -1, std::memory_order_relaxed);
+    }
+    if (per_sm <= 0 || n > (u64)per_sm * (u64)sm_count()) return false;
+    t.warps_per_cta = 1;
+    t.ctas_per_sm = 0;
+    t.queue_chunk = 1;
+    *grid = (u32)n;
+    return true;
+}
+} // namespace
+
 cudaError_t frt_launch_inflate_members(const u8 *in, const u64 *in_off, const u32 *in_len, u8 *out,
                                        const u64 *out_off, const u32 *out_cap, u32 *status, u32 *produced,
-                                       u32 *crc, u32 n, const frt_inflate_tuning &t, cudaStream_t s)
+                                       u32 *crc, u32 n, const frt_inflate_tuning &tuned, cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
+    frt_inflate_tuning t = tuned;
+    u32 unused = 0;
+    spread_launch(t, n, &unused);
     const u32 w = (u32)t.warps_per_cta * (u32)kVariants[t.variant].info.chains; // members per CTA
     kVariants[t.variant].members<<<(n + w - 1) / w, t.warps_per_cta * 32, frt_inflate_smem_bytes(t), s>>>(
         in, in_off, in_len, out, out_off, out_cap, status, produced, crc, n);
@@ -1491,8 +1523,12 @@ cudaError_t frt_launch_inflate_persistent(const u8 *in, const u64 *in_off, const
                                           const u64 *out_off, const u32 *isize, const u32 *crc_expect, u32 *status,
                                           u32 *produced, u32 *crc, const u32 *order, const u64 *n_ptr, u64 n_cap,
                                           u64 out_capacity, u32 *queue_head, u32 grid, unsigned long long *block_err,
-                                          const frt_inflate_tuning &t, cudaStream_t s)
+                                          const frt_inflate_tuning &tuned, cudaStream_t s)
 {
+    // n_cap bounds the members (the device count may be lower): fewer than
+    // the tuned grid's warps gives a spread launch of n_cap one-warp CTAs
+    frt_inflate_tuning t = tuned;
+    if (n_cap < (u64)grid * (u64)tuned.warps_per_cta) spread_launch(t, n_cap, &grid);
     kVariants[t.variant].persistent<<<grid, t.warps_per_cta * 32, frt_inflate_smem_bytes(t), s>>>(
         in, in_off, in_len, out, out_off, isize, crc_expect, status, produced, crc, order, n_ptr, n_cap,
         out_capacity, queue_head, (u32)t.queue_chunk, block_err);

@@ -134,12 +134,6 @@ struct frt_server {
     frt_codec *codec = nullptr;   // for reading BAM headers at add time
     frt_inflate_tuning tuning{};
     int inflate_grid = 0;
-    // A tick with fewer members than the tuned grid has warps is launched
-    // one warp per CTA, at most one CTA per member: the block scheduler then
-    // spreads the members over the SMs, and each decodes with its SM nearly
-    // to itself (the tuned CTAs would put eight of them on one SM).
-    frt_inflate_tuning spread{};
-    int spread_grid = 0;
     // With more than one tick in flight each runs on a stream of its own
     // (created on first use, as many as ticks in flight), so a new tick's
     // kernels start on the SMs the running one leaves idle.
@@ -338,13 +332,11 @@ int launch_tick(frt_server *sv, std::vector<SrvReq *> &batch, frt_error *err)
         return cuda_fail(err, e, "uploading a tick");
     // inflate every member of the tick
     cudaEventRecord(t->ev_inflate, st);
-    const bool few = sv->spread_grid > 0 && n < (uint64_t)sv->inflate_grid * (uint64_t)sv->tuning.warps_per_cta;
-    const frt_inflate_tuning &lt = few ? sv->spread : sv->tuning;
-    const u32 grid =
-        few ? (u32)std::max<uint64_t>(1, std::min<uint64_t>(n, (uint64_t)sv->spread_grid)) : (u32)sv->inflate_grid;
+    // (a tick of fewer members than the tuned grid has warps is spread one
+    // warp per CTA over the SMs by the launcher)
     if ((e = frt_launch_inflate_persistent(sv->files_arena, in_off, in_len, t->arena, out_off, isize, crc, status,
                                            produced, crc_out, order, n_dev, n, pl.arena_bytes, (u32 *)queue_head,
-                                           grid, block_err, lt, st)) != cudaSuccess)
+                                           (u32)sv->inflate_grid, block_err, sv->tuning, st)) != cudaSuccess)
         return cuda_fail(err, e, "launching the inflate");
     cudaEventRecord(t->ev_inflated, st);
     int32_t n_ref = 0; // bounds refID in the record-start test
@@ -462,9 +454,6 @@ extern "C" int frt_server_create(int device, void *stream, uint64_t budget_bytes
     s->budget = budget_bytes;
     s->tuning = frt_inflate_default();
     s->inflate_grid = frt_inflate_persistent_grid(s->tuning);
-    s->spread = s->tuning;
-    s->spread.warps_per_cta = 1;
-    s->spread_grid = frt_inflate_persistent_grid(s->spread);
     s->t0 = std::chrono::steady_clock::now();
     cudaEventCreate(&s->origin);
     cudaEventRecord(s->origin, s->stream);
@@ -631,13 +620,17 @@ extern "C" int frt_server_progress(frt_server *s, uint32_t *completed, frt_error
     if (completed) *completed = 0;
     if (!s) return FRT_ERR_INVALID_ARGUMENT;
     DeviceGuardLite g(s->device);
-    // completions, in launch order
-    while (!s->running.empty()) {
-        cudaError_t q = cudaEventQuery(s->running.front()->done);
-        if (q == cudaErrorNotReady) break;
+    // completions, as they happen: ticks on streams of their own may finish
+    // out of launch order, and a finished tick frees its slot at once
+    for (auto it = s->running.begin(); it != s->running.end();) {
+        cudaError_t q = cudaEventQuery((*it)->done);
+        if (q == cudaErrorNotReady) {
+            ++it;
+            continue;
+        }
         if (q != cudaSuccess) return cuda_fail(err, q, "serving tick");
-        auto t = s->running.front();
-        s->running.pop_front();
+        auto t = *it;
+        it = s->running.erase(it);
         finish_tick(s, t, completed);
     }
     // admit and launch
