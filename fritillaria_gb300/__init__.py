@@ -139,9 +139,14 @@ class EngineConfig(C.Structure):
 
 class InflateTuning(C.Structure):
     """A tuning of the member inflate: a compiled variant, warps per CTA (one
-    member per warp), CTAs per SM (0: as many as fit), members per queue pop."""
+    member per warp), CTAs per SM (0: as many as fit), members per queue pop,
+    and the one-chain variant for small launches (-1: the same variant)."""
     _fields_ = [("variant", C.c_int32), ("warps_per_cta", C.c_int32), ("ctas_per_sm", C.c_int32),
-                ("queue_chunk", C.c_int32)]
+                ("queue_chunk", C.c_int32), ("spread_variant", C.c_int32)]
+
+    def __init__(self, variant: int = 0, warps_per_cta: int = 3, ctas_per_sm: int = 0, queue_chunk: int = 1,
+                 spread_variant: int = -1):
+        super().__init__(variant, warps_per_cta, ctas_per_sm, queue_chunk, spread_variant)
 
     def as_dict(self) -> dict:
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

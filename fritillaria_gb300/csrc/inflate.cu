@@ -1371,7 +1371,7 @@ const Variant kVariants[] = {
 constexpr int kNumVariants = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
 
 std::mutex g_tuning_mu;
-frt_inflate_tuning g_tuning = {0, 3, 0, 1};
+frt_inflate_tuning g_tuning = {0, 3, 0, 1, -1};
 
 int sm_count()
 {
@@ -1433,7 +1433,8 @@ cudaError_t frt_inflate_prepare()
 int frt_inflate_ctas_per_sm(const frt_inflate_tuning &t)
 {
     if (t.variant < 0 || t.variant >= kNumVariants || t.warps_per_cta < 1 || t.warps_per_cta > FRT_INFLATE_MAX_WARPS ||
-        t.ctas_per_sm < 0 || t.queue_chunk < 1 || t.queue_chunk > FRT_INFLATE_MAX_CHUNK)
+        t.ctas_per_sm < 0 || t.queue_chunk < 1 || t.queue_chunk > FRT_INFLATE_MAX_CHUNK || t.spread_variant < -1 ||
+        t.spread_variant >= kNumVariants || (t.spread_variant >= 0 && kVariants[t.spread_variant].info.chains != 1))
         return 0;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kVariants[t.variant].persistent, t.warps_per_cta * 32,
@@ -1489,14 +1490,17 @@ std::atomic<int> g_spread_ctas[kNumVariants];
 // false (t unchanged) where the launch fills the GPU anyway.
 bool spread_launch(frt_inflate_tuning &t, u64 n, u32 *grid)
 {
-    if (t.warps_per_cta <= 1 || kVariants[t.variant].info.chains != 1 || n == 0) return false;
-    int per_sm = g_spread_ctas[t.variant].load(std::memory_order_relaxed);
+    const int v = t.spread_variant >= 0 ? t.spread_variant : t.variant;
+    if (kVariants[v].info.chains != 1 || n == 0) return false;
+    if (t.warps_per_cta <= 1 && v == t.variant) return false;
+    int per_sm = g_spread_ctas[v].load(std::memory_order_relaxed);
     if (per_sm == 0) {
-        frt_inflate_tuning one{t.variant, 1, 0, 1};
+        frt_inflate_tuning one{v, 1, 0, 1, -1};
         per_sm = frt_inflate_ctas_per_sm(one);
-        g_spread_ctas[t.variant].store(per_sm > 0 ? per_sm : -1, std::memory_order_relaxed);
+        g_spread_ctas[v].store(per_sm > 0 ? per_sm : -1, std::memory_order_relaxed);
     }
     if (per_sm <= 0 || n > (u64)per_sm * (u64)sm_count()) return false;
+    t.variant = v;
     t.warps_per_cta = 1;
     t.ctas_per_sm = 0;
     t.queue_chunk = 1;

@@ -369,6 +369,7 @@ Json tuning_json(const frt_inflate_tuning &t, double ms, double gbs, uint64_t me
     j.set("warps_per_cta", Json::number(t.warps_per_cta));
     j.set("ctas_per_sm", Json::number(t.ctas_per_sm));
     j.set("queue_chunk", Json::number(t.queue_chunk));
+    j.set("spread_variant", Json::number(t.spread_variant));
     j.set("chains", Json::number(info.chains));
     j.set("stage_half", Json::number(info.stage_half));
     j.set("sample_members", Json::number((double)members));
@@ -406,8 +407,69 @@ bool tuning_from_json(const Json &j, frt_inflate_tuning *t)
     if (info.lit_bits != (int)lb || info.dist_bits != (int)db || info.window != (int)win || info.queue != (int)qu ||
         info.max_registers != (int)mr || info.chains != (int)ch || info.stage_half != (int)sh)
         return false;
-    *t = frt_inflate_tuning{(int32_t)v, (int32_t)w, (int32_t)c, (int32_t)q};
+    // the small-launch variant: absent in entries written before it was
+    // tuned (-1, and the caller times it), else a one-chain variant
+    double sv = -1;
+    num("spread_variant", &sv);
+    if (sv >= 0) {
+        frt_inflate_variant si{};
+        if (frt_inflate_variant_info((int32_t)sv, &si, nullptr) != FRT_OK || si.chains != 1) return false;
+    }
+    *t = frt_inflate_tuning{(int32_t)v, (int32_t)w, (int32_t)c, (int32_t)q, (int32_t)sv};
     return true;
+}
+
+// The variant for small launches (spread one warp per CTA): every one-chain
+// variant timed on a launch of one member per SM, the first members of the
+// bound input, where each member's serial chain bounds the launch.
+int pick_spread_variant(frt_engine *e, int device, uint64_t members, frt_inflate_tuning &t, frt_error *err)
+{
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const uint64_t few = members < (uint64_t)sms ? members : (uint64_t)sms;
+    t.spread_variant = -1;
+    if (few == 0) return FRT_OK;
+    double best = 0;
+    int best_v = -1;
+    for (int v = 0; v < frt_inflate_variant_count(); ++v) {
+        frt_inflate_variant vi{};
+        if (frt_inflate_variant_info(v, &vi, nullptr) != FRT_OK || vi.chains != 1) continue;
+        frt_inflate_tuning c = t;
+        c.spread_variant = v;
+        if (frt_inflate_tuning_ctas_per_sm(device, &c) < 1) continue;
+        double ms = 0;
+        uint64_t b = 0;
+        int r = frt_engine_time_inflate(e, &c, few, 3, &ms, &b, err);
+        if (r != FRT_OK) return r;
+        if (ms > 0 && (best == 0 || ms < best)) {
+            best = ms;
+            best_v = v;
+        }
+    }
+    t.spread_variant = best_v;
+    return FRT_OK;
+}
+
+// Writes the cache back (a temporary file renamed over the old one).
+int write_cache(Json &doc, const std::string &path, frt_error *err)
+{
+    doc.set("format", Json::string("fritillaria_gb300 inflate tuning"));
+    doc.set("version", Json::number(1));
+    std::string text;
+    write_json(doc, text, 0);
+    text.push_back('\n');
+    make_parents(path);
+    const std::string tmp = path + ".tmp." + std::to_string((long)getpid());
+    FILE *f = fopen(tmp.c_str(), "wb");
+    bool wrote = f && fwrite(text.data(), 1, text.size(), f) == text.size();
+    if (f) wrote = (fclose(f) == 0) && wrote;
+    if (!wrote || rename(tmp.c_str(), path.c_str()) != 0) {
+        unlink(tmp.c_str());
+        frt::set_error(err, FRT_ERR_IO, 0, 0, 0, 0, nullptr, "writing the tuning cache %s: %s", path.c_str(),
+                       strerror(errno));
+        return FRT_ERR_IO;
+    }
+    return FRT_OK;
 }
 
 } // namespace
@@ -451,6 +513,15 @@ extern "C" int frt_autotune(frt_engine *e, const char *cache_path, int32_t force
         const Json *hit = entries->get(key);
         if (hit && hit->kind == Json::Object && tuning_from_json(*hit, &best) &&
             frt_inflate_tuning_ctas_per_sm(device, &best) > 0) {
+            if (best.spread_variant < 0) {
+                // an entry from before the small-launch variant was tuned: time that alone
+                if ((rc = pick_spread_variant(e, device, st.members, best, err)) != FRT_OK) return rc;
+                Json *h = entries->get_mut(key);
+                h->set("spread_variant", Json::number(best.spread_variant));
+                if ((rc = write_cache(doc, path, err)) != FRT_OK) return rc;
+                entries = doc.get_mut("entries"); // the write may have grown the document
+                hit = entries->get(key);
+            }
             if ((rc = frt_engine_set_tuning(e, &best, err)) != FRT_OK) return rc;
             if ((rc = frt_inflate_set_default_tuning(device, &best, err)) != FRT_OK) return rc;
             out->tuning = best;
@@ -489,7 +560,7 @@ extern "C" int frt_autotune(frt_engine *e, const char *cache_path, int32_t force
     static const int widths[] = {2, 3, 4, 6, 8};
     for (int v = 0; v < frt_inflate_variant_count(); ++v)
         for (int w : widths) {
-            frt_inflate_tuning t{v, w, 0, 1};
+            frt_inflate_tuning t{v, w, 0, 1, -1};
             if (t.variant == cur.variant && t.warps_per_cta == cur.warps_per_cta && cur.ctas_per_sm == 0 &&
                 cur.queue_chunk == 1)
                 continue;
@@ -505,6 +576,7 @@ extern "C" int frt_autotune(frt_engine *e, const char *cache_path, int32_t force
         frt::set_error(err, FRT_ERR_CUDA, 0, 0, 0, 0, nullptr, "no inflate tuning could be timed on device %d", device);
         return FRT_ERR_CUDA;
     }
+    if ((rc = pick_spread_variant(e, device, st.members, best, err)) != FRT_OK) return rc;
     if ((rc = frt_engine_set_tuning(e, &best, err)) != FRT_OK) return rc;
     if ((rc = frt_inflate_set_default_tuning(device, &best, err)) != FRT_OK) return rc;
     out->tuning = best;
@@ -513,24 +585,7 @@ extern "C" int frt_autotune(frt_engine *e, const char *cache_path, int32_t force
     out->members = sample;
     out->candidates = timed;
 
-    // Write the cache back (a temporary file renamed over the old one).
-    doc.set("format", Json::string("fritillaria_gb300 inflate tuning"));
-    doc.set("version", Json::number(1));
     entries = doc.get_mut("entries");
     entries->set(key, tuning_json(best, best_ms, out->gbs, sample, timed));
-    std::string text;
-    write_json(doc, text, 0);
-    text.push_back('\n');
-    make_parents(path);
-    const std::string tmp = path + ".tmp." + std::to_string((long)getpid());
-    FILE *f = fopen(tmp.c_str(), "wb");
-    bool wrote = f && fwrite(text.data(), 1, text.size(), f) == text.size();
-    if (f) wrote = (fclose(f) == 0) && wrote;
-    if (!wrote || rename(tmp.c_str(), path.c_str()) != 0) {
-        unlink(tmp.c_str());
-        frt::set_error(err, FRT_ERR_IO, 0, 0, 0, 0, nullptr, "writing the tuning cache %s: %s", path.c_str(),
-                       strerror(errno));
-        return FRT_ERR_IO;
-    }
-    return FRT_OK;
+    return write_cache(doc, path, err);
 }

@@ -608,10 +608,14 @@ void frt_server_release(frt_server *s, uint64_t request);
  * bound input and caches the winner in a JSON file keyed by device, variant
  * set and workload class. */
 typedef struct {
-    int32_t variant;       /* index of a compiled variant */
-    int32_t warps_per_cta; /* 1..8; each warp takes the variant's chains of members */
-    int32_t ctas_per_sm;   /* 0: as many as fit */
-    int32_t queue_chunk;   /* members per queue pop, 1..64 */
+    int32_t variant;        /* index of a compiled variant */
+    int32_t warps_per_cta;  /* 1..8; each warp takes the variant's chains of members */
+    int32_t ctas_per_sm;    /* 0: as many as fit */
+    int32_t queue_chunk;    /* members per queue pop, 1..64 */
+    int32_t spread_variant; /* -1, or a one-chain variant for small launches: a launch of fewer members
+                               than one wave of one-warp CTAs holds is made one warp per CTA, and then
+                               each member's serial chain bounds it, so a variant with more registers
+                               and wider tables does better than the one tuned for throughput */
 } frt_inflate_tuning;
 
 typedef struct {

@@ -130,7 +130,7 @@ def test_inflate_variants_and_default_tuning():
         assert v["window"] % 32 == 0 and v["queue"] <= 1024 and v["smem_per_warp"] > v["window"]
         assert 32 <= v["max_registers"] <= 255
     t = frt.default_tuning().as_dict()
-    assert t == {"variant": 0, "warps_per_cta": 3, "ctas_per_sm": 0, "queue_chunk": 1}
+    assert t == {"variant": 0, "warps_per_cta": 3, "ctas_per_sm": 0, "queue_chunk": 1, "spread_variant": -1}
     with pytest.raises(frt.InvalidArgument):
         err = frt._Err()
         frt._raise(frt.lib().frt_inflate_variant_info(len(vs), frt.C.byref(frt.InflateVariant()), frt.C.byref(err)),

@@ -61,6 +61,28 @@ def test_every_variant_inflates_the_golden_members(frt):
                 assert got == g["member_sha256"][i], (t.as_dict(), case.stem, i)
 
 
+def test_small_launches_take_the_spread_variant(frt):
+    """A launch of fewer members than one wave of one-warp CTAs holds runs one
+    warp per CTA with the tuning's spread variant: every one-chain variant in
+    that role gives the golden members exactly, under a base variant of
+    another shape."""
+    cases = sorted(p for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("fields_", "text_")))
+    one_chain = [i for i, v in enumerate(frt.inflate_variants()) if v["chains"] == 1]
+    for sv in one_chain:
+        base = one_chain[(one_chain.index(sv) + 3) % len(one_chain)]
+        t = frt.InflateTuning(base, 4, 0, 2, spread_variant=sv)
+        frt.set_default_tuning(t)
+        codec = frt.CudaCodec(0)
+        for case in cases:
+            g = dict(np.load(case))
+            batch = codec.inflate_batch_device(g["bgzf"], _spans(frt, g))
+            data, offs = batch.to_host(), batch.offsets()
+            assert data.size == int(g["inflated_len"]), (t.as_dict(), case.stem)
+            for i in range(len(offs) - 1):
+                got = hashlib.sha256(data[offs[i]:offs[i + 1]].tobytes()).digest()
+                assert got == g["member_sha256"][i], (t.as_dict(), case.stem, i)
+
+
 @pytest.fixture(scope="module")
 def bam():
     raw, bgzf = synth.short_read_bam(12000, n_contigs=24, genome_len=3_100_000_000, seed=33, levels=(1, 6))
@@ -95,9 +117,11 @@ def test_invalid_tunings_are_refused(frt, bam):
     torch = pytest.importorskip("torch")
     eng, dev = _engine(frt, torch, bam[0])
     n = len(frt.inflate_variants())
+    multi = next(i for i, v in enumerate(frt.inflate_variants()) if v["chains"] > 1)
     for bad in (frt.InflateTuning(n, 3, 0, 1), frt.InflateTuning(-1, 3, 0, 1), frt.InflateTuning(0, 0, 0, 1),
                 frt.InflateTuning(0, 9, 0, 1), frt.InflateTuning(0, 3, 0, 0), frt.InflateTuning(0, 3, 0, 65),
-                frt.InflateTuning(0, 3, -1, 1)):
+                frt.InflateTuning(0, 3, -1, 1), frt.InflateTuning(0, 3, 0, 1, spread_variant=n),
+                frt.InflateTuning(0, 3, 0, 1, spread_variant=-2), frt.InflateTuning(0, 3, 0, 1, spread_variant=multi)):
         with pytest.raises(frt.InvalidArgument):
             eng.set_tuning(bad)
         with pytest.raises(frt.InvalidArgument):
@@ -142,8 +166,12 @@ def test_autotune_caches_and_reads_back(frt, bam, tmp_path):
     assert entry["queue_chunk"] == first["queue_chunk"]
     shape = frt.inflate_variants()[first["variant"]]
     assert (entry["lit_bits"], entry["window"]) == (shape["lit_bits"], shape["window"])
+    # the small-launch variant is a one-chain variant, timed and cached with the rest
+    assert first["spread_variant"] >= 0 and entry["spread_variant"] == first["spread_variant"]
+    assert frt.inflate_variants()[first["spread_variant"]]["chains"] == 1
     # the winner is the engine's tuning and the process default
-    assert eng.tuning.as_dict() == {k: first[k] for k in ("variant", "warps_per_cta", "ctas_per_sm", "queue_chunk")}
+    assert eng.tuning.as_dict() == {k: first[k] for k in ("variant", "warps_per_cta", "ctas_per_sm", "queue_chunk",
+                                                          "spread_variant")}
     assert frt.default_tuning().as_dict() == eng.tuning.as_dict()
     eng.run()
     st = eng.finish()
@@ -160,6 +188,12 @@ def test_autotune_caches_and_reads_back(frt, bam, tmp_path):
     assert not forced["from_cache"]
     doc2 = json.loads(cache.read_text())
     assert "another device|sm1" in doc2["entries"] and first["key"] in doc2["entries"]
+    # an entry without a small-launch variant is completed on a hit and written back
+    del doc2["entries"][first["key"]]["spread_variant"]
+    cache.write_text(json.dumps(doc2))
+    hit = eng2.autotune(cache)
+    assert hit["from_cache"] and hit["spread_variant"] >= 0
+    assert json.loads(cache.read_text())["entries"][first["key"]]["spread_variant"] == hit["spread_variant"]
     # a cache that names a variant of another shape is not trusted
     doc2["entries"][first["key"]]["lit_bits"] = 3
     cache.write_text(json.dumps(doc2))
