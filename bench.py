@@ -665,7 +665,7 @@ def run_ours(args, rank, world, local):
         if d.get("workload") == args.workload:
             traffic = d.get("traffic_bytes_per_launch")
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 5), "traffic": traffic,
+                "frac": round(achieved / peak, 5), "traffic": traffic, "issue": issue_model(frt, eng, inflated, inflate_ms) if args.workload.startswith("short_reads") else None,
                 "kernel": "k_inflate_persistent (persistent warp-per-member inflate + CRC32/ISIZE verify)",
                 "algorithmic_bytes_per_launch": inflate_bytes, "kernel_ms": round(inflate_ms, 3),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
@@ -1133,6 +1133,34 @@ def tick_breakdown(st: dict) -> dict:
             "members_per_tick": round(st["members"] / n, 1), "host_ms": round(st["host_ms"] / n, 3),
             "upload_and_wait_ms": round(st["upload_ms"] / n, 3), "inflate_ms": round(st["inflate_ms"] / n, 3),
             "scan_emit_ms": round(st["scan_ms"] / n, 3), "max_inflate_ms": st["max_inflate_ms"]}
+
+
+def issue_model(frt, eng, inflated: int, inflate_ms: float) -> dict | None:
+    """The inflate's second roofline: it is a serial Huffman chain per member,
+    so its bound is instruction issue, not HBM.  Warp instructions and DEFLATE
+    symbols per inflated byte come from the ncu capture and the symbol count in
+    profiles/inflate_issue.json; the issue peak is SMs x 4 schedulers x the SM
+    clock.  Also the chain model: warps in flight times each warp's symbol
+    rate, against one warp alone on an SM."""
+    ip = ROOT / "profiles" / "inflate_issue.json"
+    if not ip.exists() or inflate_ms <= 0:
+        return None
+    d = json.loads(ip.read_text())
+    per_byte = d["warp_instructions_per_launch"] / d["inflated_bytes_per_launch"]
+    sym_per_byte = d["deflate_symbols_per_launch"] / d["inflated_bytes_per_launch"]
+    secs = inflate_ms / 1e3
+    peak = d["sms"] * d["schedulers_per_sm"] * d["sm_clock_hz"]
+    instr = per_byte * inflated / secs
+    t = eng.tuning
+    warps = int(d["sms"]) * int(t.warps_per_cta) * max(1, frt.inflate_ctas_per_sm(t))
+    sym = sym_per_byte * inflated / secs
+    return {"achieved": round(instr / 1e12, 4), "peak": round(peak / 1e12, 4), "unit": "T warp instructions/s",
+            "frac": round(instr / peak, 4), "instructions_per_symbol": round(per_byte / sym_per_byte, 1),
+            "chain": {"warps_in_flight": warps, "symbols_per_s": round(sym / 1e9, 3),
+                      "per_warp_symbols_per_s": round(sym / warps / 1e6, 3),
+                      "lone_warp_symbols_per_s": round(d["lone_warp_symbols_per_s"] / 1e6, 3),
+                      "unit": "G symbols/s (total), M symbols/s (per warp)"},
+            "source": "profiles/inflate_issue.json (instructions and symbols per inflated byte of the 2M capture)"}
 
 
 def run_serving(args, rank, world, local):

@@ -1355,6 +1355,11 @@ def inflate_variants() -> list[dict]:
     return out
 
 
+def inflate_ctas_per_sm(tuning: InflateTuning, device: int = 0) -> int:
+    """CTAs of this tuning one SM holds (0: the tuning is invalid or does not fit)."""
+    return int(lib().frt_inflate_tuning_ctas_per_sm(device, C.byref(tuning)))
+
+
 def default_tuning() -> InflateTuning:
     t = InflateTuning()
     lib().frt_inflate_get_default_tuning(C.byref(t))

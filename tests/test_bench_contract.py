@@ -29,3 +29,30 @@ def test_reference_arm_prints_one_contract_line(capsys):
     assert d["config"]["records"] == 100_000
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] == "port" and d["value"] > 0
+
+
+def test_issue_model_of_the_inflate():
+    """The inflate's issue roofline from the committed capture record: at the
+    capture's own size and time it reproduces the capture's issue rate."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    rec = json.loads((ROOT / "profiles" / "inflate_issue.json").read_text())
+
+    class Tuning:
+        warps_per_cta = 4
+
+    class Eng:
+        tuning = Tuning()
+
+    class Frt:
+        @staticmethod
+        def inflate_ctas_per_sm(t):
+            return 8
+
+    m = bench.issue_model(Frt, Eng, rec["inflated_bytes_per_launch"], 15.83)
+    peak = rec["sms"] * rec["schedulers_per_sm"] * rec["sm_clock_hz"]
+    want = rec["warp_instructions_per_launch"] / 15.83e-3 / peak
+    assert abs(m["frac"] - want) < 1e-3 and 0.5 < m["frac"] < 1.0
+    assert m["chain"]["warps_in_flight"] == 152 * 4 * 8
+    assert 50 < m["instructions_per_symbol"] < 60
