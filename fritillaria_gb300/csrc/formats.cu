@@ -1353,10 +1353,16 @@ frt_columns *columns_new(const Scanner &s, int format, const size_t *widths, int
     return c;
 }
 
+// The extent of the column layout: the end of its last column, from the
+// offsets laid out by columns_new (a column whose bytes are set to 0 after,
+// as FASTA's bases in their own allocation, keeps its place in the layout).
 size_t columns_bytes(const frt_columns *c)
 {
     size_t t = 0;
-    for (int k = 0; k < c->n_cols; ++k) t += (c->col_bytes[k] + 255) & ~(size_t)255;
+    for (int k = 0; k < c->n_cols; ++k) {
+        const size_t end = c->col_off[k] + ((c->col_bytes[k] + 255) & ~(size_t)255);
+        if (end > t) t = end;
+    }
     return t;
 }
 

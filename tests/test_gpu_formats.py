@@ -281,6 +281,9 @@ EDGE_FASTA = {
     "crlf": b">a\r\nAC\r\nGT\r\n",
     "interior_blank": b">a\nACGT\n\nACGT\nAC\n",
     "gt_inside_header": b">a >b >c\nAAAA\n>d\nC\n",
+    # a record start every other byte: 8,192 in a 16 KiB tile, the most a tile's count holds
+    "dense_headers": b">\n" * 20000 + b">a\nACGT\n",
+    "tiny_records": b">x\nA\n" * 9000,
 }
 
 
