@@ -14,6 +14,10 @@ column, ending with the device error word read back and checked.
   cpu_baseline  the oracle's multithreaded restatement of the noodles CPU
           path (zlib inflate + CRC on all host cores, serial record scan,
           columns and aux walk)
+  roofline  the inflate kernel's HBM fraction (algorithmic bytes over its
+          CUDA-event time), and beside it, for short reads, its issue
+          roofline: warp instructions per second over the SMs' issue
+          capacity, with warps in flight and symbols per warp per second
 
 Inputs are seeded synthetic data (no dataset is available offline); the
 workload is larger than L2, so no flush is needed between steps.
